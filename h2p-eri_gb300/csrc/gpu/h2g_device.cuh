@@ -1,0 +1,96 @@
+/*
+ * Internal GPU data structures of the H2 apply (device representation of one
+ * struct H2ERI). Host-only declarations plus the tile descriptor shared with
+ * the kernels.
+ */
+#ifndef H2G_DEVICE_CUH
+#define H2G_DEVICE_CUH
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "h2eri_types.h"
+
+namespace h2g {
+
+/* Vector spaces a tile reads from / accumulates into. */
+enum VecKind : uint8_t {
+    VK_NONE = 0,
+    VK_X = 1,    /* matvec input x        [nvec][krnl_mat_size]  */
+    VK_Y = 2,    /* matvec output y       [nvec][krnl_mat_size]  */
+    VK_Y0 = 3,   /* upward coefficients   [nvec][rank_total]     */
+    VK_Y1 = 4,   /* downward coefficients [nvec][rank_total]     */
+    VK_T = 5,    /* low-rank scratch      [nvec][lr_total]       */
+    VK_COUNT = 6
+};
+
+/* One tile of one stored matrix (a U basis, a B or D block, or a factor of a
+ * low-rank block): rows [r0, r0+nr), columns [c0, c0+nc) of a row-major
+ * matrix with leading dimension ld. Two optional products:
+ *   N: out0[r] += sum_c A[r][c] * in0[c]
+ *   T: out1[c] += sum_r A[r][c] * in1[r]
+ * Offsets are element offsets (already shifted by r0 / c0) into the vector
+ * space named by the kind byte. */
+struct Tile {
+    uint64_t a;            /* element offset of A[r0][c0] in the arena */
+    int32_t ld;
+    int16_t nr, nc;
+    int32_t in0, out0, in1, out1;
+    uint8_t k_in0, k_out0, k_in1, k_out1;
+    int32_t pad;
+};
+static_assert(sizeof(Tile) == 40, "tile descriptor layout");
+
+constexpr int kTileRows = 64;
+constexpr int kTileCols = 128;
+constexpr int kTileThreads = 256;
+
+struct VecArgs {
+    double *base[VK_COUNT];
+    long long stride[VK_COUNT];
+};
+
+struct Range {
+    int first = 0, count = 0;
+};
+
+/* Device copy of one H2 representation plus the launch plan. */
+struct DevRep {
+    int device = -1;
+    /* fingerprint of the host structure this was built from */
+    int krnl = 0, n_node = 0, num_bf = 0, n_B = 0, n_D = 0;
+    const void *fp_U = nullptr, *fp_B = nullptr, *fp_D = nullptr;
+    /* blocks */
+    double *arena = nullptr;
+    size_t arena_elems = 0;
+    size_t bytes_U = 0, bytes_B = 0, bytes_D = 0;
+    /* plan */
+    Tile *tiles = nullptr;
+    int n_tiles = 0;
+    std::vector<Range> fwd;     /* deepest level first */
+    std::vector<Range> bwd;     /* shallowest level first */
+    Range mid1, mid2, den1, den2;
+    int rank_total = 0, lr_total = 0;
+    /* algorithmic bytes / flops of one matvec (per vector), for reports */
+    double alg_bytes_matrix = 0.0, alg_bytes_vec = 0.0, alg_flops = 0.0;
+    /* J assembly maps */
+    int *unc_map = nullptr;      /* krnl entries: (D index << 1) | off-diagonal flag */
+    int *con_map = nullptr;      /* num_bf^2 entries: (y index << 1) | diagonal flag, or -1 */
+    /* work space */
+    double *work = nullptr;      /* [Y0 | Y1 | T] regions, nvec_cap vectors each */
+    int nvec_cap = 0;
+    double *xbuf = nullptr, *ybuf = nullptr;   /* matvec staging, nvec_cap vectors */
+    double *dbuf = nullptr, *jbuf = nullptr;   /* density / J staging, nden_cap matrices */
+    int nden_cap = 0;
+    cudaStream_t s_main = nullptr, s_aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_t[8] = {nullptr};
+    float last_ms[5] = {0, 0, 0, 0, 0};   /* fwd, mid, bwd, den, total */
+    int precision = 0;
+};
+
+}  // namespace h2g
+
+#endif

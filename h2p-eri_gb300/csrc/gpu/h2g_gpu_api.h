@@ -1,0 +1,25 @@
+/* Internal cross-file interface of the GPU part (not exported). */
+#ifndef H2G_GPU_API_H
+#define H2G_GPU_API_H
+
+#include <string>
+#include <cuda_runtime.h>
+#include "h2eri_types.h"
+#include "h2g_device.cuh"
+
+namespace h2g {
+
+void set_error(const std::string &msg);
+/* device representation of h, uploaded on first use */
+int get_rep(H2ERI_p h, DevRep **out);
+/* y = A x on device vectors, enqueued on s */
+int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t s, bool timed);
+int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStream_t s, bool timed);
+/* exchange state attached to a representation */
+void free_exchange_state(DevRep *d);
+/* precision switch (mixed far-field arenas) */
+int set_precision_mode(DevRep *d, H2ERI_p h, int mode);
+
+}  // namespace h2g
+
+#endif

@@ -1,0 +1,777 @@
+/*
+ * GPU H2 apply: device representation, launch plan and the FP64 kernels of
+ * the hot path (H2P-ERI src/H2ERI_matvec.c:882-957 and
+ * src/H2ERI_build_Coulomb.c:26-152).
+ *
+ * Every stored matrix (nested basis U, coupling block B, near-field block D,
+ * or one factor of a low-rank B/D) is cut into 64 x 128 tiles. One CTA runs
+ * one tile and performs the products the reference does for that block:
+ *   upward sweep   (src/H2ERI_matvec.c:93-175)   T-product with U
+ *   B intermediate (src/H2ERI_matvec.c:299-407)  N and T products (bi-GEMV)
+ *   downward sweep (src/H2ERI_matvec.c:663-757)  N-product with U
+ *   near field     (src/H2ERI_matvec.c:572-660)  N (diagonal) or N and T
+ * Partial sums go to the output vectors with FP64 atomics, replacing the
+ * reference's per-thread copies and reductions. The children of a node keep
+ * their coefficient segments next to each other, so a non-leaf U reads or
+ * writes one contiguous slice. The near field depends only on x and runs on
+ * a second stream concurrently with the tree sweeps.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "h2eri_gb300.h"
+#include "h2g_device.cuh"
+#include "h2g_gpu_stats.h"
+#include "h2g_gpu_api.h"
+
+namespace h2g {
+
+/* ======================================================================== */
+/* Error state                                                               */
+/* ======================================================================== */
+
+static thread_local std::string t_last_error;
+
+void set_error(const std::string &msg) { t_last_error = msg; }
+
+#define CUDA_TRY(call)                                                                           \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+            return 10;                                                                           \
+        }                                                                                        \
+    } while (0)
+
+/* ======================================================================== */
+/* Kernels                                                                   */
+/* ======================================================================== */
+
+__device__ __forceinline__ double *vec_ptr(const VecArgs &va, uint8_t kind, int off, int v)
+{
+    return va.base[kind] + (long long)v * va.stride[kind] + off;
+}
+
+/* One CTA per (tile, vector). 8 warps; warp w owns rows 8w..8w+7 of the
+ * tile; lane l owns columns {2l, 2l+1, 64+2l, 65+2l}. All eight rows are
+ * loaded before any arithmetic so each warp keeps 8 KB of loads in flight. */
+__global__ void __launch_bounds__(kTileThreads)
+k_tile_f64(const Tile *__restrict__ tiles, const double *__restrict__ arena, VecArgs va)
+{
+    const Tile t = tiles[blockIdx.x];
+    const int v = blockIdx.y;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
+    const int nr = t.nr, nc = t.nc;
+    const double *__restrict__ A = arena + t.a;
+    const int cA = 2 * lane, cB = 64 + 2 * lane;
+    const bool okA = cA < nc, okB = cB < nc;
+
+    double xv[4] = {0.0, 0.0, 0.0, 0.0};
+    if (opN) {
+        const double *in0 = vec_ptr(va, t.k_in0, t.in0, v);
+        if (okA) { xv[0] = in0[cA]; if (cA + 1 < nc) xv[1] = in0[cA + 1]; }
+        if (okB) { xv[2] = in0[cB]; if (cB + 1 < nc) xv[3] = in0[cB + 1]; }
+    }
+    double a[8][4];
+    const int r0 = warp * 8;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int r = r0 + i;
+        double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
+        if (r < nr) {
+            const double *row = A + (size_t)r * t.ld;
+            if (okA) pa = __ldg(reinterpret_cast<const double2 *>(row + cA));
+            if (okB) pb = __ldg(reinterpret_cast<const double2 *>(row + cB));
+        }
+        a[i][0] = pa.x; a[i][1] = pa.y; a[i][2] = pb.x; a[i][3] = pb.y;
+    }
+    if (opN) {
+        double s[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) s[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
+        /* reduce 8 row sums across the warp by recursive halving */
+        const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            double send = b16 ? s[k] : s[k + 4];
+            double keep = b16 ? s[k + 4] : s[k];
+            s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            double send = b8 ? s[k] : s[k + 2];
+            double keep = b8 ? s[k + 2] : s[k];
+            s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+        double send = b4 ? s[0] : s[1];
+        double val = (b4 ? s[1] : s[0]) + __shfl_xor_sync(0xffffffffu, send, 4);
+        val += __shfl_xor_sync(0xffffffffu, val, 2);
+        val += __shfl_xor_sync(0xffffffffu, val, 1);
+        const int row = r0 + (b16 ? 4 : 0) + (b8 ? 2 : 0) + (b4 ? 1 : 0);
+        if ((lane & 3) == 0 && row < nr) atomicAdd(vec_ptr(va, t.k_out0, t.out0, v) + row, val);
+    }
+    if (opT) {
+        __shared__ double red[8][kTileCols];
+        const double *in1 = vec_ptr(va, t.k_in1, t.in1, v);
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int r = r0 + i;
+            const double x1 = (r < nr) ? in1[r] : 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[k] += a[i][k] * x1;
+        }
+        red[warp][cA] = acc[0]; red[warp][cA + 1] = acc[1];
+        red[warp][cB] = acc[2]; red[warp][cB + 1] = acc[3];
+        __syncthreads();
+        double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
+        for (int c = threadIdx.x; c < nc; c += kTileThreads) {
+            double s = 0.0;
+#pragma unroll
+            for (int w = 0; w < 8; w++) s += red[w][c];
+            atomicAdd(out1 + c, s);
+        }
+    }
+}
+
+/* x[v][i] = c_i * D[v][map_i >> 1], c_i = 2 for off-diagonal shell pairs
+ * (src/H2ERI_build_Coulomb.c:26-62). */
+__global__ void k_uncontract(const int *__restrict__ map, int n, const double *__restrict__ den,
+                             long long den_stride, double *__restrict__ x, long long x_stride)
+{
+    const int v = blockIdx.y;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int m = map[i];
+        double d = den[v * den_stride + (m >> 1)];
+        x[v * x_stride + i] = (m & 1) ? 2.0 * d : d;
+    }
+}
+
+/* J[a][b] = T[a][b] + T[b][a], T[a][b] = c * y[map >> 1] (c = 0.5 on
+ * diagonal shell pairs) or 0 (src/H2ERI_build_Coulomb.c:78-133). */
+__global__ void k_contract(const int *__restrict__ map, int nbf, const double *__restrict__ y,
+                           long long y_stride, double *__restrict__ J, long long J_stride)
+{
+    const int v = blockIdx.y;
+    const long long n2 = (long long)nbf * nbf;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x) {
+        int a = (int)(i / nbf), b = (int)(i - (long long)a * nbf);
+        int m1 = map[i], m2 = map[(long long)b * nbf + a];
+        double s = 0.0;
+        if (m1 >= 0) s += (m1 & 1) ? 0.5 * y[v * y_stride + (m1 >> 1)] : y[v * y_stride + (m1 >> 1)];
+        if (m2 >= 0) s += (m2 & 1) ? 0.5 * y[v * y_stride + (m2 >> 1)] : y[v * y_stride + (m2 >> 1)];
+        J[v * J_stride + i] = s;
+    }
+}
+
+/* ======================================================================== */
+/* Upload and plan                                                           */
+/* ======================================================================== */
+
+static std::mutex g_mu;
+static std::unordered_map<const void *, DevRep *> g_reps;
+
+namespace {
+
+struct Packer {
+    std::vector<double> host;
+    size_t alloc(size_t elems)
+    {
+        size_t off = (host.size() + 3) & ~size_t(3);      /* 32-byte aligned blocks */
+        host.resize(off + elems, 0.0);
+        return off;
+    }
+    /* copy a row-major nrow x ncol matrix (source leading dimension lds) into a
+     * fresh region with an even leading dimension; returns offset and ld */
+    size_t put(const double *src, int nrow, int ncol, int lds, int &ld)
+    {
+        ld = (ncol + 1) & ~1;
+        size_t off = alloc((size_t)nrow * ld);
+        for (int r = 0; r < nrow; r++)
+            std::memcpy(host.data() + off + (size_t)r * ld, src + (size_t)r * lds, sizeof(double) * ncol);
+        return off;
+    }
+};
+
+struct Planner {
+    std::vector<Tile> tiles;
+    void add(size_t a, int ld, int nrow, int ncol, uint8_t kin0, int in0, uint8_t kout0, int out0,
+             uint8_t kin1, int in1, uint8_t kout1, int out1)
+    {
+        for (int r0 = 0; r0 < nrow; r0 += kTileRows)
+            for (int c0 = 0; c0 < ncol; c0 += kTileCols) {
+                Tile t;
+                std::memset(&t, 0, sizeof(t));
+                t.a = a + (size_t)r0 * ld + c0;
+                t.ld = ld;
+                t.nr = (int16_t)std::min(kTileRows, nrow - r0);
+                t.nc = (int16_t)std::min(kTileCols, ncol - c0);
+                if (kout0 != VK_NONE) { t.k_in0 = kin0; t.in0 = in0 + c0; t.k_out0 = kout0; t.out0 = out0 + r0; }
+                if (kout1 != VK_NONE) { t.k_in1 = kin1; t.in1 = in1 + r0; t.k_out1 = kout1; t.out1 = out1 + c0; }
+                tiles.push_back(t);
+            }
+    }
+};
+
+/* A stored B/D block in the arena, dense or low-rank. */
+struct BlockLoc {
+    bool lowrank = false;
+    int nrow = 0, ncol = 0, rank = 0;
+    size_t a = 0, u = 0, vt = 0;   /* dense data, or U and V^T factors */
+    int ld = 0, ldu = 0, ldv = 0;
+    int t_off = 0, s_off = 0;      /* scratch for V x_in0 and U^T x_in1 */
+};
+
+BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total)
+{
+    BlockLoc b;
+    b.nrow = m->nrow;
+    b.ncol = m->ncol;
+    if (m->ld < 0) {
+        b.lowrank = true;
+        b.rank = -m->ld;
+        b.u = pk.put(m->data, b.nrow, b.rank, b.rank, b.ldu);
+        b.vt = pk.put(m->data + (size_t)b.nrow * b.rank, b.ncol, b.rank, b.rank, b.ldv);
+        b.t_off = lr_total;
+        b.s_off = lr_total + b.rank;
+        lr_total += 2 * b.rank;
+    } else if ((size_t)b.nrow * b.ncol > 0) {
+        b.a = pk.put(m->data, b.nrow, b.ncol, m->ld, b.ld);
+    }
+    return b;
+}
+
+/* Products of one block: N-side (out0 += A in0) and T-side (out1 += A^T in1);
+ * kinds VK_NONE disable a side. Low-rank blocks use two stages. */
+void plan_block(Planner &stage1, Planner &stage2, const BlockLoc &b, uint8_t kin0, int in0, uint8_t kout0,
+                int out0, uint8_t kin1, int in1, uint8_t kout1, int out1)
+{
+    if (b.nrow == 0 || b.ncol == 0) return;
+    if (!b.lowrank) {
+        stage1.add(b.a, b.ld, b.nrow, b.ncol, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
+        return;
+    }
+    if (b.rank == 0) return;
+    if (kout0 != VK_NONE) {
+        /* t = V in0 = (V^T)^T in0 ; out0 += U t */
+        stage1.add(b.vt, b.ldv, b.ncol, b.rank, VK_NONE, 0, VK_NONE, 0, kin0, in0, VK_T, b.t_off);
+        stage2.add(b.u, b.ldu, b.nrow, b.rank, VK_T, b.t_off, kout0, out0, VK_NONE, 0, VK_NONE, 0);
+    }
+    if (kout1 != VK_NONE) {
+        /* s = U^T in1 ; out1 += V^T s */
+        stage1.add(b.u, b.ldu, b.nrow, b.rank, VK_NONE, 0, VK_NONE, 0, kin1, in1, VK_T, b.s_off);
+        stage2.add(b.vt, b.ldv, b.ncol, b.rank, VK_T, b.s_off, kout1, out1, VK_NONE, 0, VK_NONE, 0);
+    }
+}
+
+double block_elems(const BlockLoc &b)
+{
+    return b.lowrank ? (double)(b.nrow + b.ncol) * b.rank : (double)b.nrow * b.ncol;
+}
+
+}  // namespace
+
+static void free_rep(DevRep *d)
+{
+    if (d == nullptr) return;
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (d->device >= 0) cudaSetDevice(d->device);
+    cudaFree(d->arena);
+    cudaFree(d->tiles);
+    cudaFree(d->unc_map);
+    cudaFree(d->con_map);
+    cudaFree(d->work);
+    cudaFree(d->xbuf);
+    cudaFree(d->ybuf);
+    cudaFree(d->dbuf);
+    cudaFree(d->jbuf);
+    if (d->s_main) cudaStreamDestroy(d->s_main);
+    if (d->s_aux) cudaStreamDestroy(d->s_aux);
+    if (d->ev_fork) cudaEventDestroy(d->ev_fork);
+    if (d->ev_join) cudaEventDestroy(d->ev_join);
+    for (auto &e : d->ev_t)
+        if (e) cudaEventDestroy(e);
+    free_exchange_state(d);
+    if (cur >= 0) cudaSetDevice(cur);
+    delete d;
+}
+
+static int build_rep(H2ERI_p h, DevRep *d)
+{
+    if (h->U == nullptr || h->c_D_blks == nullptr || (h->n_B > 0 && h->c_B_blks == nullptr)) {
+        set_error("H2 representation not built (call H2ERI_build_H2 with BD_JIT = 0)");
+        return 2;
+    }
+    const int n_node = h->n_node, krnl = h->krnl_mat_size;
+    Packer pk;
+    pk.host.reserve((size_t)(h->mat_size[U_SIZE_IDX] + h->mat_size[B_SIZE_IDX] + h->mat_size[D_SIZE_IDX]) + 4096);
+
+    /* coefficient segments: children of a node are contiguous, in child order */
+    std::vector<int> voff(n_node, -1), rank(n_node, 0);
+    for (int i = 0; i < n_node; i++) rank[i] = h->U[i]->ncol;
+    int rtot = 0;
+    voff[h->root_idx] = rtot;
+    rtot += rank[h->root_idx];
+    for (int lv = 0; lv <= h->max_level; lv++)
+        for (int j = 0; j < h->level_n_node[lv]; j++) {
+            int node = h->level_nodes[lv * h->n_leaf_node + j];
+            for (int k = 0; k < h->n_child[node]; k++) {
+                int c = h->children[node * h->max_child + k];
+                voff[c] = rtot;
+                rtot += rank[c];
+            }
+        }
+    d->rank_total = rtot;
+
+    /* which upward / downward coefficients are ever non-zero */
+    std::vector<char> used_y0(n_node, 0), wrote_y1(n_node, 0);
+    for (int i = 0; i < h->n_r_adm_pair; i++) {
+        int n0 = h->r_adm_pairs[2 * i], n1 = h->r_adm_pairs[2 * i + 1];
+        int l0 = h->node_level[n0], l1 = h->node_level[n1];
+        if (l0 >= l1) { used_y0[n0] = 1; wrote_y1[n0] = 1; }
+        if (l0 <= l1) { used_y0[n1] = 1; wrote_y1[n1] = 1; }
+    }
+    std::vector<char> need_up(n_node, 0), need_down(n_node, 0);
+    for (int lv = h->min_adm_level; lv <= h->max_level; lv++)
+        for (int j = 0; j < h->level_n_node[lv]; j++) {
+            int node = h->level_nodes[lv * h->n_leaf_node + j];
+            int p = h->parent[node];
+            bool pin = p >= 0 && h->node_level[p] >= h->min_adm_level;
+            need_up[node] = used_y0[node] || (pin && need_up[p]);
+            need_down[node] = wrote_y1[node] || (pin && need_down[p] && rank[p] > 0);
+        }
+
+    Planner fwd_lv, bwd_lv, mid1, mid2, den1, den2;
+    std::vector<Tile> all;
+    double mat_bytes = 0.0, vec_bytes = 0.0, flops = 0.0;
+    d->fwd.clear();
+    d->bwd.clear();
+
+    /* U bases */
+    std::vector<size_t> uoff(n_node, 0);
+    std::vector<int> uld(n_node, 0);
+    for (int i = 0; i < n_node; i++) {
+        H2E_dense_mat_p U = h->U[i];
+        if (U->nrow > 0 && U->ncol > 0) uoff[i] = pk.put(U->data, U->nrow, U->ncol, U->ld, uld[i]);
+    }
+    d->bytes_U = pk.host.size() * sizeof(double);
+
+    /* upward sweep, deepest level first (src/H2ERI_matvec.c:111-156) */
+    for (int lv = h->max_level; lv >= h->min_adm_level; lv--) {
+        Planner p;
+        for (int j = 0; j < h->level_n_node[lv]; j++) {
+            int node = h->level_nodes[lv * h->n_leaf_node + j];
+            H2E_dense_mat_p U = h->U[node];
+            if (!need_up[node] || U->nrow == 0 || U->ncol == 0) continue;
+            bool leaf = h->n_child[node] == 0;
+            int in_off = leaf ? h->mat_cluster[2 * node] : voff[h->children[node * h->max_child]];
+            p.add(uoff[node], uld[node], U->nrow, U->ncol, VK_NONE, 0, VK_NONE, 0, leaf ? VK_X : VK_Y0, in_off,
+                  VK_Y0, voff[node]);
+            mat_bytes += 8.0 * U->nrow * U->ncol;
+            vec_bytes += 8.0 * (U->nrow + U->ncol);
+            flops += 2.0 * U->nrow * U->ncol;
+        }
+        Range r{(int)all.size(), (int)p.tiles.size()};
+        all.insert(all.end(), p.tiles.begin(), p.tiles.end());
+        d->fwd.push_back(r);
+    }
+
+    /* coupling blocks (src/H2ERI_matvec.c:299-407) */
+    size_t b_start = pk.host.size();
+    for (int i = 0; i < h->n_r_adm_pair; i++) {
+        int n0 = h->r_adm_pairs[2 * i], n1 = h->r_adm_pairs[2 * i + 1];
+        int l0 = h->node_level[n0], l1 = h->node_level[n1];
+        BlockLoc b = pack_block(pk, h->c_B_blks[i], d->lr_total);
+        uint8_t kin0, kout0, kin1, kout1;
+        int in0, out0, in1, out1;
+        if (l0 == l1) {
+            kin0 = VK_Y0; in0 = voff[n1]; kout0 = VK_Y1; out0 = voff[n0];
+            kin1 = VK_Y0; in1 = voff[n0]; kout1 = VK_Y1; out1 = voff[n1];
+        } else if (l0 > l1) {
+            kin0 = VK_X; in0 = h->mat_cluster[2 * n1]; kout0 = VK_Y1; out0 = voff[n0];
+            kin1 = VK_Y0; in1 = voff[n0]; kout1 = VK_Y; out1 = h->mat_cluster[2 * n1];
+        } else {
+            kin0 = VK_Y0; in0 = voff[n1]; kout0 = VK_Y; out0 = h->mat_cluster[2 * n0];
+            kin1 = VK_X; in1 = h->mat_cluster[2 * n0]; kout1 = VK_Y1; out1 = voff[n1];
+        }
+        plan_block(mid1, mid2, b, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
+        mat_bytes += 8.0 * block_elems(b);
+        vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
+        flops += 4.0 * block_elems(b);
+    }
+    d->bytes_B = (pk.host.size() - b_start) * sizeof(double);
+    d->mid1 = {(int)all.size(), (int)mid1.tiles.size()};
+    all.insert(all.end(), mid1.tiles.begin(), mid1.tiles.end());
+    d->mid2 = {(int)all.size(), (int)mid2.tiles.size()};
+    all.insert(all.end(), mid2.tiles.begin(), mid2.tiles.end());
+
+    /* downward sweep, shallowest level first (src/H2ERI_matvec.c:679-738) */
+    for (int lv = h->min_adm_level; lv <= h->max_level; lv++) {
+        Planner p;
+        for (int j = 0; j < h->level_n_node[lv]; j++) {
+            int node = h->level_nodes[lv * h->n_leaf_node + j];
+            H2E_dense_mat_p U = h->U[node];
+            if (!need_down[node] || U->nrow == 0 || U->ncol == 0) continue;
+            bool leaf = h->n_child[node] == 0;
+            int out_off = leaf ? h->mat_cluster[2 * node] : voff[h->children[node * h->max_child]];
+            p.add(uoff[node], uld[node], U->nrow, U->ncol, VK_Y1, voff[node], leaf ? VK_Y : VK_Y1, out_off, VK_NONE,
+                  0, VK_NONE, 0);
+            mat_bytes += 8.0 * U->nrow * U->ncol;
+            vec_bytes += 8.0 * (U->nrow + U->ncol);
+            flops += 2.0 * U->nrow * U->ncol;
+        }
+        Range r{(int)all.size(), (int)p.tiles.size()};
+        all.insert(all.end(), p.tiles.begin(), p.tiles.end());
+        d->bwd.push_back(r);
+    }
+
+    /* near field (src/H2ERI_matvec.c:572-660) */
+    size_t d_start = pk.host.size();
+    for (int i = 0; i < h->n_D; i++) {
+        BlockLoc b = pack_block(pk, h->c_D_blks[i], d->lr_total);
+        if (i < h->n_leaf_node) {
+            int node = h->height_nodes[i];
+            int off = h->mat_cluster[2 * node];
+            plan_block(den1, den2, b, VK_X, off, VK_Y, off, VK_NONE, 0, VK_NONE, 0);
+            vec_bytes += 8.0 * (b.nrow + b.ncol);
+            flops += 2.0 * block_elems(b);
+        } else {
+            int k = i - h->n_leaf_node;
+            int n0 = h->r_inadm_pairs[2 * k], n1 = h->r_inadm_pairs[2 * k + 1];
+            int o0 = h->mat_cluster[2 * n0], o1 = h->mat_cluster[2 * n1];
+            plan_block(den1, den2, b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
+            vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
+            flops += 4.0 * block_elems(b);
+        }
+        mat_bytes += 8.0 * block_elems(b);
+    }
+    d->bytes_D = (pk.host.size() - d_start) * sizeof(double);
+    d->den1 = {(int)all.size(), (int)den1.tiles.size()};
+    all.insert(all.end(), den1.tiles.begin(), den1.tiles.end());
+    d->den2 = {(int)all.size(), (int)den2.tiles.size()};
+    all.insert(all.end(), den2.tiles.begin(), den2.tiles.end());
+
+    d->alg_bytes_matrix = mat_bytes;
+    d->alg_bytes_vec = vec_bytes;
+    d->alg_flops = flops;
+    d->n_tiles = (int)all.size();
+    d->arena_elems = pk.host.size();
+    CUDA_TRY(cudaMalloc(&d->arena, std::max<size_t>(d->arena_elems, 4) * sizeof(double)));
+    CUDA_TRY(cudaMemcpy(d->arena, pk.host.data(), d->arena_elems * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMalloc(&d->tiles, std::max<size_t>(all.size(), 1) * sizeof(Tile)));
+    if (!all.empty()) CUDA_TRY(cudaMemcpy(d->tiles, all.data(), all.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+
+    /* J assembly maps */
+    const int nbf = h->num_bf, num_sp = h->num_sp;
+    std::vector<int> unc(std::max(krnl, 1), 0), con((size_t)nbf * nbf, -1);
+    for (int i = 0; i < num_sp; i++) {
+        int M = h->sp_shell_idx[i], N = h->sp_shell_idx[i + num_sp];
+        int srow = h->shell_bf_sidx[M], nrow = h->shell_bf_sidx[M + 1] - srow;
+        int scol = h->shell_bf_sidx[N], ncol = h->shell_bf_sidx[N + 1] - scol;
+        int base = h->sp_bfp_sidx[i];
+        for (int j = 0; j < ncol; j++)
+            for (int k = 0; k < nrow; k++) {
+                int xi = base + j * nrow + k;
+                int di = (scol + j) * nbf + srow + k;
+                unc[xi] = (di << 1) | (M != N ? 1 : 0);
+                con[di] = (xi << 1) | (M == N ? 1 : 0);
+            }
+    }
+    CUDA_TRY(cudaMalloc(&d->unc_map, unc.size() * sizeof(int)));
+    CUDA_TRY(cudaMemcpy(d->unc_map, unc.data(), unc.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMalloc(&d->con_map, std::max<size_t>(con.size(), 1) * sizeof(int)));
+    CUDA_TRY(cudaMemcpy(d->con_map, con.data(), con.size() * sizeof(int), cudaMemcpyHostToDevice));
+
+    CUDA_TRY(cudaStreamCreateWithFlags(&d->s_main, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&d->s_aux, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
+    for (auto &e : d->ev_t) CUDA_TRY(cudaEventCreate(&e));
+
+    d->krnl = krnl;
+    d->n_node = n_node;
+    d->num_bf = nbf;
+    d->n_B = h->n_B;
+    d->n_D = h->n_D;
+    d->fp_U = h->U;
+    d->fp_B = h->c_B_blks;
+    d->fp_D = h->c_D_blks;
+    return 0;
+}
+
+/* Look up (and if needed create) the device representation of h. */
+int get_rep(H2ERI_p h, DevRep **out)
+{
+    if (h == nullptr) { set_error("null H2ERI handle"); return 1; }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        set_error(std::string("no usable CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices"));
+        return 9;
+    }
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_reps.find(h);
+    if (it != g_reps.end()) {
+        DevRep *d = it->second;
+        if (d->krnl == h->krnl_mat_size && d->n_node == h->n_node && d->fp_U == h->U && d->fp_B == h->c_B_blks &&
+            d->fp_D == h->c_D_blks) {
+            *out = d;
+            return 0;
+        }
+        free_rep(d);         /* stale: the structure was rebuilt */
+        g_reps.erase(it);
+    }
+    DevRep *d = new DevRep();
+    cudaGetDevice(&d->device);
+    int rc = build_rep(h, d);
+    if (rc != 0) { free_rep(d); return rc; }
+    g_reps[h] = d;
+    *out = d;
+    return 0;
+}
+
+static int ensure_work(DevRep *d, int nvec)
+{
+    if (nvec <= d->nvec_cap) return 0;
+    cudaFree(d->work);
+    cudaFree(d->xbuf);
+    cudaFree(d->ybuf);
+    d->work = d->xbuf = d->ybuf = nullptr;
+    size_t per = (size_t)2 * d->rank_total + d->lr_total;
+    CUDA_TRY(cudaMalloc(&d->work, std::max<size_t>(per * nvec, 1) * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&d->xbuf, (size_t)std::max(d->krnl, 1) * nvec * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&d->ybuf, (size_t)std::max(d->krnl, 1) * nvec * sizeof(double)));
+    d->nvec_cap = nvec;
+    return 0;
+}
+
+static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s)
+{
+    if (r.count == 0) return;
+    dim3 grid(r.count, nvec);
+    k_tile_f64<<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena, va);
+}
+
+/* Enqueue y = A x for nvec vectors (device pointers) on stream s. If timed,
+ * per-phase events are recorded (fwd, mid, bwd on the main chain, dense on
+ * the auxiliary stream). */
+int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t s, bool timed)
+{
+    int rc = ensure_work(d, nvec);
+    if (rc) return rc;
+    const size_t per_r = (size_t)d->rank_total * nvec, per_t = (size_t)d->lr_total * nvec;
+    VecArgs va;
+    std::memset(&va, 0, sizeof(va));
+    va.base[VK_X] = const_cast<double *>(x);
+    va.stride[VK_X] = d->krnl;
+    va.base[VK_Y] = y;
+    va.stride[VK_Y] = d->krnl;
+    va.base[VK_Y0] = d->work;
+    va.stride[VK_Y0] = d->rank_total;
+    va.base[VK_Y1] = d->work + per_r;
+    va.stride[VK_Y1] = d->rank_total;
+    va.base[VK_T] = d->work + 2 * per_r;
+    va.stride[VK_T] = d->lr_total;
+    CUDA_TRY(cudaMemsetAsync(d->work, 0, (2 * per_r + per_t) * sizeof(double), s));
+    CUDA_TRY(cudaMemsetAsync(y, 0, (size_t)d->krnl * nvec * sizeof(double), s));
+    CUDA_TRY(cudaEventRecord(d->ev_fork, s));
+    CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_fork, 0));
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], d->s_aux));
+    launch_range(d, d->den1, va, nvec, d->s_aux);
+    launch_range(d, d->den2, va, nvec, d->s_aux);
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[7], d->s_aux));
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], s));
+    for (const Range &r : d->fwd) launch_range(d, r, va, nvec, s);
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[1], s));
+    launch_range(d, d->mid1, va, nvec, s);
+    launch_range(d, d->mid2, va, nvec, s);
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[2], s));
+    for (const Range &r : d->bwd) launch_range(d, r, va, nvec, s);
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[3], s));
+    CUDA_TRY(cudaEventRecord(d->ev_join, d->s_aux));
+    CUDA_TRY(cudaStreamWaitEvent(s, d->ev_join, 0));
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[4], s));
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+/* After a timed enqueue has completed: fill the reference timers. */
+static void collect_times(DevRep *d, H2ERI_p h)
+{
+    float f = 0, m = 0, b = 0, dn = 0, tot = 0;
+    cudaEventElapsedTime(&f, d->ev_t[0], d->ev_t[1]);
+    cudaEventElapsedTime(&m, d->ev_t[1], d->ev_t[2]);
+    cudaEventElapsedTime(&b, d->ev_t[2], d->ev_t[3]);
+    cudaEventElapsedTime(&dn, d->ev_t[6], d->ev_t[7]);
+    cudaEventElapsedTime(&tot, d->ev_t[0], d->ev_t[4]);
+    d->last_ms[0] = f; d->last_ms[1] = m; d->last_ms[2] = b; d->last_ms[3] = dn; d->last_ms[4] = tot;
+    h->timers[MV_FWD_TIMER_IDX] += 1e-3 * f;
+    h->timers[MV_MID_TIMER_IDX] += 1e-3 * m;
+    h->timers[MV_BWD_TIMER_IDX] += 1e-3 * b;
+    h->timers[MV_DEN_TIMER_IDX] += 1e-3 * dn;
+    h->timers[MV_VOP_TIMER_IDX] += 1e-3 * std::max(0.0f, tot - (f + m + b));
+}
+
+static int ensure_den(DevRep *d, int n_den)
+{
+    if (n_den <= d->nden_cap) return 0;
+    cudaFree(d->dbuf);
+    cudaFree(d->jbuf);
+    d->dbuf = d->jbuf = nullptr;
+    size_t n2 = (size_t)d->num_bf * d->num_bf;
+    CUDA_TRY(cudaMalloc(&d->dbuf, std::max<size_t>(n2 * n_den, 1) * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&d->jbuf, std::max<size_t>(n2 * n_den, 1) * sizeof(double)));
+    d->nden_cap = n_den;
+    return 0;
+}
+
+int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStream_t s, bool timed)
+{
+    int rc = ensure_work(d, n_den);
+    if (rc) return rc;
+    const long long n2 = (long long)d->num_bf * d->num_bf;
+    dim3 g1((d->krnl + 255) / 256 < 4096 ? (d->krnl + 255) / 256 : 4096, n_den);
+    k_uncontract<<<g1, 256, 0, s>>>(d->unc_map, d->krnl, den, n2, d->xbuf, d->krnl);
+    rc = enqueue_matvec(d, n_den, d->xbuf, d->ybuf, s, timed);
+    if (rc) return rc;
+    long long nb = (n2 + 255) / 256;
+    dim3 g2((unsigned)std::min<long long>(nb, 8192), n_den);
+    k_contract<<<g2, 256, 0, s>>>(d->con_map, d->num_bf, d->ybuf, d->krnl, J, n2);
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace h2g
+
+using namespace h2g;
+
+/* ======================================================================== */
+/* C API                                                                     */
+/* ======================================================================== */
+
+[[noreturn]] static void fatal(const char *fn)
+{
+    std::fprintf(stderr, "[h2eri_gb300 FATAL] %s failed: %s\n", fn, t_last_error.c_str());
+    std::fflush(stderr);
+    std::abort();
+}
+
+extern "C" const char *H2ERI_gpu_last_error(void) { return t_last_error.c_str(); }
+
+extern "C" int H2ERI_gpu_upload(H2ERI_p h2eri)
+{
+    DevRep *d;
+    return get_rep(h2eri, &d);
+}
+
+extern "C" void H2ERI_gpu_release(H2ERI_p h2eri)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_reps.find(h2eri);
+    if (it == g_reps.end()) return;
+    free_rep(it->second);
+    g_reps.erase(it);
+}
+
+extern "C" int H2ERI_gpu_set_precision(H2ERI_p h2eri, int mode)
+{
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return rc;
+    if (mode != H2ERI_GPU_FP64 && mode != H2ERI_GPU_MIXED) {
+        set_error("unknown precision mode");
+        return 3;
+    }
+    return set_precision_mode(d, h2eri, mode);
+}
+
+extern "C" int H2ERI_matvec_device(H2ERI_p h2eri, int nvec, const double *d_x, double *d_y, void *stream)
+{
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return rc;
+    if (nvec < 1) { set_error("nvec < 1"); return 3; }
+    cudaStream_t s = stream ? (cudaStream_t)stream : d->s_main;
+    return enqueue_matvec(d, nvec, d_x, d_y, s, false);
+}
+
+extern "C" int H2ERI_matvec_multi(H2ERI_p h2eri, int nvec, const double *x, double *y)
+{
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return rc;
+    if (nvec < 1) { set_error("nvec < 1"); return 3; }
+    rc = ensure_work(d, nvec);
+    if (rc) return rc;
+    size_t bytes = (size_t)d->krnl * nvec * sizeof(double);
+    CUDA_TRY(cudaMemcpyAsync(d->xbuf, x, bytes, cudaMemcpyHostToDevice, d->s_main));
+    rc = enqueue_matvec(d, nvec, d->xbuf, d->ybuf, d->s_main, true);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(y, d->ybuf, bytes, cudaMemcpyDeviceToHost, d->s_main));
+    CUDA_TRY(cudaStreamSynchronize(d->s_main));
+    collect_times(d, h2eri);
+    h2eri->n_matvec += nvec;
+    return 0;
+}
+
+extern "C" void H2ERI_matvec(H2ERI_p h2eri, const double *x, double *y)
+{
+    if (H2ERI_matvec_multi(h2eri, 1, x, y) != 0) fatal("H2ERI_matvec");
+}
+
+extern "C" int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double *d_den, double *d_J, void *stream)
+{
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return rc;
+    if (n_den < 1) { set_error("n_den < 1"); return 3; }
+    cudaStream_t s = stream ? (cudaStream_t)stream : d->s_main;
+    return enqueue_coulomb(d, n_den, d_den, d_J, s, false);
+}
+
+extern "C" int H2ERI_build_Coulomb_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *J_mats)
+{
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return rc;
+    if (n_den < 1) { set_error("n_den < 1"); return 3; }
+    rc = ensure_den(d, n_den);
+    if (rc) return rc;
+    size_t bytes = (size_t)d->num_bf * d->num_bf * n_den * sizeof(double);
+    CUDA_TRY(cudaMemcpyAsync(d->dbuf, den_mats, bytes, cudaMemcpyHostToDevice, d->s_main));
+    rc = enqueue_coulomb(d, n_den, d->dbuf, d->jbuf, d->s_main, true);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(J_mats, d->jbuf, bytes, cudaMemcpyDeviceToHost, d->s_main));
+    CUDA_TRY(cudaStreamSynchronize(d->s_main));
+    collect_times(d, h2eri);
+    h2eri->n_matvec += n_den;
+    return 0;
+}
+
+extern "C" void H2ERI_build_Coulomb(H2ERI_p h2eri, const double *den_mat, double *J_mat)
+{
+    if (H2ERI_build_Coulomb_multi(h2eri, 1, den_mat, J_mat) != 0) fatal("H2ERI_build_Coulomb");
+}
+
+extern "C" void h2g_gpu_print_statistic(H2ERI_p h2eri)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_reps.find(h2eri);
+    if (it == g_reps.end()) return;
+    DevRep *d = it->second;
+    std::printf("==================== GPU (device %d) =======================\n", d->device);
+    std::printf("  * Device arena U, B, D          : %.2lf, %.2lf, %.2lf (MB)\n", d->bytes_U / 1048576.0,
+                d->bytes_B / 1048576.0, d->bytes_D / 1048576.0);
+    std::printf("  * Tiles per matvec              : %d\n", d->n_tiles);
+    if (d->last_ms[4] > 0)
+        std::printf("  * Last matvec (ms) fwd/mid/bwd/dense/total : %.4f %.4f %.4f %.4f %.4f\n", d->last_ms[0],
+                    d->last_ms[1], d->last_ms[2], d->last_ms[3], d->last_ms[4]);
+}

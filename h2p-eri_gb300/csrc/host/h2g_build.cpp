@@ -1,0 +1,761 @@
+/*
+ * Per-geometry H2 construction on the host (runs once before upload):
+ * nested bases U from proxy points and far-field sketches, coupling blocks B,
+ * near-field blocks D, and their interpolative-decomposition compression.
+ * Restates H2P-ERI src/H2ERI_build_H2.c and src/H2E_ID_compress.c; the random
+ * sketches use a deterministic per-node generator instead of libc rand(), so
+ * the result is reproducible run to run (the reference's is not: rand() is
+ * called from OpenMP threads, src/H2ERI_utils.c:68,77).
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <omp.h>
+
+#include "h2g_host.h"
+#include "h2eri_gb300.h"
+
+namespace h2g {
+
+/* ---------------------------------------------------------------------- */
+/* Pivoted QR and interpolative decomposition                              */
+/* ---------------------------------------------------------------------- */
+
+/* Householder QR with column pivoting on a column-major m x n matrix R
+ * (leading dimension ld), stopping when the largest remaining column norm
+ * drops below rel_tol times the largest initial column norm
+ * (H2P-ERI src/H2E_ID_compress.c:51-184). Returns the rank; p holds the
+ * column permutation. */
+static int pivoted_qr(double *R, int m, int n, int ld, double rel_tol, int *p)
+{
+    const int max_iter = std::min(m, n);
+    std::vector<double> cn(n);
+    double norm_p = 0.0;
+    int pivot = 0;
+    for (int j = 0; j < n; j++) {
+        p[j] = j;
+        double s = 0.0;
+        const double *c = R + (size_t)j * ld;
+        for (int k = 0; k < m; k++) s += c[k] * c[k];
+        cn[j] = std::sqrt(s);
+    }
+    for (int j = 0; j < n; j++)
+        if (cn[j] > norm_p) { norm_p = cn[j]; pivot = j; }
+    double stop_norm = std::max(std::sqrt((double)m) * 1e-15, rel_tol) * norm_p;
+    int rank = max_iter;
+    for (int i = 0; i < max_iter; i++) {
+        if (norm_p < stop_norm) { rank = i; break; }
+        if (i != pivot) {
+            std::swap(p[i], p[pivot]);
+            std::swap(cn[i], cn[pivot]);
+            double *a = R + (size_t)i * ld, *b = R + (size_t)pivot * ld;
+            for (int k = 0; k < m; k++) std::swap(a[k], b[k]);
+        }
+        const int hl = m - i;
+        double *h = R + (size_t)i * ld + i;
+        double sign = (h[0] > 0.0) ? 1.0 : -1.0;
+        double hn = 0.0;
+        for (int k = 0; k < hl; k++) hn += h[k] * h[k];
+        hn = std::sqrt(hn);
+        h[0] += sign * hn;
+        double hn2 = 0.0;
+        for (int k = 0; k < hl; k++) hn2 += h[k] * h[k];
+        double inv = 1.0 / std::sqrt(hn2);
+        for (int k = 0; k < hl; k++) h[k] *= inv;
+        for (int j = i + 1; j < n; j++) {
+            double *c = R + (size_t)j * ld + i;
+            double d = 0.0;
+            for (int k = 0; k < hl; k++) d += h[k] * c[k];
+            d *= 2.0;
+            for (int k = 0; k < hl; k++) c[k] -= d * h[k];
+            if (cn[j] < stop_norm) { cn[j] = 0.0; continue; }
+            double t = cn[j] * cn[j] - c[0] * c[0];
+            if (t <= 1e-10) {
+                double s = 0.0;
+                for (int k = 1; k < hl; k++) s += c[k] * c[k];
+                cn[j] = std::sqrt(s);
+            } else {
+                cn[j] = std::sqrt(t);
+            }
+        }
+        h[0] = -sign * hn;
+        for (int k = 1; k < hl; k++) h[k] = 0.0;
+        pivot = i + 1;
+        norm_p = 0.0;
+        for (int j = i + 1; j < n; j++)
+            if (cn[j] > norm_p) { norm_p = cn[j]; pivot = j; }
+    }
+    return rank;
+}
+
+/* ID over the rows of a row-major nrow x ncol matrix A: A ~= U * A(J, :)
+ * (H2P-ERI src/H2E_ID_compress.c:433-576). A row-major is A^T column-major,
+ * so pivoted QR on that view picks skeleton rows. */
+void id_compress(H2E_dense_mat_p A, double rel_tol, H2E_dense_mat_p *U_out, H2E_int_vec_p J)
+{
+    const int nrow = A->nrow, ncol = A->ncol, ld = A->ld;
+    std::vector<int> p(std::max(nrow, 1));
+    int r = (nrow > 0 && ncol > 0) ? pivoted_qr(A->data, ncol, nrow, ld, rel_tol, p.data()) : 0;
+    if (r == 0) {
+        J->length = 0;
+        if (U_out) {
+            H2E_dense_mat_p U = dmat_new(0, 0);
+            U->nrow = nrow;
+            U->ncol = 0;
+            U->ld = 0;
+            *U_out = U;
+        }
+        return;
+    }
+    /* sorted skeleton rows and, for each, its pivot position */
+    std::vector<std::pair<int, int>> sk(r);
+    for (int k = 0; k < r; k++) sk[k] = {p[k], k};
+    std::sort(sk.begin(), sk.end());
+    ivec_reserve(J, r);
+    for (int k = 0; k < r; k++) J->data[k] = sk[k].first;
+    J->length = r;
+    if (U_out == nullptr) return;
+    /* E = R11^{-1} R12, R11 r x r upper triangular, R12 r x (nrow - r); column-major with ld */
+    const int ne = nrow - r;
+    double *R = A->data;
+    for (int c = 0; c < ne; c++) {
+        double *x = R + (size_t)(r + c) * ld;
+        for (int i = r - 1; i >= 0; i--) {
+            double s = x[i];
+            for (int k = i + 1; k < r; k++) s -= R[(size_t)k * ld + i] * x[k];
+            x[i] = s / R[(size_t)i * ld + i];
+        }
+    }
+    H2E_dense_mat_p U = dmat_new(nrow, r);
+    std::vector<int> sorted_pos(r);      /* pivot position -> sorted column */
+    for (int k = 0; k < r; k++) sorted_pos[sk[k].second] = k;
+    for (int k = 0; k < nrow; k++) {
+        int row = p[k];
+        double *u = U->data + (size_t)row * r;
+        if (k < r) {
+            std::memset(u, 0, sizeof(double) * r);
+            u[sorted_pos[k]] = 1.0;
+        } else {
+            const double *e = R + (size_t)k * ld;   /* column r + (k - r) of E */
+            for (int c = 0; c < r; c++) u[c] = e[sk[c].second];
+        }
+    }
+    *U_out = U;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Helpers for the U construction                                          */
+/* ---------------------------------------------------------------------- */
+
+namespace {
+
+struct Rng {   /* splitmix64 */
+    uint64_t s;
+    explicit Rng(uint64_t seed) : s(seed) {}
+    uint64_t next()
+    {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        return z ^ (z >> 31);
+    }
+};
+
+/* Sparse random k x n matrix with min(max_nnz_col, k) entries +-1 per column,
+ * stored as n rows (columns of the matrix) of column indices
+ * (H2P-ERI src/H2ERI_utils.c:49-96). */
+struct Sketch {
+    int nnz_col = 0, n = 0;
+    std::vector<double> val;
+    std::vector<int> col;
+};
+
+void gen_sketch(int max_nnz_col, int k, int n, Rng &rng, Sketch &s)
+{
+    s.nnz_col = std::min(max_nnz_col, k);
+    s.n = n;
+    s.val.resize((size_t)n * s.nnz_col);
+    s.col.resize((size_t)n * s.nnz_col);
+    for (auto &v : s.val) v = (rng.next() & 1) ? 1.0 : -1.0;
+    std::vector<char> flag(std::max(k, 1), 0);
+    for (int i = 0; i < n; i++) {
+        int *c = s.col.data() + (size_t)i * s.nnz_col;
+        int cnt = 0;
+        while (cnt < s.nnz_col) {
+            int x = (int)(rng.next() % (uint64_t)k);
+            if (!flag[x]) { flag[x] = 1; c[cnt++] = x; }
+        }
+        for (int j = 0; j < s.nnz_col; j++) flag[c[j]] = 0;
+    }
+}
+
+/* y (m x n, ldy) = x (m x k, ldx) * S (src/H2ERI_utils.c:99-118) */
+void sketch_apply(int m, const Sketch &s, const double *x, int ldx, double *y, int ldy)
+{
+    for (int i = 0; i < m; i++) {
+        const double *xi = x + (size_t)i * ldx;
+        double *yi = y + (size_t)i * ldy;
+        for (int j = 0; j < s.n; j++) {
+            double r = 0.0;
+            const int *c = s.col.data() + (size_t)j * s.nnz_col;
+            const double *v = s.val.data() + (size_t)j * s.nnz_col;
+            for (int l = 0; l < s.nnz_col; l++) r += v[l] * xi[c[l]];
+            yi[j] = r;
+        }
+    }
+}
+
+/* Proxy points: nlayer scaled copies of a uniform grid on the surface of
+ * [-1,1]^3 between radii r1 and r2 (src/H2ERI_build_H2.c:25-103).
+ * Output pp = [x(0..n) | y(0..n) | z(0..n)]. */
+void proxy_points(double r1, double r2, int nlayer, int npts_layer, std::vector<double> &pp, int &npts)
+{
+    int nface = npts_layer / 6;
+    int naxis = (int)std::ceil(std::sqrt((double)nface));
+    int nl = 6 * naxis * naxis;
+    npts = nlayer * nl;
+    pp.assign((size_t)npts * 3, 0.0);
+    double *x = pp.data(), *y = x + npts, *z = y + npts;
+    double hstep = 2.0 / (double)(naxis + 1);
+    int idx = 0;
+    for (int i = 0; i < naxis; i++) {
+        double hi = hstep * (i + 1) - 1.0;
+        for (int j = 0; j < naxis; j++) {
+            double hj = hstep * (j + 1) - 1.0;
+            const double f[6][3] = {{hi, hj, -1.0}, {hi, hj, 1.0}, {hi, -1.0, hj},
+                                    {hi, 1.0, hj}, {-1.0, hi, hj}, {1.0, hi, hj}};
+            for (int q = 0; q < 6; q++) { x[idx] = f[q][0]; y[idx] = f[q][1]; z[idx] = f[q][2]; idx++; }
+        }
+    }
+    for (int l = 1; l < nlayer; l++) {
+        std::memcpy(x + l * nl, x, sizeof(double) * nl);
+        std::memcpy(y + l * nl, y, sizeof(double) * nl);
+        std::memcpy(z + l * nl, z, sizeof(double) * nl);
+    }
+    int nl1 = std::max(nlayer - 1, 1);
+    double dr = ((r2 - r1) / r1) / (double)nl1;
+    for (int l = 0; l < nlayer; l++) {
+        double r = r1 * (1.0 + l * dr);
+        for (int j = 0; j < nl; j++) { x[l * nl + j] *= r; y[l * nl + j] *= r; z[l * nl + j] *= r; }
+    }
+}
+
+/* Far-field SSPs whose extents overlap each node's near field
+ * (src/H2ERI_build_H2.c:115-259). */
+void calc_ovlp_ff_idx(H2ERI_p h)
+{
+    const int n_node = h->n_node, n_point = h->n_point;
+    const double *cx = h->sp_center, *cy = cx + n_point, *cz = cy + n_point, *ext = h->sp_extent;
+    h->ovlp_ff_idx = (H2E_int_vec_p *)std::malloc(sizeof(H2E_int_vec_p) * n_node);
+    for (int i = 0; i < n_node; i++) h->ovlp_ff_idx[i] = ivec_new(n_point);
+    H2E_int_vec_p root = h->ovlp_ff_idx[h->root_idx];
+    for (int i = 0; i < n_point; i++) root->data[i] = i;
+    root->length = n_point;
+    for (int lv = 0; lv < h->max_level; lv++) {
+        for (int j = 0; j < h->level_n_node[lv]; j++) {
+            int node = h->level_nodes[lv * h->n_leaf_node + j];
+            H2E_int_vec_p par = h->ovlp_ff_idx[node];
+            for (int k = 0; k < h->n_child[node]; k++) {
+                int c = h->children[node * h->max_child + k];
+                const double *eb = h->enbox + 6 * c;
+                double ec[3] = {eb[0] + 0.5 * eb[3], eb[1] + 0.5 * eb[4], eb[2] + 0.5 * eb[5]};
+                double sup = 0.5 + H2G_ALPHA_SUP;
+                double sl[3] = {sup * eb[3], sup * eb[4], sup * eb[5]};
+                H2E_int_vec_p out = h->ovlp_ff_idx[c];
+                for (int l = 0; l < par->length; l++) {
+                    int f = par->data[l];
+                    double e = ext[f];
+                    double rel[3] = {cx[f] - ec[0] + sl[0] - e, cy[f] - ec[1] + sl[1] - e, cz[f] - ec[2] + sl[2] - e};
+                    bool adm_any = false;
+                    for (int d = 0; d < 3; d++) {
+                        bool left = rel[d] < 0, right = rel[d] >= 0;
+                        bool adm_l = std::fabs(rel[d]) >= 2.0 * e - 1e-8;
+                        bool adm_r = std::fabs(rel[d]) >= 2.0 * sl[d] - 1e-8;
+                        if ((left && adm_l) || (right && adm_r)) adm_any = true;
+                    }
+                    if (!adm_any) out->data[out->length++] = f;
+                }
+            }
+        }
+    }
+    std::vector<int> tmp(n_point);
+    for (int lv = h->min_adm_level; lv <= h->max_level; lv++) {
+        for (int j = 0; j < h->level_n_node[lv]; j++) {
+            int node = h->level_nodes[lv * h->n_leaf_node + j];
+            const double *eb = h->enbox + 6 * node;
+            double ec[3] = {eb[0] + 0.5 * eb[3], eb[1] + 0.5 * eb[4], eb[2] + 0.5 * eb[5]};
+            double ac = 0.5 + H2G_ALPHA_H2;
+            double al[3] = {ac * eb[3], ac * eb[4], ac * eb[5]};
+            H2E_int_vec_p v = h->ovlp_ff_idx[node];
+            int cnt = 0;
+            for (int l = 0; l < v->length; l++) {
+                int f = v->data[l];
+                if (std::fabs(cx[f] - ec[0]) > al[0] || std::fabs(cy[f] - ec[1]) > al[1] ||
+                    std::fabs(cz[f] - ec[2]) > al[2])
+                    tmp[cnt++] = f;
+            }
+            std::memcpy(v->data, tmp.data(), sizeof(int) * cnt);
+            v->length = cnt;
+        }
+    }
+}
+
+/* Given bf-pair row indices (ascending, relative to the concatenation of the
+ * SSPs in sp_idx), find the SSPs that contain them and the row indices inside
+ * the concatenation of just those SSPs (src/H2ERI_build_H2.c:271-335).
+ * pair_pos receives positions into sp_idx. */
+void extract_sp_idx(H2ERI_p h, const int *row_idx, int n_row, const int *sp_idx, int n_sp,
+                    std::vector<int> &pair_pos, std::vector<int> &row_new)
+{
+    std::vector<int> off(n_sp + 1, 0), which(n_row), flag(n_sp, 0);
+    for (int i = 0; i < n_sp; i++) off[i + 1] = off[i] + h->sp_nbfp[sp_idx[i]];
+    int j = 0;
+    for (int i = 0; i < n_row; i++) {
+        int x = row_idx[i];
+        /* rows are ascending, but restart the scan to be safe for unsorted input */
+        if (j >= n_sp || x < off[j]) j = 0;
+        while (j < n_sp && !(off[j] <= x && x < off[j + 1])) j++;
+        which[i] = j;
+        flag[j] = 1;
+    }
+    pair_pos.clear();
+    std::vector<int> newpos(n_sp, -1);
+    for (int i = 0; i < n_sp; i++)
+        if (flag[i]) { newpos[i] = (int)pair_pos.size(); pair_pos.push_back(i); }
+    std::vector<int> noff(pair_pos.size() + 1, 0);
+    for (size_t i = 0; i < pair_pos.size(); i++) noff[i + 1] = noff[i] + h->sp_nbfp[sp_idx[pair_pos[i]]];
+    row_new.resize(n_row);
+    for (int i = 0; i < n_row; i++) row_new[i] = row_idx[i] - off[which[i]] + noff[newpos[which[i]]];
+}
+
+int sum_nbfp(H2ERI_p h, const int *idx, int n)
+{
+    int s = 0;
+    for (int i = 0; i < n; i++) s += h->sp_nbfp[idx[i]];
+    return s;
+}
+
+/* Nested bases U and skeleton sets (src/H2ERI_build_H2.c:351-827). */
+void build_UJ_proxy(H2ERI_p h)
+{
+    const int n_node = h->n_node, n_point = h->n_point, n_leaf = h->n_leaf_node;
+    const int max_level = h->max_level, min_adm = h->min_adm_level;
+    const double rel_tol = h->QR_stop_tol;
+    h->n_UJ = n_node;
+    h->U = (H2E_dense_mat_p *)std::calloc(n_node, sizeof(H2E_dense_mat_p));
+    h->J_pair = (H2E_int_vec_p *)std::calloc(n_node, sizeof(H2E_int_vec_p));
+    h->J_row = (H2E_int_vec_p *)std::calloc(n_node, sizeof(H2E_int_vec_p));
+    std::vector<int> skel(n_point, 1);
+    std::vector<std::vector<int>> lvl_leaf(max_level + 1);
+    for (int i = 0; i < n_leaf; i++) {
+        int leaf = h->height_nodes[i];
+        for (int lv = h->node_level[leaf] + 1; lv <= max_level; lv++) lvl_leaf[lv].push_back(leaf);
+    }
+    calc_ovlp_ff_idx(h);
+
+    for (int lv = max_level; lv >= min_adm; lv--) {
+        const int nlv = h->level_n_node[lv];
+        const int *lnodes = h->level_nodes + lv * n_leaf;
+        #pragma omp parallel for schedule(dynamic, 1)
+        for (int jn = 0; jn < nlv; jn++) {
+            const int node = lnodes[jn];
+            const int nch = h->n_child[node];
+            std::vector<int> pair_idx, row_idx;
+            /* (1) candidate rows of this node */
+            if (nch == 0) {
+                for (int k = h->pt_cluster[2 * node]; k <= h->pt_cluster[2 * node + 1]; k++)
+                    pair_idx.push_back(h->index_seq[k]);
+                int nb = sum_nbfp(h, pair_idx.data(), (int)pair_idx.size());
+                for (int k = 0; k < nb; k++) row_idx.push_back(k);
+            } else {
+                int roff = 0;
+                for (int k = 0; k < nch; k++) {
+                    int c = h->children[node * h->max_child + k];
+                    for (int t = 0; t < h->J_pair[c]->length; t++) pair_idx.push_back(h->J_pair[c]->data[t]);
+                    for (int t = 0; t < h->J_row[c]->length; t++) row_idx.push_back(h->J_row[c]->data[t] + roff);
+                    roff += sum_nbfp(h, h->J_pair[c]->data, h->J_pair[c]->length);
+                }
+            }
+            /* (2) proxy points around the node box */
+            const double *eb = h->enbox + 6 * node;
+            double width = eb[3], extent = h->box_extent[node];
+            double r1 = width * (0.5 + H2G_ALPHA_SUP), r2 = width * (0.5 + extent);
+            int nlayer = 1 + (int)std::ceil((extent - H2G_ALPHA_SUP) * (h->pp_nlayer_ext - 1));
+            std::vector<double> pp;
+            int num_pp;
+            proxy_points(r1, r2, nlayer, h->pp_npts_layer, pp, num_pp);
+            double *ppx = pp.data(), *ppy = ppx + num_pp, *ppz = ppy + num_pp;
+            for (int k = 0; k < num_pp; k++) {
+                ppx[k] += eb[0] + 0.5 * eb[3];
+                ppy[k] += eb[1] + 0.5 * eb[4];
+                ppz[k] += eb[2] + 0.5 * eb[5];
+            }
+            /* (3) far-field SSPs that are still skeletons */
+            std::vector<int> ff;
+            H2E_int_vec_p ov = h->ovlp_ff_idx[node];
+            for (int k = 0; k < ov->length; k++)
+                if (skel[ov->data[k]]) ff.push_back(ov->data[k]);
+            const int nrow_blk = sum_nbfp(h, pair_idx.data(), (int)pair_idx.size());
+            const int ff_ncol = sum_nbfp(h, ff.data(), (int)ff.size());
+            const int ncol_blk = 2 * nrow_blk;
+            std::vector<double> Ablk((size_t)nrow_blk * ncol_blk, 0.0);
+            Rng rng(0x5eed0000ULL + (uint64_t)node * 7919ULL);
+            /* (4) potential of proxy points, sketched to nrow_blk columns */
+            {
+                Sketch s;
+                gen_sketch(16, num_pp, nrow_blk, rng, s);
+                std::vector<int> map(num_pp, -1);
+                for (int c : s.col) map[c] = 1;
+                int cnt = 0;
+                for (int k = 0; k < num_pp; k++)
+                    if (map[k] >= 0) {
+                        map[k] = cnt;
+                        ppx[cnt] = ppx[k]; ppy[cnt] = ppy[k]; ppz[cnt] = ppz[k];
+                        cnt++;
+                    }
+                for (auto &c : s.col) c = map[c];
+                std::vector<double> Apot((size_t)nrow_blk * std::max(cnt, 1));
+                nai_pairs_to_mat(h, (int)pair_idx.size(), pair_idx.data(), cnt, ppx, ppy, ppz, Apot.data(), cnt);
+                sketch_apply(nrow_blk, s, Apot.data(), cnt, Ablk.data(), ncol_blk);
+            }
+            /* (5) ERI with overlapping far-field SSPs, sketched to nrow_blk columns */
+            {
+                Sketch s;
+                gen_sketch(16, ff_ncol, nrow_blk, rng, s);
+                std::vector<int> used(std::max(ff_ncol, 1), -1);
+                for (int c : s.col) used[c] = 1;
+                std::vector<int> cup;
+                for (int k = 0; k < ff_ncol; k++)
+                    if (used[k] >= 0) { used[k] = (int)cup.size(); cup.push_back(k); }
+                std::vector<int> pos, cup_new;
+                extract_sp_idx(h, cup.data(), (int)cup.size(), ff.data(), (int)ff.size(), pos, cup_new);
+                std::vector<int> ff1(pos.size());
+                for (size_t k = 0; k < pos.size(); k++) ff1[k] = ff[pos[k]];
+                for (auto &c : s.col) c = cup_new[used[c]];
+                const int ff_ncol1 = sum_nbfp(h, ff1.data(), (int)ff1.size());
+                std::vector<double> Aff((size_t)15 * 15 * std::max(ff_ncol1, 1));
+                int rcnt = 0;
+                for (size_t k = 0; k < pair_idx.size(); k++) {
+                    int nb = h->sp_nbfp[pair_idx[k]];
+                    eri_pairs_to_mat(h, 1, &pair_idx[k], (int)ff1.size(), ff1.data(), Aff.data(), ff_ncol1);
+                    sketch_apply(nb, s, Aff.data(), ff_ncol1, Ablk.data() + (size_t)rcnt * ncol_blk + nrow_blk, ncol_blk);
+                    rcnt += nb;
+                }
+            }
+            /* (6) normalise columns, keep candidate rows, ID */
+            {
+                std::vector<double> inv(ncol_blk, 0.0);
+                for (int c = 0; c < ncol_blk; c++) {
+                    double s = 0.0;
+                    for (int r = 0; r < nrow_blk; r++) s += Ablk[(size_t)r * ncol_blk + c] * Ablk[(size_t)r * ncol_blk + c];
+                    inv[c] = (s > 0.0) ? 1.0 / std::sqrt(s) : 0.0;
+                }
+                const int nsel = (int)row_idx.size();
+                H2E_dense_mat_p A = dmat_new(nsel, ncol_blk);
+                for (int r = 0; r < nsel; r++) {
+                    const double *src = Ablk.data() + (size_t)row_idx[r] * ncol_blk;
+                    double *dst = A->data + (size_t)r * ncol_blk;
+                    for (int c = 0; c < ncol_blk; c++) dst[c] = src[c] * inv[c];
+                }
+                H2E_int_vec_p J = ivec_new(std::max(nsel, 1));
+                H2E_dense_mat_p U = nullptr;
+                id_compress(A, rel_tol, &U, J);
+                dmat_free(&A);
+                h->U[node] = U;
+                /* (7) skeleton SSPs and their rows */
+                std::vector<int> sub_row(J->length);
+                for (int k = 0; k < J->length; k++) sub_row[k] = row_idx[J->data[k]];
+                std::vector<int> pos, rnew;
+                extract_sp_idx(h, sub_row.data(), (int)sub_row.size(), pair_idx.data(), (int)pair_idx.size(), pos, rnew);
+                H2E_int_vec_p jp = ivec_new(std::max((int)pos.size(), 1));
+                H2E_int_vec_p jr = ivec_new(std::max((int)rnew.size(), 1));
+                for (size_t k = 0; k < pos.size(); k++) jp->data[k] = pair_idx[pos[k]];
+                jp->length = (int)pos.size();
+                for (size_t k = 0; k < rnew.size(); k++) jr->data[k] = rnew[k];
+                jr->length = (int)rnew.size();
+                h->J_pair[node] = jp;
+                h->J_row[node] = jr;
+                ivec_free(&J);
+            }
+        }
+        /* skeleton flags for the next level up */
+        std::fill(skel.begin(), skel.end(), 0);
+        for (int jn = 0; jn < nlv; jn++) {
+            int node = lnodes[jn];
+            for (int k = 0; k < h->J_pair[node]->length; k++) skel[h->J_pair[node]->data[k]] = 1;
+        }
+        for (int leaf : lvl_leaf[lv])
+            for (int k = h->pt_cluster[2 * leaf]; k <= h->pt_cluster[2 * leaf + 1]; k++) skel[k] = 1;
+    }
+    for (int i = 0; i < n_node; i++) {
+        if (h->U[i] == nullptr) {
+            h->U[i] = dmat_new(1, 1);
+            h->U[i]->nrow = 0;
+            h->U[i]->ncol = 0;
+            h->U[i]->ld = 0;
+        } else {
+            size_t nr = h->U[i]->nrow, nc = h->U[i]->ncol;
+            h->mat_size[U_SIZE_IDX] += nr * nc;
+            h->mat_size[MV_FWD_SIZE_IDX] += nr * nc + nr + nc;
+            h->mat_size[MV_BWD_SIZE_IDX] += nr * nc + nr + nc;
+        }
+        if (h->J_row[i] == nullptr) h->J_row[i] = ivec_new(1);
+        if (h->J_pair[i] == nullptr) h->J_pair[i] = ivec_new(1);
+    }
+}
+
+/* Dense block -> dense or low-rank storage (src/H2ERI_build_H2.c:843-903). */
+H2E_dense_mat_p compress_block(H2E_dense_mat_p blk, double rel_tol)
+{
+    const int nr = blk->nrow, nc = blk->ncol;
+    H2E_dense_mat_p work = dmat_new(nr, nc);
+    if ((size_t)nr * nc > 0) std::memcpy(work->data, blk->data, sizeof(double) * (size_t)nr * nc);
+    H2E_int_vec_p J = ivec_new(std::max(nr, 1));
+    H2E_dense_mat_p U = nullptr;
+    id_compress(work, rel_tol, &U, J);
+    dmat_free(&work);
+    int r = J->length;
+    int old_size = nr * nc, new_size = (nr + nc) * r;
+    H2E_dense_mat_p res;
+    if (new_size > old_size * 4 / 5) {
+        res = dmat_new(nr, nc);
+        if (old_size > 0) std::memcpy(res->data, blk->data, sizeof(double) * (size_t)old_size);
+    } else {
+        res = dmat_new(1, new_size);
+        res->nrow = nr;
+        res->ncol = nc;
+        res->ld = -r;
+        double *Up = res->data, *Vt = Up + (size_t)nr * r;
+        std::memcpy(Up, U->data, sizeof(double) * (size_t)nr * r);
+        for (int l = 0; l < nc; l++)
+            for (int k = 0; k < r; k++) Vt[(size_t)l * r + k] = blk->data[(size_t)J->data[k] * nc + l];
+    }
+    dmat_free(&U);
+    ivec_free(&J);
+    return res;
+}
+
+/* Integer COO -> CSR with columns sorted per row (src/H2ERI_utils.c:121-146). */
+void coo_to_csr(int nrow, int nnz, const int *row, const int *col, const int *val, int *rp, int *ci, int *cv)
+{
+    std::memset(rp, 0, sizeof(int) * (nrow + 1));
+    for (int i = 0; i < nnz; i++) rp[row[i] + 1]++;
+    for (int i = 1; i <= nrow; i++) rp[i] += rp[i - 1];
+    std::vector<int> pos(rp, rp + nrow);
+    for (int i = 0; i < nnz; i++) {
+        int k = pos[row[i]]++;
+        ci[k] = col[i];
+        cv[k] = val[i];
+    }
+    for (int r = 0; r < nrow; r++) {
+        std::vector<std::pair<int, int>> e;
+        for (int k = rp[r]; k < rp[r + 1]; k++) e.push_back({ci[k], cv[k]});
+        std::sort(e.begin(), e.end());
+        for (int k = rp[r]; k < rp[r + 1]; k++) { ci[k] = e[k - rp[r]].first; cv[k] = e[k - rp[r]].second; }
+    }
+}
+
+/* ERI sub-block: rows = selected bf pairs of the bra SSPs, cols = selected
+ * bf pairs of the ket SSPs. sel_row/sel_col index into the concatenations of
+ * all bf pairs of bra / ket (nullptr = all). Row-major nrow x ncol. */
+void eri_block(H2ERI_p h, const int *bra, int nbra, const int *ket, int nket,
+               const int *sel_row, int nrow, const int *sel_col, int ncol, double *out)
+{
+    const int full_r = sum_nbfp(h, bra, nbra), full_c = sum_nbfp(h, ket, nket);
+    std::vector<double> full((size_t)full_r * full_c);
+    eri_pairs_to_mat(h, nbra, bra, nket, ket, full.data(), full_c);
+    for (int r = 0; r < nrow; r++) {
+        const double *src = full.data() + (size_t)(sel_row ? sel_row[r] : r) * full_c;
+        double *dst = out + (size_t)r * ncol;
+        if (sel_col)
+            for (int c = 0; c < ncol; c++) dst[c] = src[sel_col[c]];
+        else
+            std::memcpy(dst, src, sizeof(double) * ncol);
+    }
+}
+
+/* Coupling blocks (src/H2ERI_build_H2.c:910-1152). */
+void build_B(H2ERI_p h)
+{
+    const int n_pair = h->n_r_adm_pair, n_node = h->n_node;
+    h->n_B = n_pair;
+    h->B_nrow = (int *)std::malloc(sizeof(int) * std::max(n_pair, 1));
+    h->B_ncol = (int *)std::malloc(sizeof(int) * std::max(n_pair, 1));
+    h->B_ptr = (size_t *)std::malloc(sizeof(size_t) * (n_pair + 1));
+    h->node_n_r_adm = (int *)std::calloc(n_node, sizeof(int));
+    std::vector<int> pi, pj, pv;
+    for (int i = 0; i < n_pair; i++) {
+        int n0 = h->r_adm_pairs[2 * i], n1 = h->r_adm_pairs[2 * i + 1];
+        int l0 = h->node_level[n0], l1 = h->node_level[n1];
+        h->node_n_r_adm[n0]++;
+        h->node_n_r_adm[n1]++;
+        auto leaf_nbfp = [&](int n) {
+            return h->sp_bfp_sidx[h->pt_cluster[2 * n + 1] + 1] - h->sp_bfp_sidx[h->pt_cluster[2 * n]];
+        };
+        h->B_nrow[i] = (l0 >= l1) ? h->J_row[n0]->length : leaf_nbfp(n0);
+        h->B_ncol[i] = (l0 <= l1) ? h->J_row[n1]->length : leaf_nbfp(n1);
+        pi.push_back(n0); pj.push_back(n1); pv.push_back(i + 1);
+        pi.push_back(n1); pj.push_back(n0); pv.push_back(-(i + 1));
+    }
+    h->B_p2i_rowptr = (int *)std::malloc(sizeof(int) * (n_node + 1));
+    h->B_p2i_colidx = (int *)std::malloc(sizeof(int) * std::max<size_t>(pi.size(), 1));
+    h->B_p2i_val = (int *)std::malloc(sizeof(int) * std::max<size_t>(pi.size(), 1));
+    coo_to_csr(n_node, (int)pi.size(), pi.data(), pj.data(), pv.data(), h->B_p2i_rowptr, h->B_p2i_colidx, h->B_p2i_val);
+
+    h->c_B_blks = (H2E_dense_mat_p *)std::calloc(std::max(n_pair, 1), sizeof(H2E_dense_mat_p));
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < n_pair; i++) {
+        int n0 = h->r_adm_pairs[2 * i], n1 = h->r_adm_pairs[2 * i + 1];
+        int l0 = h->node_level[n0], l1 = h->node_level[n1];
+        std::vector<int> bra, ket;
+        const int *srow = nullptr, *scol = nullptr;
+        if (l0 >= l1) {
+            bra.assign(h->J_pair[n0]->data, h->J_pair[n0]->data + h->J_pair[n0]->length);
+            srow = h->J_row[n0]->data;
+        } else {
+            for (int k = h->pt_cluster[2 * n0]; k <= h->pt_cluster[2 * n0 + 1]; k++) bra.push_back(h->index_seq[k]);
+        }
+        if (l0 <= l1) {
+            ket.assign(h->J_pair[n1]->data, h->J_pair[n1]->data + h->J_pair[n1]->length);
+            scol = h->J_row[n1]->data;
+        } else {
+            for (int k = h->pt_cluster[2 * n1]; k <= h->pt_cluster[2 * n1 + 1]; k++) ket.push_back(h->index_seq[k]);
+        }
+        H2E_dense_mat_p blk = dmat_new(h->B_nrow[i], h->B_ncol[i]);
+        eri_block(h, bra.data(), (int)bra.size(), ket.data(), (int)ket.size(), srow, h->B_nrow[i], scol,
+                  h->B_ncol[i], blk->data);
+        h->c_B_blks[i] = compress_block(blk, h->QR_stop_tol);
+        dmat_free(&blk);
+    }
+    h->mat_size[MV_MID_SIZE_IDX] = 0;
+    h->B_ptr[0] = 0;
+    size_t total = 0;
+    std::vector<size_t> sizes(std::max(n_pair, 1));
+    for (int i = 0; i < n_pair; i++) {
+        size_t s = (size_t)h->c_B_blks[i]->size;
+        h->mat_size[MV_MID_SIZE_IDX] += s + 2 * (size_t)(h->B_nrow[i] + h->B_ncol[i]);
+        sizes[i] = s;
+        total += s;
+        h->B_ptr[i + 1] = h->B_ptr[i] + s;
+    }
+    partition_workload(n_pair, sizes.data(), total, h->n_thread, h->B_blk);
+    h->mat_size[B_SIZE_IDX] = total;
+}
+
+/* Near-field blocks (src/H2ERI_build_H2.c:1159-1403). Diagonal blocks are
+ * symmetric; only their upper shell-pair triangle is evaluated and mirrored. */
+void build_D(H2ERI_p h)
+{
+    const int n_leaf = h->n_leaf_node, n_pair = h->n_r_inadm_pair, n_node = h->n_node;
+    const int n_D = n_leaf + n_pair;
+    h->n_D = n_D;
+    h->D_nrow = (int *)std::malloc(sizeof(int) * std::max(n_D, 1));
+    h->D_ncol = (int *)std::malloc(sizeof(int) * std::max(n_D, 1));
+    h->D_ptr = (size_t *)std::malloc(sizeof(size_t) * (n_D + 1));
+    auto leaf_nbfp = [&](int n) {
+        return h->sp_bfp_sidx[h->pt_cluster[2 * n + 1] + 1] - h->sp_bfp_sidx[h->pt_cluster[2 * n]];
+    };
+    std::vector<int> pi, pj, pv;
+    for (int i = 0; i < n_leaf; i++) {
+        int node = h->height_nodes[i];
+        h->D_nrow[i] = h->D_ncol[i] = leaf_nbfp(node);
+        pi.push_back(node); pj.push_back(node); pv.push_back(i + 1);
+    }
+    for (int i = 0; i < n_pair; i++) {
+        int n0 = h->r_inadm_pairs[2 * i], n1 = h->r_inadm_pairs[2 * i + 1];
+        h->D_nrow[n_leaf + i] = leaf_nbfp(n0);
+        h->D_ncol[n_leaf + i] = leaf_nbfp(n1);
+        pi.push_back(n0); pj.push_back(n1); pv.push_back(n_leaf + i + 1);
+        pi.push_back(n1); pj.push_back(n0); pv.push_back(-(n_leaf + i + 1));
+    }
+    h->D_p2i_rowptr = (int *)std::malloc(sizeof(int) * (n_node + 1));
+    h->D_p2i_colidx = (int *)std::malloc(sizeof(int) * std::max<size_t>(pi.size(), 1));
+    h->D_p2i_val = (int *)std::malloc(sizeof(int) * std::max<size_t>(pi.size(), 1));
+    coo_to_csr(n_node, (int)pi.size(), pi.data(), pj.data(), pv.data(), h->D_p2i_rowptr, h->D_p2i_colidx, h->D_p2i_val);
+
+    h->c_D_blks = (H2E_dense_mat_p *)std::calloc(std::max(n_D, 1), sizeof(H2E_dense_mat_p));
+    /* larger blocks first for load balance */
+    std::vector<int> order(n_D);
+    for (int i = 0; i < n_D; i++) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        return (size_t)h->D_nrow[a] * h->D_ncol[a] > (size_t)h->D_nrow[b] * h->D_ncol[b];
+    });
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < n_D; t++) {
+        int i = order[t];
+        H2E_dense_mat_p blk = dmat_new(h->D_nrow[i], h->D_ncol[i]);
+        if (i < n_leaf) {
+            int node = h->height_nodes[i];
+            int ps = h->pt_cluster[2 * node], pe = h->pt_cluster[2 * node + 1];
+            int n = blk->nrow;
+            std::vector<double> buf(15 * 15 * 15 * 15);
+            for (int a = ps; a <= pe; a++) {
+                int ra = h->sp_bfp_sidx[a] - h->sp_bfp_sidx[ps], na = h->sp_nbfp[a];
+                const h2g_pair *pa = sp_pair(h, a);
+                for (int b = a; b <= pe; b++) {
+                    int rb = h->sp_bfp_sidx[b] - h->sp_bfp_sidx[ps], nb = h->sp_nbfp[b];
+                    h2g_eri_quartet(pa, sp_pair(h, b), buf.data());
+                    for (int x = 0; x < na; x++)
+                        for (int y = 0; y < nb; y++) {
+                            double v = buf[(size_t)x * nb + y];
+                            blk->data[(size_t)(ra + x) * n + rb + y] = v;
+                            blk->data[(size_t)(rb + y) * n + ra + x] = v;
+                        }
+                }
+            }
+        } else {
+            int n0 = h->r_inadm_pairs[2 * (i - n_leaf)], n1 = h->r_inadm_pairs[2 * (i - n_leaf) + 1];
+            std::vector<int> bra, ket;
+            for (int k = h->pt_cluster[2 * n0]; k <= h->pt_cluster[2 * n0 + 1]; k++) bra.push_back(k);
+            for (int k = h->pt_cluster[2 * n1]; k <= h->pt_cluster[2 * n1 + 1]; k++) ket.push_back(k);
+            eri_pairs_to_mat(h, (int)bra.size(), bra.data(), (int)ket.size(), ket.data(), blk->data, blk->ncol);
+        }
+        h->c_D_blks[i] = compress_block(blk, h->QR_stop_tol);
+        dmat_free(&blk);
+    }
+    h->mat_size[MV_DEN_SIZE_IDX] = 0;
+    h->D_ptr[0] = 0;
+    std::vector<size_t> sizes(std::max(n_D, 1));
+    size_t tot0 = 0, tot1 = 0;
+    for (int i = 0; i < n_D; i++) {
+        H2E_dense_mat_p d = h->c_D_blks[i];
+        size_t s = (size_t)d->size;
+        sizes[i] = s;
+        h->mat_size[MV_DEN_SIZE_IDX] += s + (size_t)(d->nrow + d->ncol) * (i < n_leaf ? 1 : 2);
+        if (i < n_leaf) tot0 += s; else tot1 += s;
+        h->D_ptr[i + 1] = h->D_ptr[i] + s;
+    }
+    partition_workload(n_leaf, sizes.data(), tot0, h->n_thread, h->D_blk0);
+    partition_workload(n_pair, sizes.data() + n_leaf, tot1, h->n_thread, h->D_blk1);
+    h->mat_size[D_SIZE_IDX] = tot0 + tot1;
+}
+
+}  // namespace
+
+void build_h2(H2ERI_p h)
+{
+    double t0 = wtime();
+    build_UJ_proxy(h);
+    double t1 = wtime();
+    build_B(h);
+    double t2 = wtime();
+    build_D(h);
+    double t3 = wtime();
+    h->timers[U_BUILD_TIMER_IDX] = t1 - t0;
+    h->timers[B_BUILD_TIMER_IDX] = t2 - t1;
+    h->timers[D_BUILD_TIMER_IDX] = t3 - t2;
+}
+
+}  // namespace h2g
+
+extern "C" void H2ERI_build_H2(H2ERI_p h2eri, const int BD_JIT)
+{
+    H2G_CHECK(BD_JIT == 0,
+              "H2ERI_build_H2: BD_JIT=1 (just-in-time B/D) is not supported; the GPU hot path needs the "
+              "blocks built ahead of time\n");
+    H2G_CHECK(h2eri->n_node > 0, "H2ERI_build_H2: call H2ERI_partition first\n");
+    h2eri->BD_JIT = 0;
+    h2g::build_h2(h2eri);
+}

@@ -1,0 +1,407 @@
+/*
+ * Gaussian integral engine: ERI (Obara-Saika VRR + Head-Gordon-Pople HRR) and
+ * point-charge potential integrals, plus the Boys function. See h2g_ints.h for
+ * the conventions (they follow what the reference expects from SIMINT:
+ * H2P-ERI src/CMS.c:387-482, src/H2ERI_partition.c:84-96).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <pthread.h>
+
+#include "h2g_ints.h"
+
+#define H2G_MAX_L    (2 * H2G_MAX_AM)          /* max total L on one side */
+#define H2G_MAX_M    (4 * H2G_MAX_AM + 1)      /* max Boys order used     */
+#define H2G_NCUM(L)  (((L) + 1) * ((L) + 2) * ((L) + 3) / 6)
+#define H2G_MAXCUM   H2G_NCUM(H2G_MAX_L)
+
+/* ------------------------------------------------------------------------ */
+/* Cartesian component tables                                               */
+/* ------------------------------------------------------------------------ */
+
+/* Flat index over all components with total L <= H2G_MAX_L, ordered by L then
+ * by the standard in-shell order. */
+static int g_lxyz[H2G_MAXCUM][3];
+static int g_cum[H2G_MAX_L + 2];             /* first flat index of each L     */
+static int g_dir[H2G_MAXCUM];                /* recurrence direction          */
+static int g_prev[H2G_MAXCUM];               /* c - 1_dir                      */
+static int g_prev2[H2G_MAXCUM];              /* c - 2_dir (or -1)              */
+static int g_minus[H2G_MAXCUM][3];           /* c - 1_i (or -1)                */
+static int g_plus[H2G_MAXCUM][3];            /* c + 1_i (or -1 beyond table)   */
+
+static int flat_index(int lx, int ly, int lz)
+{
+    int L = lx + ly + lz;
+    /* position inside shell L: components ordered by decreasing lx, then ly */
+    int pos = 0;
+    for (int x = L; x > lx; x--) pos += L - x + 1;
+    pos += (L - lx) - ly;
+    return g_cum[L] + pos;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Boys function table                                                      */
+/* ------------------------------------------------------------------------ */
+
+#define BOYS_H      0.05
+#define BOYS_TMAX   40.0
+#define BOYS_NGRID  801                 /* 0 .. 40 step 0.05 */
+#define BOYS_NTAY   7
+#define BOYS_MTAB   (H2G_MAX_M + BOYS_NTAY + 1)
+
+static double g_boys_tab[BOYS_NGRID][BOYS_MTAB];
+static pthread_once_t g_once = PTHREAD_ONCE_INIT;
+
+/* F_m(T) = exp(-T) sum_i (2T)^i / ((2m+1)(2m+3)...(2m+2i+1)), evaluated in
+ * long double; converges for every T (terms peak near i ~ T). */
+static long double boys_series(int m, long double T)
+{
+    long double term = 1.0L / (2 * m + 1), sum = term;
+    for (int i = 1; i < 2000; i++) {
+        term *= 2.0L * T / (long double)(2 * m + 2 * i + 1);
+        sum += term;
+        if (term < sum * 1e-21L) break;
+    }
+    return expl(-T) * sum;
+}
+
+static void init_tables(void)
+{
+    int idx = 0;
+    for (int L = 0; L <= H2G_MAX_L; L++) {
+        g_cum[L] = idx;
+        for (int lx = L; lx >= 0; lx--)
+            for (int ly = L - lx; ly >= 0; ly--) {
+                g_lxyz[idx][0] = lx; g_lxyz[idx][1] = ly; g_lxyz[idx][2] = L - lx - ly;
+                idx++;
+            }
+    }
+    g_cum[H2G_MAX_L + 1] = idx;
+    for (int c = 0; c < idx; c++) {
+        const int *l = g_lxyz[c];
+        for (int i = 0; i < 3; i++) {
+            int t[3] = {l[0], l[1], l[2]};
+            t[i]--;
+            g_minus[c][i] = (t[i] >= 0) ? flat_index(t[0], t[1], t[2]) : -1;
+            t[i] += 2;
+            g_plus[c][i] = (t[0] + t[1] + t[2] <= H2G_MAX_L) ? flat_index(t[0], t[1], t[2]) : -1;
+        }
+        if (c == 0) { g_dir[c] = -1; g_prev[c] = -1; g_prev2[c] = -1; continue; }
+        int d = (l[0] > 0) ? 0 : ((l[1] > 0) ? 1 : 2);
+        g_dir[c] = d;
+        g_prev[c] = g_minus[c][d];
+        g_prev2[c] = (l[d] >= 2) ? g_minus[g_prev[c]][d] : -1;
+    }
+    for (int k = 0; k < BOYS_NGRID; k++) {
+        long double T = (long double)k * BOYS_H;
+        for (int m = 0; m < BOYS_MTAB; m++) g_boys_tab[k][m] = (double)boys_series(m, T);
+    }
+}
+
+void h2g_ints_init(void) { pthread_once(&g_once, init_tables); }
+
+void h2g_boys(int mmax, double T, double *F)
+{
+    if (T < BOYS_TMAX) {
+        int k = (int)(T / BOYS_H + 0.5);
+        double d = T - k * BOYS_H;                   /* |d| <= h/2 */
+        const double *row = g_boys_tab[k];
+        for (int m = 0; m <= mmax; m++) {
+            /* F_m(T_k + d) = sum_j F_{m+j}(T_k) (-d)^j / j! */
+            double s = 0.0, f = 1.0;
+            for (int j = 0; j < BOYS_NTAY; j++) {
+                s += row[m + j] * f;
+                f *= -d / (double)(j + 1);
+            }
+            F[m] = s;
+        }
+    } else {
+        double et = exp(-T), inv2t = 0.5 / T;
+        F[0] = 0.5 * sqrt(M_PI / T);                  /* erf(sqrt(T)) == 1 here */
+        for (int m = 0; m < mmax; m++) F[m + 1] = ((2 * m + 1) * F[m] - et) * inv2t;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Shell normalisation                                                      */
+/* ------------------------------------------------------------------------ */
+
+static double dfact_odd(int L) /* (2L-1)!! with (-1)!! = 1 */
+{
+    double r = 1.0;
+    for (int k = 2 * L - 1; k > 1; k -= 2) r *= k;
+    return r;
+}
+
+void h2g_normalize_shell(int am, int nprim, const double *alpha, double *coef)
+{
+    const double m = am + 1.5, m2 = 0.5 * m;
+    double sum = 0.0;
+    for (int j = 0; j < nprim; j++)
+        for (int k = 0; k < nprim; k++)
+            sum += coef[j] * coef[k] * pow(alpha[j] * alpha[k], m2) / pow(alpha[j] + alpha[k], m);
+    /* <x^L g_j | x^L g_k> for raw Gaussians = pi^1.5 (2L-1)!! / (2^L (a_j+a_k)^(L+1.5)) */
+    double fac = pow(M_PI, 1.5) * dfact_odd(am) / pow(2.0, am);
+    double norm = 1.0 / sqrt(sum * fac);
+    for (int j = 0; j < nprim; j++) coef[j] *= norm * pow(alpha[j], m2);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Primitive-pair data                                                      */
+/* ------------------------------------------------------------------------ */
+
+void h2g_pair_init(h2g_pair *pr, const h2g_shell *A, const h2g_shell *B)
+{
+    h2g_ints_init();
+    pr->am1 = A->am; pr->am2 = B->am;
+    pr->A[0] = A->x; pr->A[1] = A->y; pr->A[2] = A->z;
+    pr->B[0] = B->x; pr->B[1] = B->y; pr->B[2] = B->z;
+    int np = A->nprim * B->nprim;
+    pr->P = (double *)malloc(sizeof(double) * (size_t)np * 3);
+    pr->p = (double *)malloc(sizeof(double) * (size_t)np);
+    pr->K = (double *)malloc(sizeof(double) * (size_t)np);
+    pr->bexp = (double *)malloc(sizeof(double) * (size_t)np);
+    double ab2 = 0.0;
+    for (int d = 0; d < 3; d++) ab2 += (pr->A[d] - pr->B[d]) * (pr->A[d] - pr->B[d]);
+    int n = 0;
+    for (int i = 0; i < A->nprim; i++)
+        for (int j = 0; j < B->nprim; j++) {
+            double a = A->alpha[i], b = B->alpha[j], p = a + b;
+            double K = A->coef[i] * B->coef[j] * exp(-a * b / p * ab2);
+            if (fabs(K) < 1e-30) continue;
+            pr->p[n] = p;
+            pr->K[n] = K;
+            pr->bexp[n] = b;
+            for (int d = 0; d < 3; d++) pr->P[3 * n + d] = (a * pr->A[d] + b * pr->B[d]) / p;
+            n++;
+        }
+    pr->nprim = n;
+}
+
+void h2g_pair_free(h2g_pair *pr)
+{
+    free(pr->P); free(pr->p); free(pr->K); free(pr->bexp);
+    pr->P = pr->p = pr->K = pr->bexp = NULL;
+    pr->nprim = 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Horizontal recurrence                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Transfer angular momentum from the first to the second index of a pair:
+ *   (a, b + 1_i| = (a + 1_i, b| + AB_i (a, b|
+ * in:  src[e * stride] for flat e with l1 <= |e| <= l1 + l2 (flat cumulative
+ *      index), repeated over `nrep` independent trailing entries (stride apart
+ *      handled by caller through `nrep` contiguous values per e).
+ * out: dst[(ia * nb + ib) * nrep + r] with ia over comps of l1, ib over l2. */
+static void hrr(int l1, int l2, const double AB[3], const double *src, int nrep, double *dst, double *work)
+{
+    const int na = h2g_ncart(l1), nb = h2g_ncart(l2);
+    if (l2 == 0) {
+        memcpy(dst, src + (size_t)g_cum[l1] * nrep, sizeof(double) * (size_t)na * nrep);
+        return;
+    }
+    /* cur[e][b][r]: e flat over cumulative index, b within shell of current level j */
+    const int ne = g_cum[l1 + l2 + 1];
+    double *cur = work, *nxt = work + (size_t)ne * h2g_ncart(l2) * nrep;
+    /* level 0: b = s */
+    for (int e = g_cum[l1]; e < ne; e++)
+        memcpy(cur + (size_t)e * nrep, src + (size_t)e * nrep, sizeof(double) * nrep);
+    for (int j = 1; j <= l2; j++) {
+        int nbj = h2g_ncart(j), nbp = h2g_ncart(j - 1);
+        int emax = g_cum[l1 + l2 - j + 1];
+        for (int e = g_cum[l1]; e < emax; e++) {
+            for (int ib = 0; ib < nbj; ib++) {
+                int bf = g_cum[j] + ib;
+                int d = g_dir[bf];
+                int bp = g_prev[bf] - g_cum[j - 1];
+                int ep = g_plus[e][d];
+                const double *x1 = cur + ((size_t)ep * nbp + bp) * nrep;
+                const double *x2 = cur + ((size_t)e * nbp + bp) * nrep;
+                double *y = nxt + ((size_t)e * nbj + ib) * nrep;
+                double ab = AB[d];
+                for (int r = 0; r < nrep; r++) y[r] = x1[r] + ab * x2[r];
+            }
+        }
+        double *t = cur; cur = nxt; nxt = t;
+    }
+    for (int ia = 0; ia < na; ia++)
+        memcpy(dst + (size_t)ia * nb * nrep, cur + (size_t)(g_cum[l1] + ia) * nb * nrep,
+               sizeof(double) * (size_t)nb * nrep);
+}
+
+/* ------------------------------------------------------------------------ */
+/* ERI                                                                      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    double vrr[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L) * (H2G_MAX_M + 1)];
+    double acc[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L)];
+    double t1[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L) * 8];
+    double w1[2 * H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L) * 16];
+} eri_ws;
+
+static __thread eri_ws *tls_ws = NULL;
+
+static eri_ws *get_ws(void)
+{
+    if (tls_ws == NULL) tls_ws = (eri_ws *)malloc(sizeof(eri_ws));
+    return tls_ws;
+}
+
+void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
+{
+    const int la = bra->am1, lb = bra->am2, lc = ket->am1, ld = ket->am2;
+    const int La = la + lb, Lc = lc + ld, M = La + Lc;
+    const int nA = h2g_ncart(la), nB = h2g_ncart(lb), nC = h2g_ncart(lc), nD = h2g_ncart(ld);
+    const int ne = g_cum[La + 1], nf = g_cum[Lc + 1], nm = M + 1;
+    eri_ws *ws = get_ws();
+    double *acc = ws->acc;
+    const double two_pi_52 = 2.0 * pow(M_PI, 2.5);
+
+    if (M == 0) {
+        double s = 0.0, F[1];
+        for (int i = 0; i < bra->nprim; i++) {
+            const double p = bra->p[i], *P = bra->P + 3 * i;
+            for (int j = 0; j < ket->nprim; j++) {
+                const double q = ket->p[j], *Q = ket->P + 3 * j;
+                double pq = p + q, rho = p * q / pq;
+                double dx = P[0] - Q[0], dy = P[1] - Q[1], dz = P[2] - Q[2];
+                h2g_boys(0, rho * (dx * dx + dy * dy + dz * dz), F);
+                s += two_pi_52 / (p * q * sqrt(pq)) * bra->K[i] * ket->K[j] * F[0];
+            }
+        }
+        out[0] = s;
+        return;
+    }
+
+    memset(acc, 0, sizeof(double) * (size_t)ne * nf);
+    double *V = ws->vrr;
+    /* V[(e * nf + f) * nm + m] */
+    for (int i = 0; i < bra->nprim; i++) {
+        const double p = bra->p[i], *P = bra->P + 3 * i;
+        double PA[3] = {P[0] - bra->A[0], P[1] - bra->A[1], P[2] - bra->A[2]};
+        for (int j = 0; j < ket->nprim; j++) {
+            const double q = ket->p[j], *Q = ket->P + 3 * j;
+            const double pq = p + q, rho = p * q / pq;
+            double W[3], WP[3], WQ[3], QC[3];
+            double PQ2 = 0.0;
+            for (int d = 0; d < 3; d++) {
+                W[d] = (p * P[d] + q * Q[d]) / pq;
+                WP[d] = W[d] - P[d];
+                WQ[d] = W[d] - Q[d];
+                QC[d] = Q[d] - ket->A[d];
+                PQ2 += (P[d] - Q[d]) * (P[d] - Q[d]);
+            }
+            double F[H2G_MAX_M + 1];
+            h2g_boys(M, rho * PQ2, F);
+            const double pref = two_pi_52 / (p * q * sqrt(pq)) * bra->K[i] * ket->K[j];
+            for (int m = 0; m <= M; m++) V[m] = pref * F[m];
+            const double i2p = 0.5 / p, rp = rho / p, i2q = 0.5 / q, rq = rho / q, i2pq = 0.5 / pq;
+            /* bra side: [e|0]^(m) */
+            for (int c = 1; c < ne; c++) {
+                const int L = g_lxyz[c][0] + g_lxyz[c][1] + g_lxyz[c][2];
+                const int d = g_dir[c], e = g_prev[c], e2 = g_prev2[c];
+                const double ei = (double)(g_lxyz[c][d] - 1);
+                double *vc = V + (size_t)c * nf * nm;
+                const double *ve = V + (size_t)e * nf * nm;
+                for (int m = 0; m <= M - L; m++) {
+                    double v = PA[d] * ve[m] + WP[d] * ve[m + 1];
+                    if (e2 >= 0) {
+                        const double *ve2 = V + (size_t)e2 * nf * nm;
+                        v += ei * i2p * (ve2[m] - rp * ve2[m + 1]);
+                    }
+                    vc[m] = v;
+                }
+            }
+            /* ket side: [e|f]^(m) */
+            for (int c = 1; c < nf; c++) {
+                const int Lf = g_lxyz[c][0] + g_lxyz[c][1] + g_lxyz[c][2];
+                const int d = g_dir[c], f = g_prev[c], f2 = g_prev2[c];
+                const double fi = (double)(g_lxyz[c][d] - 1);
+                for (int e = 0; e < ne; e++) {
+                    const int Le = g_lxyz[e][0] + g_lxyz[e][1] + g_lxyz[e][2];
+                    const int mmax = M - Le - Lf;
+                    if (mmax < 0) continue;
+                    double *vc = V + ((size_t)e * nf + c) * nm;
+                    const double *vf = V + ((size_t)e * nf + f) * nm;
+                    const double *vf2 = (f2 >= 0) ? V + ((size_t)e * nf + f2) * nm : NULL;
+                    const int em = g_minus[e][d];
+                    const double ed = (double)g_lxyz[e][d];
+                    const double *vem = (em >= 0) ? V + ((size_t)em * nf + f) * nm : NULL;
+                    for (int m = 0; m <= mmax; m++) {
+                        double v = QC[d] * vf[m] + WQ[d] * vf[m + 1];
+                        if (vf2) v += fi * i2q * (vf2[m] - rq * vf2[m + 1]);
+                        if (vem) v += ed * i2pq * vem[m + 1];
+                        vc[m] = v;
+                    }
+                }
+            }
+            for (int e = g_cum[la]; e < ne; e++)
+                for (int f = g_cum[lc]; f < nf; f++)
+                    acc[e * nf + f] += V[((size_t)e * nf + f) * nm];
+        }
+    }
+
+    /* HRR on the bra: acc[e][f] -> t1[(a b)][f], f kept as a trailing vector */
+    double ABv[3] = {bra->A[0] - bra->B[0], bra->A[1] - bra->B[1], bra->A[2] - bra->B[2]};
+    double CDv[3] = {ket->A[0] - ket->B[0], ket->A[1] - ket->B[1], ket->A[2] - ket->B[2]};
+    double *t1 = ws->t1;
+    hrr(la, lb, ABv, acc, nf, t1, ws->w1);
+    /* HRR on the ket for each (a,b) */
+    const int nab = nA * nB;
+    for (int ab = 0; ab < nab; ab++)
+        hrr(lc, ld, CDv, t1 + (size_t)ab * nf, 1, out + (size_t)ab * nC * nD, ws->w1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Point-charge potential integrals                                         */
+/* ------------------------------------------------------------------------ */
+
+void h2g_potential(const h2g_shell *A, const h2g_shell *B,
+                   double cx, double cy, double cz, double charge, double *out)
+{
+    h2g_ints_init();
+    const int la = A->am, lb = B->am, L = la + lb;
+    const int ne = g_cum[L + 1], nm = L + 1;
+    double acc[H2G_NCUM(H2G_MAX_L)];
+    double V[H2G_NCUM(H2G_MAX_L) * (H2G_MAX_L + 1)];
+    double work[2 * H2G_NCUM(H2G_MAX_L) * 16];
+    memset(acc, 0, sizeof(double) * ne);
+    const double Av[3] = {A->x, A->y, A->z}, Bv[3] = {B->x, B->y, B->z}, C[3] = {cx, cy, cz};
+    double ab2 = 0.0;
+    for (int d = 0; d < 3; d++) ab2 += (Av[d] - Bv[d]) * (Av[d] - Bv[d]);
+    for (int i = 0; i < A->nprim; i++)
+        for (int j = 0; j < B->nprim; j++) {
+            const double a = A->alpha[i], b = B->alpha[j], p = a + b;
+            const double K = A->coef[i] * B->coef[j] * exp(-a * b / p * ab2);
+            double P[3], PA[3], PC[3], PC2 = 0.0;
+            for (int d = 0; d < 3; d++) {
+                P[d] = (a * Av[d] + b * Bv[d]) / p;
+                PA[d] = P[d] - Av[d];
+                PC[d] = P[d] - C[d];
+                PC2 += PC[d] * PC[d];
+            }
+            double F[H2G_MAX_L + 1];
+            h2g_boys(L, p * PC2, F);
+            const double pref = -charge * 2.0 * M_PI / p * K;
+            for (int m = 0; m <= L; m++) V[m] = pref * F[m];
+            const double i2p = 0.5 / p;
+            /* [e+1_i]^(m) = PA_i [e]^(m) - PC_i [e]^(m+1) + e_i/(2p) ([e-1_i]^(m) - [e-1_i]^(m+1)) */
+            for (int c = 1; c < ne; c++) {
+                const int Lc = g_lxyz[c][0] + g_lxyz[c][1] + g_lxyz[c][2];
+                const int d = g_dir[c], e = g_prev[c], e2 = g_prev2[c];
+                const double ei = (double)(g_lxyz[c][d] - 1);
+                for (int m = 0; m <= L - Lc; m++) {
+                    double v = PA[d] * V[e * nm + m] - PC[d] * V[e * nm + m + 1];
+                    if (e2 >= 0) v += ei * i2p * (V[e2 * nm + m] - V[e2 * nm + m + 1]);
+                    V[c * nm + m] = v;
+                }
+            }
+            for (int e = g_cum[la]; e < ne; e++) acc[e] += V[e * nm];
+        }
+    double ABv[3] = {Av[0] - Bv[0], Av[1] - Bv[1], Av[2] - Bv[2]};
+    hrr(la, lb, ABv, acc, 1, out, work);
+}

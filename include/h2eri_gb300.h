@@ -1,0 +1,106 @@
+/*
+ * h2eri_gb300: GPU (sm_103a) drop-in for the H2P-ERI C API.
+ *
+ * The entry points in the first block keep the reference names, argument
+ * meanings and void/abort error behaviour; each comment names the reference
+ * declaration it replaces. Set-up (init, shells, partition, build_H2) runs on
+ * the host once per geometry; the hot path (matvec, Coulomb, exchange) runs on
+ * the GPU with the H2 blocks resident in device memory after the first call
+ * (or an explicit H2ERI_gpu_upload). There is no CPU fallback: on a machine
+ * without a usable CUDA device the hot-path calls print the reason and abort,
+ * the int-returning extensions return a nonzero status instead.
+ *
+ * Not re-entrant per H2ERI_p (same as the reference): one host thread at a
+ * time may use a given structure.
+ */
+#ifndef H2ERI_GB300_H
+#define H2ERI_GB300_H
+
+#include "h2eri_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Reference API                                                             */
+/* ------------------------------------------------------------------------ */
+
+/* replaces H2P-ERI src/H2ERI_typedef.h:169 */
+void H2ERI_init(H2ERI_p *h2eri_, const double scr_tol, const double ext_tol, const double QR_tol);
+/* replaces src/H2ERI_typedef.h:174; also releases the GPU state */
+void H2ERI_destroy(H2ERI_p h2eri);
+/* replaces src/H2ERI_typedef.h:179; adds GPU columns when timings exist */
+void H2ERI_print_statistic(H2ERI_p h2eri);
+/* replaces src/CMS.h:49 */
+void CMS_read_mol_file(const char *mol_fname, int *natom_, int *nshell_, shell_t **shells_);
+/* replaces src/CMS.h:55 */
+void CMS_destroy_shells(const int nshell, shell_t *shells);
+/* replaces src/H2ERI_shell_operations.h:25 */
+void H2ERI_process_shells(H2ERI_p h2eri);
+/* replaces src/H2ERI_partition.h:28 */
+void H2ERI_partition(H2ERI_p h2eri);
+/* replaces src/H2ERI_build_H2.h:16; only BD_JIT == 0 is supported (the GPU
+ * path needs the blocks built ahead of time); BD_JIT == 1 aborts */
+void H2ERI_build_H2(H2ERI_p h2eri, const int BD_JIT);
+/* replaces src/H2ERI_matvec.h:16: y = A x over the krnl_mat_size SSP
+ * basis-function-pair space; x, y host arrays */
+void H2ERI_matvec(H2ERI_p h2eri, const double *x, double *y);
+/* replaces src/H2ERI_build_Coulomb.h:16: J from a symmetric density, both
+ * num_bf x num_bf row-major host arrays */
+void H2ERI_build_Coulomb(H2ERI_p h2eri, const double *den_mat, double *J_mat);
+/* replaces src/H2ERI_build_exchange.h:16: K from a symmetric density */
+void H2ERI_build_exchange(H2ERI_p h2eri, const double *den_mat, double *K_mat);
+/* replace src/H2ERI_build_exchange.h:19,22; the GPU exchange keeps its own
+ * device workspace, these only manage the host-side field */
+void H2ERI_exchange_workbuf_init(H2ERI_p h2eri);
+void H2ERI_exchange_workbuf_free(H2ERI_p h2eri);
+/* replaces src/H2ERI_typedef.c:303 (exported, undeclared in the reference) */
+void H2E_reset_timers(H2ERI_p h2eri);
+
+/* ------------------------------------------------------------------------ */
+/* GPU extensions (no counterpart in the reference)                          */
+/* ------------------------------------------------------------------------ */
+
+/* Precision of the far-field (U, B) blocks on the GPU. */
+#define H2ERI_GPU_FP64   0   /* everything FP64                                   */
+#define H2ERI_GPU_MIXED  1   /* U, B in FP32 (hi+lo split where needed), D FP64   */
+
+/* Upload the H2 blocks and tree arrays of a built structure to the current
+ * CUDA device. Called implicitly by the first hot-path call. Returns 0 on
+ * success. */
+int H2ERI_gpu_upload(H2ERI_p h2eri);
+/* Free the device copy of a structure (called by H2ERI_destroy). */
+void H2ERI_gpu_release(H2ERI_p h2eri);
+/* Select the far-field precision for subsequent calls (default FP64).
+ * Re-uploads the far-field blocks if needed. Returns 0 on success. */
+int H2ERI_gpu_set_precision(H2ERI_p h2eri, int mode);
+/* Message of the last failure of any gpu extension call on this thread
+ * ("" if none). */
+const char *H2ERI_gpu_last_error(void);
+
+/* y = A x for nvec vectors stored back to back ([nvec][krnl_mat_size]),
+ * host arrays. Returns 0 on success. */
+int H2ERI_matvec_multi(H2ERI_p h2eri, int nvec, const double *x, double *y);
+/* Same on device arrays, enqueued on a CUDA stream (cudaStream_t passed as
+ * void*, NULL = the library's stream); returns after enqueueing. */
+int H2ERI_matvec_device(H2ERI_p h2eri, int nvec, const double *d_x, double *d_y, void *stream);
+/* J for n_den densities stored back to back ([n_den][num_bf][num_bf]) on the
+ * host. Returns 0 on success. */
+int H2ERI_build_Coulomb_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *J_mats);
+/* Same on device arrays, enqueued on a stream. */
+int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double *d_den, double *d_J, void *stream);
+/* K on device arrays, enqueued on a stream. Returns 0 on success. */
+int H2ERI_build_exchange_device(H2ERI_p h2eri, const double *d_den, double *d_K, void *stream);
+
+/* Save / load the H2 representation (tree, pair lists, U, B, D and the
+ * basis-function bookkeeping used by J and K) in a self-describing binary
+ * file, so the same blocks can be applied on another machine or process. */
+int H2ERI_save_representation(H2ERI_p h2eri, const char *path);
+int H2ERI_load_representation(const char *path, H2ERI_p *h2eri_);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
