@@ -1,0 +1,344 @@
+"""Benchmark: Coulomb (J) builds per second through the H2 representation of
+the ERI tensor, C30H62 (all-trans zigzag, cc-pVDZ Cartesian, 760 basis
+functions), QR tolerance 1e-8, one seeded density (n_occ = 121).
+
+Default (GPU) arm: the representation is built on the host (set-up, not
+timed), uploaded once, then each step is one J build
+(uncontract -> H2 matvec -> contract) with the density already in HBM. The
+e2e figure times the reference-signature host API (density H2D, build,
+J D2H) per step. Precision: mixed (far-field FP32 / FP32 pairs, near field
+compensated FP32 pairs) when available, else FP64; the FP64 figure is
+always reported beside it, together with the relative error of each against
+the FP64 CPU oracle.
+
+--impl reference: the reference's CPU implementation of this path, timed on
+the host cores (the oracle restatement of H2ERI_build_Coulomb, OpenMP over
+all host threads), same workload and metric.
+
+Multi-GPU (torchrun): one independent replica per GPU (the path does not
+shard: a J build has no exchange step); value = builds of all ranks / max
+time over ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "h2p-eri_gb300"))
+sys.path.insert(0, REPO)
+
+WORKLOAD = {"workload": "J build C30H62 cc-pVDZ (760 bf, cartesian), QR tol 1e-8, 1 density n_occ=121",
+            "molecule": "C30H62", "n_carbon": 30, "qr_tol": 1e-8, "n_occ": 121, "seed": 2000,
+            "inputs_vs_L2": "H2 representation ~1.8 GB read per step > 129 MB L2 (no flush needed)"}
+METRIC = "J builds/s C30H62 (mixed vs FP64) at relerr<=1e-8"
+CACHE_DIR = os.path.join(tempfile.gettempdir(), "h2eri_gb300_cache")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def representation(hg, molecules, rank, ws, barrier):
+    """Build (rank 0) or load the cached representation of the workload."""
+    os.makedirs(CACHE_DIR, exist_ok=True)
+    path = os.path.join(CACHE_DIR, f"alk{WORKLOAD['n_carbon']}_{WORKLOAD['qr_tol']:g}.h2r")
+    setup_s = None
+    if rank == 0 and not os.path.exists(path):
+        mol = os.path.join(CACHE_DIR, f"alk{WORKLOAD['n_carbon']}.mol")
+        molecules.write_alkane(mol, WORKLOAD["n_carbon"])
+        t0 = time.perf_counter()
+        h = hg.H2ERI.from_mol(mol, qr_tol=WORKLOAD["qr_tol"])
+        setup_s = time.perf_counter() - t0
+        tmp = path + ".tmp"
+        h.save(tmp)
+        os.replace(tmp, path)
+        log(f"set-up (host, not timed): {setup_s:.1f} s")
+    else:
+        h = None
+    barrier()
+    if h is None:
+        h = hg.H2ERI.load(path)
+    return h, setup_s
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(orc, h, D, budget_s=12.0, max_builds=40):
+    """Oracle restatement of H2ERI_build_Coulomb on the host cores."""
+    J = np.zeros_like(D)
+    orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)   # warm-up
+    n, t0 = 0, time.perf_counter()
+    while n < max_builds and time.perf_counter() - t0 < budget_s:
+        orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)
+        n += 1
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt, J
+
+
+def load_oracle():
+    from oracle import build_oracle
+    orc = ctypes.CDLL(build_oracle.build())
+    for f in ("oracle_matvec", "oracle_build_Coulomb"):
+        getattr(orc, f).argtypes = [ctypes.c_void_p] * 3
+        getattr(orc, f).restype = None
+    return orc
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import h2eri_gb300 as hg
+    from h2eri_gb300 import build as hb, molecules
+    hb.build()
+    orc = load_oracle()
+    h, _ = representation(hg, molecules, 0, 1, lambda: None)
+    D = molecules.seeded_density(h.num_bf, WORKLOAD["n_occ"], WORKLOAD["seed"])
+    J = np.zeros_like(D)
+    for _ in range(args.warmup):
+        orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    v = args.steps / dt
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "J builds/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (generated alkane geometry, seeded density)", "config": dict(WORKLOAD),
+           "cpu_baseline": {"value": v, "unit": "J builds/s", "cores": cores, "kind": "port",
+                            "sample": f"{args.steps} J builds of the workload"},
+           "e2e": {"value": v, "unit": "J builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    h.destroy()
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    import h2eri_gb300 as hg
+    from h2eri_gb300 import build as hb, molecules
+    if rank == 0:
+        hb.build()
+    barrier()
+    h, setup_s = representation(hg, molecules, rank, ws, barrier)
+    L = hg.lib()
+    nbf = h.num_bf
+    D = molecules.seeded_density(nbf, WORKLOAD["n_occ"], WORKLOAD["seed"])
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    dD = torch.tensor(D, device="cuda")
+    dJ = torch.empty_like(dD)
+    t_up = time.perf_counter()
+    h.upload()
+    upload_s = time.perf_counter() - t_up
+    rep = h.report()
+    launches_per_J = int(rep["launches_per_matvec"]) + 2
+
+    modes = ["fp64"]
+    if args.precision in ("auto", "mixed"):
+        if L.H2ERI_gpu_set_precision(h.handle, hg.MIXED) == 0:
+            modes.append("mixed")
+        elif args.precision == "mixed":
+            raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+
+    def device_run(mode):
+        L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if mode == "mixed" else hg.FP64)
+        for _ in range(args.warmup):
+            if L.H2ERI_build_Coulomb_device(h.handle, 1, dD.data_ptr(), dJ.data_ptr(), sp) != 0:
+                raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                L.H2ERI_build_Coulomb_device(h.handle, 1, dD.data_ptr(), dJ.data_ptr(), sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        return ms, dJ.cpu().numpy(), clk.summary()
+
+    results = {}
+    for mode in modes:
+        ms, J, clk = device_run(mode)
+        results[mode] = {"ms": ms, "J": J, "clocks": clk}
+    best = "mixed" if "mixed" in results else "fp64"
+    L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if best == "mixed" else hg.FP64)
+
+    # e2e through the reference-signature host API with pinned host buffers
+    hD = torch.from_numpy(D).pin_memory()
+    hJ = torch.empty_like(hD).pin_memory()
+    for _ in range(args.warmup):
+        L.H2ERI_build_Coulomb_multi(h.handle, 1, hD.data_ptr(), hJ.data_ptr())
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.H2ERI_build_Coulomb_multi(h.handle, 1, hD.data_ptr(), hJ.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ms_best = max_over_ranks(results[best]["ms"])
+    ms_fp64 = max_over_ranks(results["fp64"]["ms"])
+    e2e_s = max_over_ranks(e2e_s)
+    if rank != 0:
+        barrier()
+        return
+
+    orc = load_oracle()
+    cpu_v, cpu_n, cpu_dt, J_ref = cpu_baseline(orc, h, D)
+    def rel(J):
+        return float(np.linalg.norm(J - J_ref) / np.linalg.norm(J_ref))
+
+    step_s = ms_best / 1e3 / args.steps
+    value = ws * args.steps / (ms_best / 1e3)
+    alg_bytes = rep["alg_matrix_bytes"] + rep["alg_vector_bytes"] + 2 * 8 * nbf * nbf
+    if best == "mixed":
+        rep_m = h.report()
+        alg_bytes = rep_m["alg_matrix_bytes"] + rep_m["alg_vector_bytes"] + 2 * 8 * nbf * nbf
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / step_s / 1e9
+    clk = results[best]["clocks"]
+    out = {
+        "metric": METRIC, "value": value, "unit": "J builds/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32x2+f64" if best == "mixed" else "f64",
+        "data": "synthetic (generated alkane geometry, seeded density)",
+        "config": dict(WORKLOAD, precision=best, parallelism=f"replicas x{ws}"),
+        "fp64": {"value": ws * args.steps / (ms_fp64 / 1e3), "unit": "J builds/s",
+                 "ms_per_step": ms_fp64 / args.steps, "relerr_vs_fp64_oracle": rel(results["fp64"]["J"])},
+        "relerr_vs_fp64_oracle": rel(results[best]["J"]),
+        "e2e": {"value": ws * args.steps / e2e_s, "unit": "J builds/s", "h2d_bytes_per_step": 8 * nbf * nbf,
+                "d2h_bytes_per_step": 8 * nbf * nbf},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_tile (all tile launches of one J build)",
+                     "alg_bytes_per_step": alg_bytes, "peak_kind": peak_kind},
+        "cpu_baseline": {"value": cpu_v, "unit": "J builds/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{cpu_n} J builds of the workload in {cpu_dt:.1f} s (oracle, OpenMP)"},
+        "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
+        "gpu_launches": launches_per_J * args.steps,
+        "setup_s": setup_s, "upload_s": upload_s,
+    }
+    print(json.dumps(out), flush=True)
+    barrier()
+    h.destroy()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

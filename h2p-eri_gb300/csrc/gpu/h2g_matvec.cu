@@ -761,6 +761,24 @@ extern "C" void H2ERI_build_Coulomb(H2ERI_p h2eri, const double *den_mat, double
     if (H2ERI_build_Coulomb_multi(h2eri, 1, den_mat, J_mat) != 0) fatal("H2ERI_build_Coulomb");
 }
 
+extern "C" int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n)
+{
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return -rc;
+    int launches = 0;
+    for (const Range &r : d->fwd) launches += r.count > 0;
+    for (const Range &r : d->bwd) launches += r.count > 0;
+    launches += (d->mid1.count > 0) + (d->mid2.count > 0) + (d->den1.count > 0) + (d->den2.count > 0);
+    double vals[13] = {(double)launches, d->alg_bytes_matrix, d->alg_bytes_vec, d->alg_flops,
+                       (double)d->bytes_U, (double)d->bytes_B, (double)d->bytes_D,
+                       d->last_ms[0], d->last_ms[1], d->last_ms[2], d->last_ms[3], d->last_ms[4],
+                       (double)d->precision};
+    int m = std::min(n, 13);
+    for (int i = 0; i < m; i++) out[i] = vals[i];
+    return m;
+}
+
 extern "C" void h2g_gpu_print_statistic(H2ERI_p h2eri)
 {
     std::lock_guard<std::mutex> lk(g_mu);

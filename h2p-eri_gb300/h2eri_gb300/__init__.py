@@ -89,6 +89,7 @@ SIGNATURES = {
     "H2ERI_build_Coulomb_multi": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
     "H2ERI_build_Coulomb_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     "H2ERI_build_exchange_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "H2ERI_gpu_report": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     "H2ERI_save_representation": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "H2ERI_load_representation": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
 }
@@ -230,6 +231,16 @@ class H2ERI:
         torch.cuda.synchronize()
         return K.cpu().numpy()
 
+    def report(self):
+        """Device-copy figures (see H2ERI_gpu_report in include/h2eri_gb300.h)."""
+        out = np.zeros(16)
+        n = lib().H2ERI_gpu_report(self.handle, out.ctypes.data, 16)
+        if n < 0:
+            _check(-n, "gpu_report")
+        keys = ["launches_per_matvec", "alg_matrix_bytes", "alg_vector_bytes", "alg_flops", "arena_U", "arena_B",
+                "arena_D", "ms_fwd", "ms_mid", "ms_bwd", "ms_den", "ms_total", "precision"]
+        return dict(zip(keys, out[:n].tolist()))
+
     def print_statistic(self):
         lib().H2ERI_print_statistic(self.handle)
 
@@ -243,3 +254,6 @@ class H2ERI:
             self.destroy()
         except Exception:
             pass
+
+
+from . import molecules  # noqa: E402,F401

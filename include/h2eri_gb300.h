@@ -93,6 +93,14 @@ int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double *d_den, do
 /* K on device arrays, enqueued on a stream. Returns 0 on success. */
 int H2ERI_build_exchange_device(H2ERI_p h2eri, const double *d_den, double *d_K, void *stream);
 
+/* Figures of the device copy, for reports. out[0] kernel launches per matvec
+ * call (one vector block), out[1] algorithmic matrix bytes read per matvec,
+ * out[2] algorithmic vector bytes per vector, out[3] flops per vector,
+ * out[4..6] arena bytes of U, B, D, out[7..11] last timed phase durations
+ * in ms (upward, coupling, downward, near field, total), out[12] far-field
+ * precision mode. Returns the number of values written (<= n), or < 0. */
+int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n);
+
 /* Save / load the H2 representation (tree, pair lists, U, B, D and the
  * basis-function bookkeeping used by J and K) in a self-describing binary
  * file, so the same blocks can be applied on another machine or process. */
