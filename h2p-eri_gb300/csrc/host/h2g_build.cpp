@@ -382,7 +382,7 @@ void build_UJ_proxy(H2ERI_p h)
             const double *eb = h->enbox + 6 * node;
             double width = eb[3], extent = h->box_extent[node];
             double r1 = width * (0.5 + H2G_ALPHA_SUP), r2 = width * (0.5 + extent);
-            int nlayer = 1 + (int)std::ceil((extent - H2G_ALPHA_SUP) * (h->pp_nlayer_ext - 1));
+            int nlayer = std::max(1, 1 + (int)std::ceil((extent - H2G_ALPHA_SUP) * (h->pp_nlayer_ext - 1)));
             std::vector<double> pp;
             int num_pp;
             proxy_points(r1, r2, nlayer, h->pp_npts_layer, pp, num_pp);

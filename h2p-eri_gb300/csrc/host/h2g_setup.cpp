@@ -871,7 +871,9 @@ extern "C" void H2ERI_partition(H2ERI_p h)
     /* 3. box extents (src/H2ERI_partition.c:152-226) */
     int n_node = h->n_node;
     h->box_extent = (double *)std::calloc((size_t)n_node, sizeof(double));
-    for (int lv = h->max_level; lv >= 1; lv--) {
+    /* the reference stops at level 1; the root is included here so that a
+     * one-node tree (tiny molecule, root admissible level 0) has a defined extent */
+    for (int lv = h->max_level; lv >= 0; lv--) {
         for (int j = 0; j < h->level_n_node[lv]; j++) {
             int node = h->level_nodes[lv * h->n_leaf_node + j];
             const double *eb = h->enbox + 6 * node;
