@@ -36,9 +36,17 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "h2p-eri_gb300"))
 sys.path.insert(0, REPO)
 
-WORKLOAD = {"workload": "J build C30H62 cc-pVDZ (760 bf, cartesian), QR tol 1e-8, 1 density n_occ=121",
+WORKLOADS = {
+    # the headline configuration (fits one GPU)
+    "c30": {"workload": "J build C30H62 cc-pVDZ (760 bf, cartesian), QR tol 1e-8, 1 density n_occ=121",
             "molecule": "C30H62", "n_carbon": 30, "qr_tol": 1e-8, "n_occ": 121, "seed": 2000,
-            "inputs_vs_L2": "H2 representation ~1.8 GB read per step > 129 MB L2 (no flush needed)"}
+            "inputs_vs_L2": "H2 representation ~1.8 GB read per step > 129 MB L2 (no flush needed)"},
+    # small case for profiler captures (the reference's CPU-runnable size)
+    "c10": {"workload": "J build C10H22 cc-pVDZ (260 bf, cartesian), QR tol 1e-6, 1 density n_occ=41",
+            "molecule": "C10H22", "n_carbon": 10, "qr_tol": 1e-6, "n_occ": 41, "seed": 1000,
+            "inputs_vs_L2": "H2 representation ~0.28 GB read per step > 129 MB L2"},
+}
+WORKLOAD = dict(WORKLOADS["c30"])
 METRIC = "J builds/s C30H62 (mixed vs FP64) at relerr<=1e-8"
 CACHE_DIR = os.path.join(tempfile.gettempdir(), "h2eri_gb300_cache")
 
@@ -141,7 +149,7 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(orc, h, D, budget_s=12.0, max_builds=40):
+def cpu_baseline(orc, h, D, budget_s=12.0, max_builds=100000):
     """Oracle restatement of H2ERI_build_Coulomb on the host cores."""
     J = np.zeros_like(D)
     orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)   # warm-up
@@ -214,10 +222,14 @@ def run_gpu(args):
     L = hg.lib()
     nbf = h.num_bf
     D = molecules.seeded_density(nbf, WORKLOAD["n_occ"], WORKLOAD["seed"])
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library enqueues on it and the events below are
+    # recorded on it (the legacy default stream would not order with the
+    # library's non-blocking streams)
+    stream = torch.cuda.Stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     dD = torch.tensor(D, device="cuda")
     dJ = torch.empty_like(dD)
+    torch.cuda.synchronize()
     t_up = time.perf_counter()
     h.upload()
     upload_s = time.perf_counter() - t_up
@@ -284,7 +296,12 @@ def run_gpu(args):
         return
 
     orc = load_oracle()
-    cpu_v, cpu_n, cpu_dt, J_ref = cpu_baseline(orc, h, D)
+    if args.skip_cpu:
+        J_ref = np.zeros_like(D)
+        orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J_ref.ctypes.data)
+        cpu_v, cpu_n, cpu_dt = None, 0, 0.0
+    else:
+        cpu_v, cpu_n, cpu_dt, J_ref = cpu_baseline(orc, h, D)
     def rel(J):
         return float(np.linalg.norm(J - J_ref) / np.linalg.norm(J_ref))
 
@@ -315,6 +332,7 @@ def run_gpu(args):
                          "sample": f"{cpu_n} J builds of the workload in {cpu_dt:.1f} s (oracle, OpenMP)"},
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
         "gpu_launches": launches_per_J * args.steps,
+        "phase_ms_last_host_call": {k: h.report()[k] for k in ("ms_fwd", "ms_mid", "ms_bwd", "ms_den", "ms_total")},
         "setup_s": setup_s, "upload_s": upload_s,
     }
     print(json.dumps(out), flush=True)
@@ -331,7 +349,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--workload", default="c30", choices=sorted(WORKLOADS))
+    ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg (profiler runs)")
     args = ap.parse_args()
+    WORKLOAD.clear()
+    WORKLOAD.update(WORKLOADS[args.workload])
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
