@@ -34,14 +34,30 @@ enum VecKind : uint8_t {
  * Offsets are element offsets (already shifted by r0 / c0) into the vector
  * space named by the kind byte. */
 struct Tile {
-    uint64_t a;            /* element offset of A[r0][c0] in the arena */
-    int32_t ld;
+    uint64_t a;            /* element offset of A[r0][c0] in the FP64 arena        */
+    uint64_t a2;           /* element offset in the mixed arena of the same matrix */
+    int32_t ld, ld2;       /* leading dimensions in the two arenas                 */
     int16_t nr, nc;
     int32_t in0, out0, in1, out1;
     uint8_t k_in0, k_out0, k_in1, k_out1;
-    int32_t pad;
 };
-static_assert(sizeof(Tile) == 40, "tile descriptor layout");
+static_assert(sizeof(Tile) == 48, "tile descriptor layout");
+
+/* Storage formats of the stored matrices. */
+enum MatFmt : int {
+    FMT_F64 = 0,    /* double                                               */
+    FMT_F32 = 1,    /* float (coupling and near-field blocks, mixed mode)   */
+    FMT_F32X2 = 2   /* float pair hi + lo, value = hi + lo (bases, mixed)   */
+};
+
+/* One matrix to copy into the mixed arenas when mixed mode is first used. */
+struct PackItem {
+    const double *src;
+    int nrow, ncol, lds;
+    int fmt;              /* FMT_F32 or FMT_F32X2 */
+    size_t off;           /* element offset in the float (F32) or float2 (F32X2) arena */
+    int ld;
+};
 
 constexpr int kTileRows = 64;
 constexpr int kTileCols = 128;
@@ -65,6 +81,11 @@ struct DevRep {
     /* blocks */
     double *arena = nullptr;
     size_t arena_elems = 0;
+    float *arena32 = nullptr;         /* B and D blocks, mixed mode */
+    float2 *arena32x2 = nullptr;      /* U bases as hi/lo pairs, mixed mode */
+    size_t arena32_elems = 0, arena32x2_elems = 0;
+    std::vector<PackItem> mixed_items;
+    double alg_bytes_matrix_mixed = 0.0;
     size_t bytes_U = 0, bytes_B = 0, bytes_D = 0;
     /* plan */
     Tile *tiles = nullptr;

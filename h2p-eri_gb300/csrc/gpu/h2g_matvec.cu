@@ -1,5 +1,5 @@
 /*
- * GPU H2 apply: device representation, launch plan and the FP64 kernels of
+ * GPU H2 apply: device representation, launch plan and the kernels of
  * the hot path (H2P-ERI src/H2ERI_matvec.c:882-957 and
  * src/H2ERI_build_Coulomb.c:26-152).
  *
@@ -58,44 +58,127 @@ __device__ __forceinline__ double *vec_ptr(const VecArgs &va, uint8_t kind, int 
     return va.base[kind] + (long long)v * va.stride[kind] + off;
 }
 
+/* Compensated FP32 arithmetic (mixed mode). A product a * x with a = a_hi +
+ * a_lo and x = x_hi + x_lo is accumulated into a float pair (sh, sl):
+ * p = fl(a_hi x_hi) with its exact rounding error e from an FMA, the small
+ * cross terms folded into e, and p added to sh with an error-free two-sum
+ * whose error goes to sl. Explicit _rn intrinsics keep the compiler from
+ * contracting the two-sum into FMAs. Only the stored-matrix rounding remains
+ * (2^-24 relative for single floats, ~2^-48 for float pairs). */
+__device__ __forceinline__ void cacc(float &sh, float &sl, float ah, float al, float xh, float xl)
+{
+    const float p = __fmul_rn(ah, xh);
+    const float e = fmaf(ah, xh, -p);
+    const float c = fmaf(ah, xl, fmaf(al, xh, e));
+    const float s = __fadd_rn(sh, p);
+    const float bp = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(err, c));
+}
+
+/* cacc for a single-float matrix entry (a_lo = 0) */
+__device__ __forceinline__ void cacc1(float &sh, float &sl, float ah, float xh, float xl)
+{
+    const float p = __fmul_rn(ah, xh);
+    const float c = fmaf(ah, xl, fmaf(ah, xh, -p));
+    const float s = __fadd_rn(sh, p);
+    const float bp = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(err, c));
+}
+
+__device__ __forceinline__ void split(double x, float &hi, float &lo)
+{
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+}
+
+/* Column owned by lane `lane` in slot k (0..3) of a 128-column tile strip. */
+template <int FMT>
+__device__ __forceinline__ int lane_col(int lane, int k)
+{
+    if (FMT == FMT_F32) return 4 * lane + k;
+    return (k < 2) ? 2 * lane + k : 64 + 2 * lane + (k - 2);
+}
+
 /* One CTA per (tile, vector). 8 warps; warp w owns rows 8w..8w+7 of the
- * tile; lane l owns columns {2l, 2l+1, 64+2l, 65+2l}. All eight rows are
- * loaded before any arithmetic so each warp keeps 8 KB of loads in flight. */
-__global__ void __launch_bounds__(kTileThreads)
-k_tile_f64(const Tile *__restrict__ tiles, const double *__restrict__ arena, VecArgs va)
+ * tile; each lane owns 4 columns (lane_col). All eight rows are loaded before
+ * any arithmetic so each warp keeps its row loads in flight together.
+ * FMT_F64: plain FP64 FMAs. FMT_F32 / FMT_F32X2: compensated FP32 products
+ * (cacc) with per-lane float-pair partial sums; cross-lane and cross-warp
+ * reductions and the output atomics are FP64. */
+template <int FMT>
+__global__ void __launch_bounds__(kTileThreads, 2)
+k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va)
 {
     const Tile t = tiles[blockIdx.x];
     const int v = blockIdx.y;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
     const int nr = t.nr, nc = t.nc;
-    const double *__restrict__ A = arena + t.a;
-    const int cA = 2 * lane, cB = 64 + 2 * lane;
-    const bool okA = cA < nc, okB = cB < nc;
+    bool ok[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) ok[k] = lane_col<FMT>(lane, k) < nc;
 
+    /* N-side input, split into float pairs for the mixed formats */
     double xv[4] = {0.0, 0.0, 0.0, 0.0};
     if (opN) {
         const double *in0 = vec_ptr(va, t.k_in0, t.in0, v);
-        if (okA) { xv[0] = in0[cA]; if (cA + 1 < nc) xv[1] = in0[cA + 1]; }
-        if (okB) { xv[2] = in0[cB]; if (cB + 1 < nc) xv[3] = in0[cB + 1]; }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (ok[k]) xv[k] = in0[lane_col<FMT>(lane, k)];
     }
+    float xh[4], xl[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) split(xv[k], xh[k], xl[k]);
+
+    /* load 8 rows x 4 columns of the tile */
     double a[8][4];
+    float ahi[8][4], alo[8][4];
     const int r0 = warp * 8;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const int r = r0 + i;
-        double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
-        if (r < nr) {
-            const double *row = A + (size_t)r * t.ld;
-            if (okA) pa = __ldg(reinterpret_cast<const double2 *>(row + cA));
-            if (okB) pb = __ldg(reinterpret_cast<const double2 *>(row + cB));
+        const bool live = r < nr;
+        if (FMT == FMT_F64) {
+            const double *row = reinterpret_cast<const double *>(arena_v) + t.a + (size_t)r * t.ld;
+            double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
+            if (live && ok[0]) pa = __ldg(reinterpret_cast<const double2 *>(row + 2 * lane));
+            if (live && ok[2]) pb = __ldg(reinterpret_cast<const double2 *>(row + 64 + 2 * lane));
+            a[i][0] = pa.x; a[i][1] = pa.y; a[i][2] = pb.x; a[i][3] = pb.y;
+        } else if (FMT == FMT_F32) {
+            const float *row = reinterpret_cast<const float *>(arena_v) + t.a2 + (size_t)r * t.ld2;
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (live && ok[0]) q = __ldg(reinterpret_cast<const float4 *>(row + 4 * lane));
+            ahi[i][0] = q.x; ahi[i][1] = q.y; ahi[i][2] = q.z; ahi[i][3] = q.w;
+        } else {
+            const float2 *row = reinterpret_cast<const float2 *>(arena_v) + t.a2 + (size_t)r * t.ld2;
+            float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (live && ok[0]) qa = __ldg(reinterpret_cast<const float4 *>(row + 2 * lane));
+            if (live && ok[2]) qb = __ldg(reinterpret_cast<const float4 *>(row + 64 + 2 * lane));
+            ahi[i][0] = qa.x; alo[i][0] = qa.y; ahi[i][1] = qa.z; alo[i][1] = qa.w;
+            ahi[i][2] = qb.x; alo[i][2] = qb.y; ahi[i][3] = qb.z; alo[i][3] = qb.w;
         }
-        a[i][0] = pa.x; a[i][1] = pa.y; a[i][2] = pb.x; a[i][3] = pb.y;
     }
+
     if (opN) {
         double s[8];
 #pragma unroll
-        for (int i = 0; i < 8; i++) s[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
+        for (int i = 0; i < 8; i++) {
+            if (FMT == FMT_F64) {
+                s[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
+            } else {
+                float sh = 0.f, sl = 0.f;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (FMT == FMT_F32) cacc1(sh, sl, ahi[i][k], xh[k], xl[k]);
+                    else cacc(sh, sl, ahi[i][k], alo[i][k], xh[k], xl[k]);
+                }
+                s[i] = (double)sh + (double)sl;
+            }
+        }
         /* reduce 8 row sums across the warp by recursive halving */
         const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
 #pragma unroll
@@ -121,22 +204,37 @@ k_tile_f64(const Tile *__restrict__ tiles, const double *__restrict__ arena, Vec
         __shared__ double red[8][kTileCols];
         const double *in1 = vec_ptr(va, t.k_in1, t.in1, v);
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        if (FMT == FMT_F64) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const int r = r0 + i;
-            const double x1 = (r < nr) ? in1[r] : 0.0;
+            for (int i = 0; i < 8; i++) {
+                const double x1 = (r0 + i < nr) ? in1[r0 + i] : 0.0;
 #pragma unroll
-            for (int k = 0; k < 4; k++) acc[k] += a[i][k] * x1;
+                for (int k = 0; k < 4; k++) acc[k] += a[i][k] * x1;
+            }
+        } else {
+            float sh[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                float x1h, x1l;
+                split((r0 + i < nr) ? in1[r0 + i] : 0.0, x1h, x1l);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (FMT == FMT_F32) cacc1(sh[k], sl[k], ahi[i][k], x1h, x1l);
+                    else cacc(sh[k], sl[k], ahi[i][k], alo[i][k], x1h, x1l);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[k] = (double)sh[k] + (double)sl[k];
         }
-        red[warp][cA] = acc[0]; red[warp][cA + 1] = acc[1];
-        red[warp][cB] = acc[2]; red[warp][cB + 1] = acc[3];
+#pragma unroll
+        for (int k = 0; k < 4; k++) red[warp][lane_col<FMT>(lane, k)] = acc[k];
         __syncthreads();
         double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
         for (int c = threadIdx.x; c < nc; c += kTileThreads) {
-            double s = 0.0;
+            double sum = 0.0;
 #pragma unroll
-            for (int w = 0; w < 8; w++) s += red[w][c];
-            atomicAdd(out1 + c, s);
+            for (int w = 0; w < 8; w++) sum += red[w][c];
+            atomicAdd(out1 + c, sum);
         }
     }
 }
@@ -180,37 +278,56 @@ static std::unordered_map<const void *, DevRep *> g_reps;
 
 namespace {
 
+/* Location of one stored matrix in the FP64 arena and in the mixed arena of
+ * its mixed-mode format. */
+struct MatLoc {
+    size_t a = 0, a2 = 0;
+    int ld = 0, ld2 = 0;
+};
+
+/* Packs matrices into the FP64 arena now and records where each goes in the
+ * mixed arenas (filled on first use of mixed mode). Leading dimensions are
+ * padded to 16-byte multiples and every matrix starts 32-byte aligned, so
+ * rows can be read with 16-byte vector loads; padding is zero. */
 struct Packer {
     std::vector<double> host;
-    size_t alloc(size_t elems)
+    size_t n32 = 0, n32x2 = 0;
+    std::vector<PackItem> items;
+    MatLoc put(const double *src, int nrow, int ncol, int lds, int mixed_fmt)
     {
-        size_t off = (host.size() + 3) & ~size_t(3);      /* 32-byte aligned blocks */
-        host.resize(off + elems, 0.0);
-        return off;
-    }
-    /* copy a row-major nrow x ncol matrix (source leading dimension lds) into a
-     * fresh region with an even leading dimension; returns offset and ld */
-    size_t put(const double *src, int nrow, int ncol, int lds, int &ld)
-    {
-        ld = (ncol + 1) & ~1;
-        size_t off = alloc((size_t)nrow * ld);
+        MatLoc m;
+        m.ld = (ncol + 1) & ~1;
+        m.a = (host.size() + 3) & ~size_t(3);
+        host.resize(m.a + (size_t)nrow * m.ld, 0.0);
         for (int r = 0; r < nrow; r++)
-            std::memcpy(host.data() + off + (size_t)r * ld, src + (size_t)r * lds, sizeof(double) * ncol);
-        return off;
+            std::memcpy(host.data() + m.a + (size_t)r * m.ld, src + (size_t)r * lds, sizeof(double) * ncol);
+        if (mixed_fmt == FMT_F32) {
+            m.ld2 = (ncol + 3) & ~3;
+            m.a2 = (n32 + 7) & ~size_t(7);
+            n32 = m.a2 + (size_t)nrow * m.ld2;
+        } else {
+            m.ld2 = (ncol + 1) & ~1;
+            m.a2 = (n32x2 + 3) & ~size_t(3);
+            n32x2 = m.a2 + (size_t)nrow * m.ld2;
+        }
+        items.push_back(PackItem{src, nrow, ncol, lds, mixed_fmt, m.a2, m.ld2});
+        return m;
     }
 };
 
 struct Planner {
     std::vector<Tile> tiles;
-    void add(size_t a, int ld, int nrow, int ncol, uint8_t kin0, int in0, uint8_t kout0, int out0,
+    void add(const MatLoc &m, int nrow, int ncol, uint8_t kin0, int in0, uint8_t kout0, int out0,
              uint8_t kin1, int in1, uint8_t kout1, int out1)
     {
         for (int r0 = 0; r0 < nrow; r0 += kTileRows)
             for (int c0 = 0; c0 < ncol; c0 += kTileCols) {
                 Tile t;
                 std::memset(&t, 0, sizeof(t));
-                t.a = a + (size_t)r0 * ld + c0;
-                t.ld = ld;
+                t.a = m.a + (size_t)r0 * m.ld + c0;
+                t.a2 = m.a2 + (size_t)r0 * m.ld2 + c0;
+                t.ld = m.ld;
+                t.ld2 = m.ld2;
                 t.nr = (int16_t)std::min(kTileRows, nrow - r0);
                 t.nc = (int16_t)std::min(kTileCols, ncol - c0);
                 if (kout0 != VK_NONE) { t.k_in0 = kin0; t.in0 = in0 + c0; t.k_out0 = kout0; t.out0 = out0 + r0; }
@@ -220,12 +337,11 @@ struct Planner {
     }
 };
 
-/* A stored B/D block in the arena, dense or low-rank. */
+/* A stored B/D block, dense or low-rank. */
 struct BlockLoc {
     bool lowrank = false;
     int nrow = 0, ncol = 0, rank = 0;
-    size_t a = 0, u = 0, vt = 0;   /* dense data, or U and V^T factors */
-    int ld = 0, ldu = 0, ldv = 0;
+    MatLoc a, u, vt;               /* dense data, or U and V^T factors */
     int t_off = 0, s_off = 0;      /* scratch for V x_in0 and U^T x_in1 */
 };
 
@@ -237,13 +353,13 @@ BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total)
     if (m->ld < 0) {
         b.lowrank = true;
         b.rank = -m->ld;
-        b.u = pk.put(m->data, b.nrow, b.rank, b.rank, b.ldu);
-        b.vt = pk.put(m->data + (size_t)b.nrow * b.rank, b.ncol, b.rank, b.rank, b.ldv);
+        b.u = pk.put(m->data, b.nrow, b.rank, b.rank, FMT_F32);
+        b.vt = pk.put(m->data + (size_t)b.nrow * b.rank, b.ncol, b.rank, b.rank, FMT_F32);
         b.t_off = lr_total;
         b.s_off = lr_total + b.rank;
         lr_total += 2 * b.rank;
     } else if ((size_t)b.nrow * b.ncol > 0) {
-        b.a = pk.put(m->data, b.nrow, b.ncol, m->ld, b.ld);
+        b.a = pk.put(m->data, b.nrow, b.ncol, m->ld, FMT_F32);
     }
     return b;
 }
@@ -255,19 +371,19 @@ void plan_block(Planner &stage1, Planner &stage2, const BlockLoc &b, uint8_t kin
 {
     if (b.nrow == 0 || b.ncol == 0) return;
     if (!b.lowrank) {
-        stage1.add(b.a, b.ld, b.nrow, b.ncol, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
+        stage1.add(b.a, b.nrow, b.ncol, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
         return;
     }
     if (b.rank == 0) return;
     if (kout0 != VK_NONE) {
         /* t = V in0 = (V^T)^T in0 ; out0 += U t */
-        stage1.add(b.vt, b.ldv, b.ncol, b.rank, VK_NONE, 0, VK_NONE, 0, kin0, in0, VK_T, b.t_off);
-        stage2.add(b.u, b.ldu, b.nrow, b.rank, VK_T, b.t_off, kout0, out0, VK_NONE, 0, VK_NONE, 0);
+        stage1.add(b.vt, b.ncol, b.rank, VK_NONE, 0, VK_NONE, 0, kin0, in0, VK_T, b.t_off);
+        stage2.add(b.u, b.nrow, b.rank, VK_T, b.t_off, kout0, out0, VK_NONE, 0, VK_NONE, 0);
     }
     if (kout1 != VK_NONE) {
         /* s = U^T in1 ; out1 += V^T s */
-        stage1.add(b.u, b.ldu, b.nrow, b.rank, VK_NONE, 0, VK_NONE, 0, kin1, in1, VK_T, b.s_off);
-        stage2.add(b.vt, b.ldv, b.ncol, b.rank, VK_T, b.s_off, kout1, out1, VK_NONE, 0, VK_NONE, 0);
+        stage1.add(b.u, b.nrow, b.rank, VK_NONE, 0, VK_NONE, 0, kin1, in1, VK_T, b.s_off);
+        stage2.add(b.vt, b.ncol, b.rank, VK_T, b.s_off, kout1, out1, VK_NONE, 0, VK_NONE, 0);
     }
 }
 
@@ -285,6 +401,8 @@ static void free_rep(DevRep *d)
     cudaGetDevice(&cur);
     if (d->device >= 0) cudaSetDevice(d->device);
     cudaFree(d->arena);
+    cudaFree(d->arena32);
+    cudaFree(d->arena32x2);
     cudaFree(d->tiles);
     cudaFree(d->unc_map);
     cudaFree(d->con_map);
@@ -351,16 +469,15 @@ static int build_rep(H2ERI_p h, DevRep *d)
 
     Planner fwd_lv, bwd_lv, mid1, mid2, den1, den2;
     std::vector<Tile> all;
-    double mat_bytes = 0.0, vec_bytes = 0.0, flops = 0.0;
+    double mat_bytes = 0.0, mat_bytes_mixed = 0.0, vec_bytes = 0.0, flops = 0.0;
     d->fwd.clear();
     d->bwd.clear();
 
     /* U bases */
-    std::vector<size_t> uoff(n_node, 0);
-    std::vector<int> uld(n_node, 0);
+    std::vector<MatLoc> uloc(n_node);
     for (int i = 0; i < n_node; i++) {
         H2E_dense_mat_p U = h->U[i];
-        if (U->nrow > 0 && U->ncol > 0) uoff[i] = pk.put(U->data, U->nrow, U->ncol, U->ld, uld[i]);
+        if (U->nrow > 0 && U->ncol > 0) uloc[i] = pk.put(U->data, U->nrow, U->ncol, U->ld, FMT_F32X2);
     }
     d->bytes_U = pk.host.size() * sizeof(double);
 
@@ -373,9 +490,10 @@ static int build_rep(H2ERI_p h, DevRep *d)
             if (!need_up[node] || U->nrow == 0 || U->ncol == 0) continue;
             bool leaf = h->n_child[node] == 0;
             int in_off = leaf ? h->mat_cluster[2 * node] : voff[h->children[node * h->max_child]];
-            p.add(uoff[node], uld[node], U->nrow, U->ncol, VK_NONE, 0, VK_NONE, 0, leaf ? VK_X : VK_Y0, in_off,
+            p.add(uloc[node], U->nrow, U->ncol, VK_NONE, 0, VK_NONE, 0, leaf ? VK_X : VK_Y0, in_off,
                   VK_Y0, voff[node]);
             mat_bytes += 8.0 * U->nrow * U->ncol;
+            mat_bytes_mixed += 8.0 * U->nrow * U->ncol;
             vec_bytes += 8.0 * (U->nrow + U->ncol);
             flops += 2.0 * U->nrow * U->ncol;
         }
@@ -404,6 +522,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
         }
         plan_block(mid1, mid2, b, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
         mat_bytes += 8.0 * block_elems(b);
+        mat_bytes_mixed += 4.0 * block_elems(b);
         vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
         flops += 4.0 * block_elems(b);
     }
@@ -422,9 +541,10 @@ static int build_rep(H2ERI_p h, DevRep *d)
             if (!need_down[node] || U->nrow == 0 || U->ncol == 0) continue;
             bool leaf = h->n_child[node] == 0;
             int out_off = leaf ? h->mat_cluster[2 * node] : voff[h->children[node * h->max_child]];
-            p.add(uoff[node], uld[node], U->nrow, U->ncol, VK_Y1, voff[node], leaf ? VK_Y : VK_Y1, out_off, VK_NONE,
+            p.add(uloc[node], U->nrow, U->ncol, VK_Y1, voff[node], leaf ? VK_Y : VK_Y1, out_off, VK_NONE,
                   0, VK_NONE, 0);
             mat_bytes += 8.0 * U->nrow * U->ncol;
+            mat_bytes_mixed += 8.0 * U->nrow * U->ncol;
             vec_bytes += 8.0 * (U->nrow + U->ncol);
             flops += 2.0 * U->nrow * U->ncol;
         }
@@ -452,6 +572,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
             flops += 4.0 * block_elems(b);
         }
         mat_bytes += 8.0 * block_elems(b);
+        mat_bytes_mixed += 4.0 * block_elems(b);
     }
     d->bytes_D = (pk.host.size() - d_start) * sizeof(double);
     d->den1 = {(int)all.size(), (int)den1.tiles.size()};
@@ -460,6 +581,10 @@ static int build_rep(H2ERI_p h, DevRep *d)
     all.insert(all.end(), den2.tiles.begin(), den2.tiles.end());
 
     d->alg_bytes_matrix = mat_bytes;
+    d->alg_bytes_matrix_mixed = mat_bytes_mixed;
+    d->mixed_items = std::move(pk.items);
+    d->arena32_elems = pk.n32;
+    d->arena32x2_elems = pk.n32x2;
     d->alg_bytes_vec = vec_bytes;
     d->alg_flops = flops;
     d->n_tiles = (int)all.size();
@@ -553,11 +678,56 @@ static int ensure_work(DevRep *d, int nvec)
     return 0;
 }
 
-static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s)
+/* basis: the range holds U tiles (mixed mode stores U as float pairs) */
+static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s, bool basis)
 {
     if (r.count == 0) return;
     dim3 grid(r.count, nvec);
-    k_tile_f64<<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena, va);
+    if (d->precision == H2ERI_GPU_FP64)
+        k_tile<FMT_F64><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena, va);
+    else if (basis)
+        k_tile<FMT_F32X2><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena32x2, va);
+    else
+        k_tile<FMT_F32><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena32, va);
+}
+
+/* Fill the mixed arenas from the host blocks (first use of mixed mode). */
+static int pack_mixed(DevRep *d)
+{
+    if (d->arena32 != nullptr || d->arena32x2 != nullptr) return 0;
+    std::vector<float> h32(std::max<size_t>(d->arena32_elems, 4), 0.f);
+    std::vector<float2> h32x2(std::max<size_t>(d->arena32x2_elems, 2), make_float2(0.f, 0.f));
+    for (const PackItem &it : d->mixed_items) {
+        for (int r = 0; r < it.nrow; r++) {
+            const double *src = it.src + (size_t)r * it.lds;
+            if (it.fmt == FMT_F32) {
+                float *dst = h32.data() + it.off + (size_t)r * it.ld;
+                for (int c = 0; c < it.ncol; c++) dst[c] = (float)src[c];
+            } else {
+                float2 *dst = h32x2.data() + it.off + (size_t)r * it.ld;
+                for (int c = 0; c < it.ncol; c++) {
+                    float hi = (float)src[c];
+                    dst[c] = make_float2(hi, (float)(src[c] - (double)hi));
+                }
+            }
+        }
+    }
+    CUDA_TRY(cudaMalloc(&d->arena32, h32.size() * sizeof(float)));
+    CUDA_TRY(cudaMemcpy(d->arena32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMalloc(&d->arena32x2, h32x2.size() * sizeof(float2)));
+    CUDA_TRY(cudaMemcpy(d->arena32x2, h32x2.data(), h32x2.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int set_precision_mode(DevRep *d, H2ERI_p h, int mode)
+{
+    (void)h;
+    if (mode == H2ERI_GPU_MIXED) {
+        int rc = pack_mixed(d);
+        if (rc) return rc;
+    }
+    d->precision = mode;
+    return 0;
 }
 
 /* Enqueue y = A x for nvec vectors (device pointers) on stream s. If timed,
@@ -585,16 +755,16 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     CUDA_TRY(cudaEventRecord(d->ev_fork, s));
     CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_fork, 0));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], d->s_aux));
-    launch_range(d, d->den1, va, nvec, d->s_aux);
-    launch_range(d, d->den2, va, nvec, d->s_aux);
+    launch_range(d, d->den1, va, nvec, d->s_aux, false);
+    launch_range(d, d->den2, va, nvec, d->s_aux, false);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[7], d->s_aux));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], s));
-    for (const Range &r : d->fwd) launch_range(d, r, va, nvec, s);
+    for (const Range &r : d->fwd) launch_range(d, r, va, nvec, s, true);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[1], s));
-    launch_range(d, d->mid1, va, nvec, s);
-    launch_range(d, d->mid2, va, nvec, s);
+    launch_range(d, d->mid1, va, nvec, s, false);
+    launch_range(d, d->mid2, va, nvec, s, false);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[2], s));
-    for (const Range &r : d->bwd) launch_range(d, r, va, nvec, s);
+    for (const Range &r : d->bwd) launch_range(d, r, va, nvec, s, true);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[3], s));
     CUDA_TRY(cudaEventRecord(d->ev_join, d->s_aux));
     CUDA_TRY(cudaStreamWaitEvent(s, d->ev_join, 0));
@@ -770,7 +940,8 @@ extern "C" int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n)
     for (const Range &r : d->fwd) launches += r.count > 0;
     for (const Range &r : d->bwd) launches += r.count > 0;
     launches += (d->mid1.count > 0) + (d->mid2.count > 0) + (d->den1.count > 0) + (d->den2.count > 0);
-    double vals[13] = {(double)launches, d->alg_bytes_matrix, d->alg_bytes_vec, d->alg_flops,
+    double mbytes = d->precision == H2ERI_GPU_MIXED ? d->alg_bytes_matrix_mixed : d->alg_bytes_matrix;
+    double vals[13] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
                        (double)d->bytes_U, (double)d->bytes_B, (double)d->bytes_D,
                        d->last_ms[0], d->last_ms[1], d->last_ms[2], d->last_ms[3], d->last_ms[4],
                        (double)d->precision};
