@@ -70,6 +70,7 @@ struct VecArgs {
 
 struct Range {
     int first = 0, count = 0;
+    bool pair = false;     /* mixed mode: matrices of this range are float pairs */
 };
 
 /* Device copy of one H2 representation plus the launch plan. */
@@ -92,7 +93,8 @@ struct DevRep {
     int n_tiles = 0;
     std::vector<Range> fwd;     /* deepest level first */
     std::vector<Range> bwd;     /* shallowest level first */
-    Range mid1, mid2, den1, den2;
+    Range mid1, mid2;
+    std::vector<Range> den;     /* near field: stage-1 ranges, then stage-2 ranges */
     int rank_total = 0, lr_total = 0;
     /* algorithmic bytes / flops of one matvec (per vector), for reports */
     double alg_bytes_matrix = 0.0, alg_bytes_vec = 0.0, alg_flops = 0.0;

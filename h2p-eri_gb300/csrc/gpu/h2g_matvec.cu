@@ -345,7 +345,7 @@ struct BlockLoc {
     int t_off = 0, s_off = 0;      /* scratch for V x_in0 and U^T x_in1 */
 };
 
-BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total)
+BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total, int fmt)
 {
     BlockLoc b;
     b.nrow = m->nrow;
@@ -353,13 +353,13 @@ BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total)
     if (m->ld < 0) {
         b.lowrank = true;
         b.rank = -m->ld;
-        b.u = pk.put(m->data, b.nrow, b.rank, b.rank, FMT_F32);
-        b.vt = pk.put(m->data + (size_t)b.nrow * b.rank, b.ncol, b.rank, b.rank, FMT_F32);
+        b.u = pk.put(m->data, b.nrow, b.rank, b.rank, fmt);
+        b.vt = pk.put(m->data + (size_t)b.nrow * b.rank, b.ncol, b.rank, b.rank, fmt);
         b.t_off = lr_total;
         b.s_off = lr_total + b.rank;
         lr_total += 2 * b.rank;
     } else if ((size_t)b.nrow * b.ncol > 0) {
-        b.a = pk.put(m->data, b.nrow, b.ncol, m->ld, FMT_F32);
+        b.a = pk.put(m->data, b.nrow, b.ncol, m->ld, fmt);
     }
     return b;
 }
@@ -467,7 +467,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
             need_down[node] = wrote_y1[node] || (pin && need_down[p] && rank[p] > 0);
         }
 
-    Planner fwd_lv, bwd_lv, mid1, mid2, den1, den2;
+    Planner mid1, mid2, den1d, den2d, den1o, den2o;
     std::vector<Tile> all;
     double mat_bytes = 0.0, mat_bytes_mixed = 0.0, vec_bytes = 0.0, flops = 0.0;
     d->fwd.clear();
@@ -497,7 +497,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
             vec_bytes += 8.0 * (U->nrow + U->ncol);
             flops += 2.0 * U->nrow * U->ncol;
         }
-        Range r{(int)all.size(), (int)p.tiles.size()};
+        Range r{(int)all.size(), (int)p.tiles.size(), true};
         all.insert(all.end(), p.tiles.begin(), p.tiles.end());
         d->fwd.push_back(r);
     }
@@ -507,7 +507,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
     for (int i = 0; i < h->n_r_adm_pair; i++) {
         int n0 = h->r_adm_pairs[2 * i], n1 = h->r_adm_pairs[2 * i + 1];
         int l0 = h->node_level[n0], l1 = h->node_level[n1];
-        BlockLoc b = pack_block(pk, h->c_B_blks[i], d->lr_total);
+        BlockLoc b = pack_block(pk, h->c_B_blks[i], d->lr_total, FMT_F32);
         uint8_t kin0, kout0, kin1, kout1;
         int in0, out0, in1, out1;
         if (l0 == l1) {
@@ -548,7 +548,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
             vec_bytes += 8.0 * (U->nrow + U->ncol);
             flops += 2.0 * U->nrow * U->ncol;
         }
-        Range r{(int)all.size(), (int)p.tiles.size()};
+        Range r{(int)all.size(), (int)p.tiles.size(), true};
         all.insert(all.end(), p.tiles.begin(), p.tiles.end());
         d->bwd.push_back(r);
     }
@@ -556,29 +556,33 @@ static int build_rep(H2ERI_p h, DevRep *d)
     /* near field (src/H2ERI_matvec.c:572-660) */
     size_t d_start = pk.host.size();
     for (int i = 0; i < h->n_D; i++) {
-        BlockLoc b = pack_block(pk, h->c_D_blks[i], d->lr_total);
-        if (i < h->n_leaf_node) {
+        /* mixed mode keeps the leaf self-interaction blocks as float pairs */
+        const bool diag = i < h->n_leaf_node;
+        BlockLoc b = pack_block(pk, h->c_D_blks[i], d->lr_total, diag ? FMT_F32X2 : FMT_F32);
+        if (diag) {
             int node = h->height_nodes[i];
             int off = h->mat_cluster[2 * node];
-            plan_block(den1, den2, b, VK_X, off, VK_Y, off, VK_NONE, 0, VK_NONE, 0);
+            plan_block(den1d, den2d, b, VK_X, off, VK_Y, off, VK_NONE, 0, VK_NONE, 0);
             vec_bytes += 8.0 * (b.nrow + b.ncol);
             flops += 2.0 * block_elems(b);
         } else {
             int k = i - h->n_leaf_node;
             int n0 = h->r_inadm_pairs[2 * k], n1 = h->r_inadm_pairs[2 * k + 1];
             int o0 = h->mat_cluster[2 * n0], o1 = h->mat_cluster[2 * n1];
-            plan_block(den1, den2, b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
+            plan_block(den1o, den2o, b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
             vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
             flops += 4.0 * block_elems(b);
         }
         mat_bytes += 8.0 * block_elems(b);
-        mat_bytes_mixed += 4.0 * block_elems(b);
+        mat_bytes_mixed += (diag ? 8.0 : 4.0) * block_elems(b);
     }
     d->bytes_D = (pk.host.size() - d_start) * sizeof(double);
-    d->den1 = {(int)all.size(), (int)den1.tiles.size()};
-    all.insert(all.end(), den1.tiles.begin(), den1.tiles.end());
-    d->den2 = {(int)all.size(), (int)den2.tiles.size()};
-    all.insert(all.end(), den2.tiles.begin(), den2.tiles.end());
+    d->den.clear();
+    for (Planner *p : {&den1d, &den1o, &den2d, &den2o}) {
+        bool pair = (p == &den1d || p == &den2d);
+        d->den.push_back(Range{(int)all.size(), (int)p->tiles.size(), pair});
+        all.insert(all.end(), p->tiles.begin(), p->tiles.end());
+    }
 
     d->alg_bytes_matrix = mat_bytes;
     d->alg_bytes_matrix_mixed = mat_bytes_mixed;
@@ -678,14 +682,15 @@ static int ensure_work(DevRep *d, int nvec)
     return 0;
 }
 
-/* basis: the range holds U tiles (mixed mode stores U as float pairs) */
-static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s, bool basis)
+/* Mixed mode picks the float-pair kernel for ranges marked pair (U bases,
+ * near-field diagonal blocks) and the single-float kernel otherwise. */
+static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s)
 {
     if (r.count == 0) return;
     dim3 grid(r.count, nvec);
     if (d->precision == H2ERI_GPU_FP64)
         k_tile<FMT_F64><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena, va);
-    else if (basis)
+    else if (r.pair)
         k_tile<FMT_F32X2><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena32x2, va);
     else
         k_tile<FMT_F32><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena32, va);
@@ -755,16 +760,15 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     CUDA_TRY(cudaEventRecord(d->ev_fork, s));
     CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_fork, 0));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], d->s_aux));
-    launch_range(d, d->den1, va, nvec, d->s_aux, false);
-    launch_range(d, d->den2, va, nvec, d->s_aux, false);
+    for (const Range &r : d->den) launch_range(d, r, va, nvec, d->s_aux);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[7], d->s_aux));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], s));
-    for (const Range &r : d->fwd) launch_range(d, r, va, nvec, s, true);
+    for (const Range &r : d->fwd) launch_range(d, r, va, nvec, s);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[1], s));
-    launch_range(d, d->mid1, va, nvec, s, false);
-    launch_range(d, d->mid2, va, nvec, s, false);
+    launch_range(d, d->mid1, va, nvec, s);
+    launch_range(d, d->mid2, va, nvec, s);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[2], s));
-    for (const Range &r : d->bwd) launch_range(d, r, va, nvec, s, true);
+    for (const Range &r : d->bwd) launch_range(d, r, va, nvec, s);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[3], s));
     CUDA_TRY(cudaEventRecord(d->ev_join, d->s_aux));
     CUDA_TRY(cudaStreamWaitEvent(s, d->ev_join, 0));
@@ -939,7 +943,8 @@ extern "C" int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n)
     int launches = 0;
     for (const Range &r : d->fwd) launches += r.count > 0;
     for (const Range &r : d->bwd) launches += r.count > 0;
-    launches += (d->mid1.count > 0) + (d->mid2.count > 0) + (d->den1.count > 0) + (d->den2.count > 0);
+    for (const Range &r : d->den) launches += r.count > 0;
+    launches += (d->mid1.count > 0) + (d->mid2.count > 0);
     double mbytes = d->precision == H2ERI_GPU_MIXED ? d->alg_bytes_matrix_mixed : d->alg_bytes_matrix;
     double vals[13] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
                        (double)d->bytes_U, (double)d->bytes_B, (double)d->bytes_D,
