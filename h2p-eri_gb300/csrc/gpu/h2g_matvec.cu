@@ -95,6 +95,17 @@ __device__ __forceinline__ void split(double x, float &hi, float &lo)
     lo = __double2float_rn(x - (double)hi);
 }
 
+/* Float-pair addition (a_h + a_l) += (b_h + b_l) with an error-free two-sum
+ * on the high parts; the pair is left unnormalised. */
+__device__ __forceinline__ void dfadd(float &ah, float &al, float bh, float bl)
+{
+    const float s = __fadd_rn(ah, bh);
+    const float bp = __fsub_rn(s, ah);
+    const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bp)), __fsub_rn(bh, bp));
+    ah = s;
+    al = __fadd_rn(__fadd_rn(al, bl), err);
+}
+
 /* Column owned by lane `lane` in slot k (0..3) of a 128-column tile strip. */
 template <int FMT>
 __device__ __forceinline__ int lane_col(int lane, int k)
@@ -103,52 +114,157 @@ __device__ __forceinline__ int lane_col(int lane, int k)
     return (k < 2) ? 2 * lane + k : 64 + 2 * lane + (k - 2);
 }
 
+/* Warp reduction of 8 per-lane row partials (rows r0..r0+7) by recursive
+ * halving; afterwards lanes with (lane & 3) == 0 hold the full sum of row
+ * r0 + row_of_lane(lane). T is double, or float pairs given as (h, l). */
+__device__ __forceinline__ int halving_row(int lane)
+{
+    return ((lane & 16) ? 4 : 0) + ((lane & 8) ? 2 : 0) + ((lane & 4) ? 1 : 0);
+}
+
+__device__ __forceinline__ double reduce8_f64(double s[8], int lane)
+{
+    const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        double send = b16 ? s[k] : s[k + 4];
+        double keep = b16 ? s[k + 4] : s[k];
+        s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        double send = b8 ? s[k] : s[k + 2];
+        double keep = b8 ? s[k + 2] : s[k];
+        s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    double send = b4 ? s[0] : s[1];
+    double val = (b4 ? s[1] : s[0]) + __shfl_xor_sync(0xffffffffu, send, 4);
+    val += __shfl_xor_sync(0xffffffffu, val, 2);
+    val += __shfl_xor_sync(0xffffffffu, val, 1);
+    return val;
+}
+
+__device__ __forceinline__ double reduce8_df(float h[8], float l[8], int lane)
+{
+    const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float sh = b16 ? h[k] : h[k + 4], sl = b16 ? l[k] : l[k + 4];
+        float kh = b16 ? h[k + 4] : h[k], kl = b16 ? l[k + 4] : l[k];
+        dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 16), __shfl_xor_sync(0xffffffffu, sl, 16));
+        h[k] = kh; l[k] = kl;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        float sh = b8 ? h[k] : h[k + 2], sl = b8 ? l[k] : l[k + 2];
+        float kh = b8 ? h[k + 2] : h[k], kl = b8 ? l[k + 2] : l[k];
+        dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 8), __shfl_xor_sync(0xffffffffu, sl, 8));
+        h[k] = kh; l[k] = kl;
+    }
+    float sh = b4 ? h[0] : h[1], sl = b4 ? l[0] : l[1];
+    float vh = b4 ? h[1] : h[0], vl = b4 ? l[1] : l[0];
+    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, sh, 4), __shfl_xor_sync(0xffffffffu, sl, 4));
+    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 2), __shfl_xor_sync(0xffffffffu, vl, 2));
+    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 1), __shfl_xor_sync(0xffffffffu, vl, 1));
+    return (double)vh + (double)vl;
+}
+
 /* One CTA per (tile, vector). 8 warps; warp w owns rows 8w..8w+7 of the
  * tile; each lane owns 4 columns (lane_col). All eight rows are loaded before
  * any arithmetic so each warp keeps its row loads in flight together.
- * FMT_F64: plain FP64 FMAs. FMT_F32 / FMT_F32X2: compensated FP32 products
- * (cacc) with per-lane float-pair partial sums; cross-lane and cross-warp
- * reductions and the output atomics are FP64. */
+ *   FMT_F64   : FP64 FMAs, FP64 reductions.
+ *   FMT_F32X2 : matrix stored as float pairs; products are error-free
+ *               (cacc) and partial sums are float pairs, so the result keeps
+ *               ~2^-48 relative accuracy while running on the FP32 pipe.
+ *   FMT_F32   : matrix stored as single floats (2^-24 storage rounding);
+ *               products a*(x_hi + x_lo) with FP32 FMAs over the lane's short
+ *               chain (4 or 8 terms), float-pair reductions beyond it.
+ * The tile's input slices are split into float pairs once, in shared memory;
+ * every output element is converted to FP64 once and added with an FP64
+ * atomic. */
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
 k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va)
 {
+    __shared__ float sx0h[kTileCols], sx0l[kTileCols], sx1h[kTileRows], sx1l[kTileRows];
+    __shared__ __align__(16) unsigned char red_raw[8 * kTileCols * 8];
     const Tile t = tiles[blockIdx.x];
     const int v = blockIdx.y;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
     const int nr = t.nr, nc = t.nc;
+    const int r0 = warp * 8;
     bool ok[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) ok[k] = lane_col<FMT>(lane, k) < nc;
 
-    /* N-side input, split into float pairs for the mixed formats */
-    double xv[4] = {0.0, 0.0, 0.0, 0.0};
-    if (opN) {
-        const double *in0 = vec_ptr(va, t.k_in0, t.in0, v);
+    if (FMT == FMT_F64) {
+        double xv[4] = {0.0, 0.0, 0.0, 0.0};
+        if (opN) {
+            const double *in0 = vec_ptr(va, t.k_in0, t.in0, v);
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (ok[k]) xv[k] = in0[lane_col<FMT>(lane, k)];
+            for (int k = 0; k < 4; k++)
+                if (ok[k]) xv[k] = in0[lane_col<FMT>(lane, k)];
+        }
+        double a[8][4];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int r = r0 + i;
+            const double *row = reinterpret_cast<const double *>(arena_v) + t.a + (size_t)r * t.ld;
+            double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
+            if (r < nr && ok[0]) pa = __ldg(reinterpret_cast<const double2 *>(row + 2 * lane));
+            if (r < nr && ok[2]) pb = __ldg(reinterpret_cast<const double2 *>(row + 64 + 2 * lane));
+            a[i][0] = pa.x; a[i][1] = pa.y; a[i][2] = pb.x; a[i][3] = pb.y;
+        }
+        if (opN) {
+            double s[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) s[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
+            const double val = reduce8_f64(s, lane);
+            const int row = r0 + halving_row(lane);
+            if ((lane & 3) == 0 && row < nr) atomicAdd(vec_ptr(va, t.k_out0, t.out0, v) + row, val);
+        }
+        if (opT) {
+            double (*red)[kTileCols] = reinterpret_cast<double (*)[kTileCols]>(red_raw);
+            const double *in1 = vec_ptr(va, t.k_in1, t.in1, v);
+            double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const double x1 = (r0 + i < nr) ? in1[r0 + i] : 0.0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc[k] += a[i][k] * x1;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) red[warp][lane_col<FMT>(lane, k)] = acc[k];
+            __syncthreads();
+            double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
+            for (int c = tid; c < nc; c += kTileThreads) {
+                double sum = 0.0;
+#pragma unroll
+                for (int w = 0; w < 8; w++) sum += red[w][c];
+                atomicAdd(out1 + c, sum);
+            }
+        }
+        return;
     }
-    float xh[4], xl[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) split(xv[k], xh[k], xl[k]);
 
-    /* load 8 rows x 4 columns of the tile */
-    double a[8][4];
+    /* ---- FP32 formats: split the tile's input slices once ---- */
+    if (tid < kTileCols) {
+        float h = 0.f, l = 0.f;
+        if (opN && tid < nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
+        sx0h[tid] = h; sx0l[tid] = l;
+    } else if (tid < kTileCols + kTileRows) {
+        const int r = tid - kTileCols;
+        float h = 0.f, l = 0.f;
+        if (opT && r < nr) split(vec_ptr(va, t.k_in1, t.in1, v)[r], h, l);
+        sx1h[r] = h; sx1l[r] = l;
+    }
     float ahi[8][4], alo[8][4];
-    const int r0 = warp * 8;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const int r = r0 + i;
         const bool live = r < nr;
-        if (FMT == FMT_F64) {
-            const double *row = reinterpret_cast<const double *>(arena_v) + t.a + (size_t)r * t.ld;
-            double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
-            if (live && ok[0]) pa = __ldg(reinterpret_cast<const double2 *>(row + 2 * lane));
-            if (live && ok[2]) pb = __ldg(reinterpret_cast<const double2 *>(row + 64 + 2 * lane));
-            a[i][0] = pa.x; a[i][1] = pa.y; a[i][2] = pb.x; a[i][3] = pb.y;
-        } else if (FMT == FMT_F32) {
+        if (FMT == FMT_F32) {
             const float *row = reinterpret_cast<const float *>(arena_v) + t.a2 + (size_t)r * t.ld2;
             float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
             if (live && ok[0]) q = __ldg(reinterpret_cast<const float4 *>(row + 4 * lane));
@@ -162,79 +278,55 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
             ahi[i][2] = qb.x; alo[i][2] = qb.y; ahi[i][3] = qb.z; alo[i][3] = qb.w;
         }
     }
+    __syncthreads();
 
     if (opN) {
-        double s[8];
+        float xh[4], xl[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) { xh[k] = sx0h[lane_col<FMT>(lane, k)]; xl[k] = sx0l[lane_col<FMT>(lane, k)]; }
+        float sh[8], sl[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) {
-            if (FMT == FMT_F64) {
-                s[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
-            } else {
-                float sh = 0.f, sl = 0.f;
+            if (FMT == FMT_F32) {
+                float s = 0.f;
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    if (FMT == FMT_F32) cacc1(sh, sl, ahi[i][k], xh[k], xl[k]);
-                    else cacc(sh, sl, ahi[i][k], alo[i][k], xh[k], xl[k]);
-                }
-                s[i] = (double)sh + (double)sl;
+                for (int k = 0; k < 4; k++) s = fmaf(ahi[i][k], xh[k], fmaf(ahi[i][k], xl[k], s));
+                sh[i] = s; sl[i] = 0.f;
+            } else {
+                sh[i] = 0.f; sl[i] = 0.f;
+#pragma unroll
+                for (int k = 0; k < 4; k++) cacc(sh[i], sl[i], ahi[i][k], alo[i][k], xh[k], xl[k]);
             }
         }
-        /* reduce 8 row sums across the warp by recursive halving */
-        const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            double send = b16 ? s[k] : s[k + 4];
-            double keep = b16 ? s[k + 4] : s[k];
-            s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-        }
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            double send = b8 ? s[k] : s[k + 2];
-            double keep = b8 ? s[k + 2] : s[k];
-            s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-        }
-        double send = b4 ? s[0] : s[1];
-        double val = (b4 ? s[1] : s[0]) + __shfl_xor_sync(0xffffffffu, send, 4);
-        val += __shfl_xor_sync(0xffffffffu, val, 2);
-        val += __shfl_xor_sync(0xffffffffu, val, 1);
-        const int row = r0 + (b16 ? 4 : 0) + (b8 ? 2 : 0) + (b4 ? 1 : 0);
+        const double val = reduce8_df(sh, sl, lane);
+        const int row = r0 + halving_row(lane);
         if ((lane & 3) == 0 && row < nr) atomicAdd(vec_ptr(va, t.k_out0, t.out0, v) + row, val);
     }
     if (opT) {
-        __shared__ double red[8][kTileCols];
-        const double *in1 = vec_ptr(va, t.k_in1, t.in1, v);
-        double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        if (FMT == FMT_F64) {
+        float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw);
+        float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw + 8 * kTileCols * 4);
+        float ch[4] = {0.f, 0.f, 0.f, 0.f}, cl[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const double x1 = (r0 + i < nr) ? in1[r0 + i] : 0.0;
+        for (int i = 0; i < 8; i++) {
+            const float x1h = sx1h[r0 + i], x1l = sx1l[r0 + i];
 #pragma unroll
-                for (int k = 0; k < 4; k++) acc[k] += a[i][k] * x1;
+            for (int k = 0; k < 4; k++) {
+                if (FMT == FMT_F32) ch[k] = fmaf(ahi[i][k], x1h, fmaf(ahi[i][k], x1l, ch[k]));
+                else cacc(ch[k], cl[k], ahi[i][k], alo[i][k], x1h, x1l);
             }
-        } else {
-            float sh[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                float x1h, x1l;
-                split((r0 + i < nr) ? in1[r0 + i] : 0.0, x1h, x1l);
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    if (FMT == FMT_F32) cacc1(sh[k], sl[k], ahi[i][k], x1h, x1l);
-                    else cacc(sh[k], sl[k], ahi[i][k], alo[i][k], x1h, x1l);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < 4; k++) acc[k] = (double)sh[k] + (double)sl[k];
         }
 #pragma unroll
-        for (int k = 0; k < 4; k++) red[warp][lane_col<FMT>(lane, k)] = acc[k];
+        for (int k = 0; k < 4; k++) {
+            rh[warp][lane_col<FMT>(lane, k)] = ch[k];
+            rl[warp][lane_col<FMT>(lane, k)] = cl[k];
+        }
         __syncthreads();
         double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
-        for (int c = threadIdx.x; c < nc; c += kTileThreads) {
-            double sum = 0.0;
+        for (int c = tid; c < nc; c += kTileThreads) {
+            float h = rh[0][c], l = rl[0][c];
 #pragma unroll
-            for (int w = 0; w < 8; w++) sum += red[w][c];
-            atomicAdd(out1 + c, sum);
+            for (int w = 1; w < 8; w++) dfadd(h, l, rh[w][c], rl[w][c]);
+            atomicAdd(out1 + c, (double)h + (double)l);
         }
     }
 }
