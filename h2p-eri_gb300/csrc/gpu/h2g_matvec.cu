@@ -169,9 +169,12 @@ __device__ __forceinline__ double reduce8_df(float h[8], float l[8], int lane)
     return (double)vh + (double)vl;
 }
 
-/* One CTA per (tile, vector). 8 warps; warp w owns rows 8w..8w+7 of the
- * tile; each lane owns 4 columns (lane_col). All eight rows are loaded before
- * any arithmetic so each warp keeps its row loads in flight together.
+/* One CTA per (tile, vector). A tile is a chunk of up to kChunkRows rows and
+ * kTileCols columns, processed as 64-row sub-tiles: warp w owns rows 8w..8w+7
+ * of each sub-tile, each lane owns 4 columns (lane_col), and all eight rows
+ * of a sub-tile are loaded before any arithmetic. N-side row sums are added
+ * per sub-tile; T-side column sums stay in registers over the whole chunk
+ * and are added once, so a tall basis sees few atomics per coefficient.
  *   FMT_F64   : FP64 FMAs, FP64 reductions.
  *   FMT_F32X2 : matrix stored as float pairs; products are error-free
  *               (cacc) and partial sums are float pairs, so the result keeps
@@ -187,17 +190,17 @@ template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
 k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va)
 {
-    __shared__ float sx0h[kTileCols], sx0l[kTileCols], sx1h[kTileRows], sx1l[kTileRows];
+    __shared__ float sx0h[kTileCols], sx0l[kTileCols], sx1h[kChunkRows], sx1l[kChunkRows];
     __shared__ __align__(16) unsigned char red_raw[8 * kTileCols * 8];
     const Tile t = tiles[blockIdx.x];
     const int v = blockIdx.y;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
     const int nr = t.nr, nc = t.nc;
-    const int r0 = warp * 8;
     bool ok[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) ok[k] = lane_col<FMT>(lane, k) < nc;
+    double *out0 = opN ? vec_ptr(va, t.k_out0, t.out0, v) : nullptr;
 
     if (FMT == FMT_F64) {
         double xv[4] = {0.0, 0.0, 0.0, 0.0};
@@ -207,34 +210,39 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
             for (int k = 0; k < 4; k++)
                 if (ok[k]) xv[k] = in0[lane_col<FMT>(lane, k)];
         }
-        double a[8][4];
+        const double *in1 = opT ? vec_ptr(va, t.k_in1, t.in1, v) : nullptr;
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int sub = 0; sub < nr; sub += kTileRows) {
+            const int r0 = sub + warp * 8;
+            double a[8][4];
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const int r = r0 + i;
-            const double *row = reinterpret_cast<const double *>(arena_v) + t.a + (size_t)r * t.ld;
-            double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
-            if (r < nr && ok[0]) pa = __ldg(reinterpret_cast<const double2 *>(row + 2 * lane));
-            if (r < nr && ok[2]) pb = __ldg(reinterpret_cast<const double2 *>(row + 64 + 2 * lane));
-            a[i][0] = pa.x; a[i][1] = pa.y; a[i][2] = pb.x; a[i][3] = pb.y;
-        }
-        if (opN) {
-            double s[8];
+            for (int i = 0; i < 8; i++) {
+                const int r = r0 + i;
+                const double *row = reinterpret_cast<const double *>(arena_v) + t.a + (size_t)r * t.ld;
+                double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
+                if (r < nr && ok[0]) pa = __ldg(reinterpret_cast<const double2 *>(row + 2 * lane));
+                if (r < nr && ok[2]) pb = __ldg(reinterpret_cast<const double2 *>(row + 64 + 2 * lane));
+                a[i][0] = pa.x; a[i][1] = pa.y; a[i][2] = pb.x; a[i][3] = pb.y;
+            }
+            if (opN) {
+                double sr[8];
 #pragma unroll
-            for (int i = 0; i < 8; i++) s[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
-            const double val = reduce8_f64(s, lane);
-            const int row = r0 + halving_row(lane);
-            if ((lane & 3) == 0 && row < nr) atomicAdd(vec_ptr(va, t.k_out0, t.out0, v) + row, val);
+                for (int i = 0; i < 8; i++) sr[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
+                const double val = reduce8_f64(sr, lane);
+                const int row = r0 + halving_row(lane);
+                if ((lane & 3) == 0 && row < nr) atomicAdd(out0 + row, val);
+            }
+            if (opT) {
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    const double x1 = (r0 + i < nr) ? in1[r0 + i] : 0.0;
+#pragma unroll
+                    for (int k = 0; k < 4; k++) acc[k] += a[i][k] * x1;
+                }
+            }
         }
         if (opT) {
             double (*red)[kTileCols] = reinterpret_cast<double (*)[kTileCols]>(red_raw);
-            const double *in1 = vec_ptr(va, t.k_in1, t.in1, v);
-            double acc[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const double x1 = (r0 + i < nr) ? in1[r0 + i] : 0.0;
-#pragma unroll
-                for (int k = 0; k < 4; k++) acc[k] += a[i][k] * x1;
-            }
 #pragma unroll
             for (int k = 0; k < 4; k++) red[warp][lane_col<FMT>(lane, k)] = acc[k];
             __syncthreads();
@@ -254,64 +262,69 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
         float h = 0.f, l = 0.f;
         if (opN && tid < nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
         sx0h[tid] = h; sx0l[tid] = l;
-    } else if (tid < kTileCols + kTileRows) {
-        const int r = tid - kTileCols;
+    }
+    for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
         float h = 0.f, l = 0.f;
         if (opT && r < nr) split(vec_ptr(va, t.k_in1, t.in1, v)[r], h, l);
         sx1h[r] = h; sx1l[r] = l;
     }
-    float ahi[8][4], alo[8][4];
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const int r = r0 + i;
-        const bool live = r < nr;
-        if (FMT == FMT_F32) {
-            const float *row = reinterpret_cast<const float *>(arena_v) + t.a2 + (size_t)r * t.ld2;
-            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (live && ok[0]) q = __ldg(reinterpret_cast<const float4 *>(row + 4 * lane));
-            ahi[i][0] = q.x; ahi[i][1] = q.y; ahi[i][2] = q.z; ahi[i][3] = q.w;
-        } else {
-            const float2 *row = reinterpret_cast<const float2 *>(arena_v) + t.a2 + (size_t)r * t.ld2;
-            float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (live && ok[0]) qa = __ldg(reinterpret_cast<const float4 *>(row + 2 * lane));
-            if (live && ok[2]) qb = __ldg(reinterpret_cast<const float4 *>(row + 64 + 2 * lane));
-            ahi[i][0] = qa.x; alo[i][0] = qa.y; ahi[i][1] = qa.z; alo[i][1] = qa.w;
-            ahi[i][2] = qb.x; alo[i][2] = qb.y; ahi[i][3] = qb.z; alo[i][3] = qb.w;
-        }
-    }
     __syncthreads();
-
-    if (opN) {
-        float xh[4], xl[4];
+    float xh[4], xl[4];
 #pragma unroll
-        for (int k = 0; k < 4; k++) { xh[k] = sx0h[lane_col<FMT>(lane, k)]; xl[k] = sx0l[lane_col<FMT>(lane, k)]; }
-        float sh[8], sl[8];
+    for (int k = 0; k < 4; k++) { xh[k] = sx0h[lane_col<FMT>(lane, k)]; xl[k] = sx0l[lane_col<FMT>(lane, k)]; }
+    float ch[4] = {0.f, 0.f, 0.f, 0.f}, cl[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int sub = 0; sub < nr; sub += kTileRows) {
+        const int r0 = sub + warp * 8;
+        float ahi[8][4], alo[8][4];
 #pragma unroll
         for (int i = 0; i < 8; i++) {
-            sh[i] = 0.f; sl[i] = 0.f;
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                if (FMT == FMT_F32) cacc1(sh[i], sl[i], ahi[i][k], xh[k], xl[k]);
-                else cacc(sh[i], sl[i], ahi[i][k], alo[i][k], xh[k], xl[k]);
+            const int r = r0 + i;
+            const bool live = r < nr;
+            if (FMT == FMT_F32) {
+                const float *row = reinterpret_cast<const float *>(arena_v) + t.a2 + (size_t)r * t.ld2;
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (live && ok[0]) q = __ldg(reinterpret_cast<const float4 *>(row + 4 * lane));
+                ahi[i][0] = q.x; ahi[i][1] = q.y; ahi[i][2] = q.z; ahi[i][3] = q.w;
+            } else {
+                const float2 *row = reinterpret_cast<const float2 *>(arena_v) + t.a2 + (size_t)r * t.ld2;
+                float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (live && ok[0]) qa = __ldg(reinterpret_cast<const float4 *>(row + 2 * lane));
+                if (live && ok[2]) qb = __ldg(reinterpret_cast<const float4 *>(row + 64 + 2 * lane));
+                ahi[i][0] = qa.x; alo[i][0] = qa.y; ahi[i][1] = qa.z; alo[i][1] = qa.w;
+                ahi[i][2] = qb.x; alo[i][2] = qb.y; ahi[i][3] = qb.z; alo[i][3] = qb.w;
             }
         }
-        const double val = reduce8_df(sh, sl, lane);
-        const int row = r0 + halving_row(lane);
-        if ((lane & 3) == 0 && row < nr) atomicAdd(vec_ptr(va, t.k_out0, t.out0, v) + row, val);
+        if (opN) {
+            float sh[8], sl[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                sh[i] = 0.f; sl[i] = 0.f;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (FMT == FMT_F32) cacc1(sh[i], sl[i], ahi[i][k], xh[k], xl[k]);
+                    else cacc(sh[i], sl[i], ahi[i][k], alo[i][k], xh[k], xl[k]);
+                }
+            }
+            const double val = reduce8_df(sh, sl, lane);
+            const int row = r0 + halving_row(lane);
+            if ((lane & 3) == 0 && row < nr) atomicAdd(out0 + row, val);
+        }
+        if (opT) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int r = min(r0 + i, kChunkRows - 1);
+                const float x1h = sx1h[r], x1l = sx1l[r];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (FMT == FMT_F32) cacc1(ch[k], cl[k], ahi[i][k], x1h, x1l);
+                    else cacc(ch[k], cl[k], ahi[i][k], alo[i][k], x1h, x1l);
+                }
+            }
+        }
     }
     if (opT) {
         float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw);
         float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw + 8 * kTileCols * 4);
-        float ch[4] = {0.f, 0.f, 0.f, 0.f}, cl[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const float x1h = sx1h[r0 + i], x1l = sx1l[r0 + i];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                if (FMT == FMT_F32) cacc1(ch[k], cl[k], ahi[i][k], x1h, x1l);
-                else cacc(ch[k], cl[k], ahi[i][k], alo[i][k], x1h, x1l);
-            }
-        }
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             rh[warp][lane_col<FMT>(lane, k)] = ch[k];
@@ -409,7 +422,7 @@ struct Planner {
     void add(const MatLoc &m, int nrow, int ncol, uint8_t kin0, int in0, uint8_t kout0, int out0,
              uint8_t kin1, int in1, uint8_t kout1, int out1)
     {
-        for (int r0 = 0; r0 < nrow; r0 += kTileRows)
+        for (int r0 = 0; r0 < nrow; r0 += kChunkRows)
             for (int c0 = 0; c0 < ncol; c0 += kTileCols) {
                 Tile t;
                 std::memset(&t, 0, sizeof(t));
@@ -417,7 +430,7 @@ struct Planner {
                 t.a2 = m.a2 + (size_t)r0 * m.ld2 + c0;
                 t.ld = m.ld;
                 t.ld2 = m.ld2;
-                t.nr = (int16_t)std::min(kTileRows, nrow - r0);
+                t.nr = (int16_t)std::min(kChunkRows, nrow - r0);
                 t.nc = (int16_t)std::min(kTileCols, ncol - c0);
                 if (kout0 != VK_NONE) { t.k_in0 = kin0; t.in0 = in0 + c0; t.k_out0 = kout0; t.out0 = out0 + r0; }
                 if (kout1 != VK_NONE) { t.k_in1 = kin1; t.in1 = in1 + r0; t.k_out1 = kout1; t.out1 = out1 + c0; }
