@@ -169,12 +169,153 @@ __device__ __forceinline__ double reduce8_df(float h[8], float l[8], int lane)
     return (double)vh + (double)vl;
 }
 
+/* ---- shared-memory staging with cp.async ---- */
+constexpr int kStageBytes = 32768;
+constexpr int kStages = 3;
+constexpr size_t kTileSmem = (size_t)kStageBytes * kStages;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <int FMT> struct FmtInfo;
+template <> struct FmtInfo<FMT_F64> { static constexpr int ebytes = 8; };
+template <> struct FmtInfo<FMT_F32> { static constexpr int ebytes = 4; };
+template <> struct FmtInfo<FMT_F32X2> { static constexpr int ebytes = 8; };
+
+/* Issue the copies of one stage: rows [row0, row0 + SR) of the tile, all
+ * kTileCols columns, into a dense SR x (kTileCols * ebytes) smem block. Rows
+ * at or beyond nr and columns beyond the tile are zero-filled. */
+template <int FMT>
+__device__ __forceinline__ void issue_stage(unsigned char *buf, const unsigned char *base, size_t ld_bytes, int row0,
+                                            int nr, int nc_bytes16, int tid)
+{
+    constexpr int RB = kTileCols * FmtInfo<FMT>::ebytes;   /* bytes per stage row */
+    constexpr int CPR = RB / 16;                            /* 16-byte chunks per row */
+    constexpr int NCH = kStageBytes / 16;
+#pragma unroll
+    for (int j = 0; j < NCH / kTileThreads; j++) {
+        const int c = tid + j * kTileThreads;
+        const int row = c / CPR, cc = c - row * CPR;
+        const int grow = row0 + row;
+        int valid = 0;
+        const unsigned char *src = base;
+        if (grow < nr) {
+            valid = min(16, max(0, nc_bytes16 - cc * 16));
+            if (valid > 0) src = base + (size_t)grow * ld_bytes + cc * 16;
+        }
+        cp_async16(buf + c * 16, src, valid);
+    }
+}
+
+/* Row partials of R rows per warp (R = 8 or 4) reduced across the warp by
+ * recursive halving; returns the value of row `halving_row_R(lane)` on the
+ * lanes that finish with a full sum. */
+template <int R>
+__device__ __forceinline__ int halving_row_R(int lane)
+{
+    if (R == 8) return ((lane & 16) ? 4 : 0) + ((lane & 8) ? 2 : 0) + ((lane & 4) ? 1 : 0);
+    return ((lane & 16) ? 2 : 0) + ((lane & 8) ? 1 : 0);
+}
+template <int R>
+__device__ __forceinline__ bool halving_owner(int lane)
+{
+    return (R == 8) ? ((lane & 3) == 0) : ((lane & 7) == 0);
+}
+
+template <int R>
+__device__ __forceinline__ double reduceR_f64(double *s, int lane)
+{
+    const bool b16 = lane & 16, b8 = lane & 8;
+    if (R == 8) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            double send = b16 ? s[k] : s[k + 4];
+            double keep = b16 ? s[k + 4] : s[k];
+            s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            double send = b8 ? s[k] : s[k + 2];
+            double keep = b8 ? s[k + 2] : s[k];
+            s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+        const bool b4 = lane & 4;
+        double send = b4 ? s[0] : s[1];
+        double val = (b4 ? s[1] : s[0]) + __shfl_xor_sync(0xffffffffu, send, 4);
+        val += __shfl_xor_sync(0xffffffffu, val, 2);
+        val += __shfl_xor_sync(0xffffffffu, val, 1);
+        return val;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        double send = b16 ? s[k] : s[k + 2];
+        double keep = b16 ? s[k + 2] : s[k];
+        s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    double send = b8 ? s[0] : s[1];
+    double val = (b8 ? s[1] : s[0]) + __shfl_xor_sync(0xffffffffu, send, 8);
+    val += __shfl_xor_sync(0xffffffffu, val, 4);
+    val += __shfl_xor_sync(0xffffffffu, val, 2);
+    val += __shfl_xor_sync(0xffffffffu, val, 1);
+    return val;
+}
+
+template <int R>
+__device__ __forceinline__ void reduceR_df(float *h, float *l, int lane, float &vh, float &vl)
+{
+    const bool b16 = lane & 16, b8 = lane & 8;
+    if (R == 8) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            float sh = b16 ? h[k] : h[k + 4], sl = b16 ? l[k] : l[k + 4];
+            float kh = b16 ? h[k + 4] : h[k], kl = b16 ? l[k + 4] : l[k];
+            dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 16), __shfl_xor_sync(0xffffffffu, sl, 16));
+            h[k] = kh; l[k] = kl;
+        }
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            float sh = b8 ? h[k] : h[k + 2], sl = b8 ? l[k] : l[k + 2];
+            float kh = b8 ? h[k + 2] : h[k], kl = b8 ? l[k + 2] : l[k];
+            dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 8), __shfl_xor_sync(0xffffffffu, sl, 8));
+            h[k] = kh; l[k] = kl;
+        }
+        const bool b4 = lane & 4;
+        float sh = b4 ? h[0] : h[1], sl = b4 ? l[0] : l[1];
+        vh = b4 ? h[1] : h[0];
+        vl = b4 ? l[1] : l[0];
+        dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, sh, 4), __shfl_xor_sync(0xffffffffu, sl, 4));
+    } else {
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            float sh = b16 ? h[k] : h[k + 2], sl = b16 ? l[k] : l[k + 2];
+            float kh = b16 ? h[k + 2] : h[k], kl = b16 ? l[k + 2] : l[k];
+            dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 16), __shfl_xor_sync(0xffffffffu, sl, 16));
+            h[k] = kh; l[k] = kl;
+        }
+        float sh = b8 ? h[0] : h[1], sl = b8 ? l[0] : l[1];
+        vh = b8 ? h[1] : h[0];
+        vl = b8 ? l[1] : l[0];
+        dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, sh, 8), __shfl_xor_sync(0xffffffffu, sl, 8));
+        dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 4), __shfl_xor_sync(0xffffffffu, vl, 4));
+    }
+    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 2), __shfl_xor_sync(0xffffffffu, vl, 2));
+    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 1), __shfl_xor_sync(0xffffffffu, vl, 1));
+}
+
 /* One CTA per (tile, vector). A tile is a chunk of up to kChunkRows rows and
- * kTileCols columns, processed as 64-row sub-tiles: warp w owns rows 8w..8w+7
- * of each sub-tile, each lane owns 4 columns (lane_col), and all eight rows
- * of a sub-tile are loaded before any arithmetic. N-side row sums are added
- * per sub-tile; T-side column sums stay in registers over the whole chunk
- * and are added once, so a tall basis sees few atomics per coefficient.
+ * kTileCols columns. The chunk streams through a kStages-deep ring of 32 KB
+ * shared-memory stages filled with cp.async (16-byte copies, any leading
+ * dimension, zero fill past the tile edge), so the next stages are in flight
+ * while the current one is multiplied. A stage holds SR = 64 rows of single
+ * floats or 32 rows of 8-byte elements; warp w multiplies rows
+ * [w*SR/8, (w+1)*SR/8) and each lane owns 4 columns (lane_col).
+ * N-side row sums are added per stage; T-side column sums stay in registers
+ * over the whole chunk and are added once (few atomics per coefficient).
  *   FMT_F64   : FP64 FMAs, FP64 reductions.
  *   FMT_F32X2 : matrix stored as float pairs; products are error-free
  *               (cacc) and partial sums are float pairs, so the result keeps
@@ -183,24 +324,46 @@ __device__ __forceinline__ double reduce8_df(float h[8], float l[8], int lane)
  *               products and sums as for float pairs, so the storage
  *               rounding is the only error (plain FP32 FMA chains roughly
  *               double it, measured 1.2e-8 vs 5e-9 on C10H22).
- * The tile's input slices are split into float pairs once, in shared memory;
- * every output element is converted to FP64 once and added with an FP64
- * atomic. */
+ * Inputs are split into float pairs once per tile in shared memory; every
+ * output element is converted to FP64 once and added with an FP64 atomic. */
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
 k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va)
 {
+    constexpr int EB = FmtInfo<FMT>::ebytes;
+    constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage   */
+    constexpr int RW = SR / 8;                            /* rows per warp    */
+    constexpr int RB = kTileCols * EB;                    /* bytes per row    */
+    extern __shared__ __align__(128) unsigned char stage_raw[];
     __shared__ float sx0h[kTileCols], sx0l[kTileCols], sx1h[kChunkRows], sx1l[kChunkRows];
     __shared__ __align__(16) unsigned char red_raw[8 * kTileCols * 8];
+
     const Tile t = tiles[blockIdx.x];
     const int v = blockIdx.y;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
     const int nr = t.nr, nc = t.nc;
+    const int nstage = (nr + SR - 1) / SR;
+    const unsigned char *base = (FMT == FMT_F64)
+        ? reinterpret_cast<const unsigned char *>(reinterpret_cast<const double *>(arena_v) + t.a)
+        : (FMT == FMT_F32) ? reinterpret_cast<const unsigned char *>(reinterpret_cast<const float *>(arena_v) + t.a2)
+                           : reinterpret_cast<const unsigned char *>(reinterpret_cast<const float2 *>(arena_v) + t.a2);
+    const size_t ld_bytes = (size_t)((FMT == FMT_F64) ? t.ld : t.ld2) * EB;
+    const int nc_bytes16 = ((nc * EB) + 15) & ~15;
+
+    /* prologue: first two stages in flight */
+    issue_stage<FMT>(stage_raw, base, ld_bytes, 0, nr, nc_bytes16, tid);
+    cp_async_commit();
+    if (nstage > 1) issue_stage<FMT>(stage_raw + kStageBytes, base, ld_bytes, SR, nr, nc_bytes16, tid);
+    cp_async_commit();
+
+    double *out0 = opN ? vec_ptr(va, t.k_out0, t.out0, v) : nullptr;
     bool ok[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) ok[k] = lane_col<FMT>(lane, k) < nc;
-    double *out0 = opN ? vec_ptr(va, t.k_out0, t.out0, v) : nullptr;
+    /* byte offsets of this lane's two 16-byte pieces inside a stage row */
+    const int offA = (FMT == FMT_F32) ? 16 * lane : 16 * lane;
+    const int offB = 512 + 16 * lane;   /* used by the 8-byte formats only */
 
     if (FMT == FMT_F64) {
         double xv[4] = {0.0, 0.0, 0.0, 0.0};
@@ -212,39 +375,44 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
         }
         const double *in1 = opT ? vec_ptr(va, t.k_in1, t.in1, v) : nullptr;
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int sub = 0; sub < nr; sub += kTileRows) {
-            const int r0 = sub + warp * 8;
-            double a[8][4];
+        for (int k = 0; k < nstage; k++) {
+            cp_async_wait1();
+            __syncthreads();
+            if (k + 2 < nstage)
+                issue_stage<FMT>(stage_raw + ((k + 2) % kStages) * kStageBytes, base, ld_bytes, (k + 2) * SR, nr,
+                                 nc_bytes16, tid);
+            cp_async_commit();
+            const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
+            const int r0 = k * SR + warp * RW;
+            double a[RW][4];
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const int r = r0 + i;
-                const double *row = reinterpret_cast<const double *>(arena_v) + t.a + (size_t)r * t.ld;
-                double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
-                if (r < nr && ok[0]) pa = __ldg(reinterpret_cast<const double2 *>(row + 2 * lane));
-                if (r < nr && ok[2]) pb = __ldg(reinterpret_cast<const double2 *>(row + 64 + 2 * lane));
+            for (int i = 0; i < RW; i++) {
+                const unsigned char *row = buf + (warp * RW + i) * RB;
+                const double2 pa = *reinterpret_cast<const double2 *>(row + offA);
+                const double2 pb = *reinterpret_cast<const double2 *>(row + offB);
                 a[i][0] = pa.x; a[i][1] = pa.y; a[i][2] = pb.x; a[i][3] = pb.y;
             }
             if (opN) {
-                double sr[8];
+                double sr[RW];
 #pragma unroll
-                for (int i = 0; i < 8; i++) sr[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
-                const double val = reduce8_f64(sr, lane);
-                const int row = r0 + halving_row(lane);
-                if ((lane & 3) == 0 && row < nr) atomicAdd(out0 + row, val);
+                for (int i = 0; i < RW; i++) sr[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
+                const double val = reduceR_f64<RW>(sr, lane);
+                const int row = r0 + halving_row_R<RW>(lane);
+                if (halving_owner<RW>(lane) && row < nr) atomicAdd(out0 + row, val);
             }
             if (opT) {
 #pragma unroll
-                for (int i = 0; i < 8; i++) {
+                for (int i = 0; i < RW; i++) {
                     const double x1 = (r0 + i < nr) ? in1[r0 + i] : 0.0;
 #pragma unroll
-                    for (int k = 0; k < 4; k++) acc[k] += a[i][k] * x1;
+                    for (int c = 0; c < 4; c++) acc[c] += a[i][c] * x1;
                 }
             }
         }
         if (opT) {
             double (*red)[kTileCols] = reinterpret_cast<double (*)[kTileCols]>(red_raw);
 #pragma unroll
-            for (int k = 0; k < 4; k++) red[warp][lane_col<FMT>(lane, k)] = acc[k];
+            for (int c = 0; c < 4; c++) red[warp][lane_col<FMT>(lane, c)] = acc[c];
             __syncthreads();
             double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
             for (int c = tid; c < nc; c += kTileThreads) {
@@ -271,53 +439,56 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     __syncthreads();
     float xh[4], xl[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) { xh[k] = sx0h[lane_col<FMT>(lane, k)]; xl[k] = sx0l[lane_col<FMT>(lane, k)]; }
+    for (int c = 0; c < 4; c++) { xh[c] = sx0h[lane_col<FMT>(lane, c)]; xl[c] = sx0l[lane_col<FMT>(lane, c)]; }
     float ch[4] = {0.f, 0.f, 0.f, 0.f}, cl[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int sub = 0; sub < nr; sub += kTileRows) {
-        const int r0 = sub + warp * 8;
-        float ahi[8][4], alo[8][4];
+    for (int k = 0; k < nstage; k++) {
+        cp_async_wait1();
+        __syncthreads();
+        if (k + 2 < nstage)
+            issue_stage<FMT>(stage_raw + ((k + 2) % kStages) * kStageBytes, base, ld_bytes, (k + 2) * SR, nr,
+                             nc_bytes16, tid);
+        cp_async_commit();
+        const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
+        const int r0 = k * SR + warp * RW;
+        float ahi[RW][4], alo[RW][4];
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const int r = r0 + i;
-            const bool live = r < nr;
+        for (int i = 0; i < RW; i++) {
+            const unsigned char *row = buf + (warp * RW + i) * RB;
             if (FMT == FMT_F32) {
-                const float *row = reinterpret_cast<const float *>(arena_v) + t.a2 + (size_t)r * t.ld2;
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (live && ok[0]) q = __ldg(reinterpret_cast<const float4 *>(row + 4 * lane));
+                const float4 q = *reinterpret_cast<const float4 *>(row + offA);
                 ahi[i][0] = q.x; ahi[i][1] = q.y; ahi[i][2] = q.z; ahi[i][3] = q.w;
             } else {
-                const float2 *row = reinterpret_cast<const float2 *>(arena_v) + t.a2 + (size_t)r * t.ld2;
-                float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (live && ok[0]) qa = __ldg(reinterpret_cast<const float4 *>(row + 2 * lane));
-                if (live && ok[2]) qb = __ldg(reinterpret_cast<const float4 *>(row + 64 + 2 * lane));
+                const float4 qa = *reinterpret_cast<const float4 *>(row + offA);
+                const float4 qb = *reinterpret_cast<const float4 *>(row + offB);
                 ahi[i][0] = qa.x; alo[i][0] = qa.y; ahi[i][1] = qa.z; alo[i][1] = qa.w;
                 ahi[i][2] = qb.x; alo[i][2] = qb.y; ahi[i][3] = qb.z; alo[i][3] = qb.w;
             }
         }
         if (opN) {
-            float sh[8], sl[8];
+            float sh[RW], sl[RW];
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
+            for (int i = 0; i < RW; i++) {
                 sh[i] = 0.f; sl[i] = 0.f;
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    if (FMT == FMT_F32) cacc1(sh[i], sl[i], ahi[i][k], xh[k], xl[k]);
-                    else cacc(sh[i], sl[i], ahi[i][k], alo[i][k], xh[k], xl[k]);
+                for (int c = 0; c < 4; c++) {
+                    if (FMT == FMT_F32) cacc1(sh[i], sl[i], ahi[i][c], xh[c], xl[c]);
+                    else cacc(sh[i], sl[i], ahi[i][c], alo[i][c], xh[c], xl[c]);
                 }
             }
-            const double val = reduce8_df(sh, sl, lane);
-            const int row = r0 + halving_row(lane);
-            if ((lane & 3) == 0 && row < nr) atomicAdd(out0 + row, val);
+            float vh, vl;
+            reduceR_df<RW>(sh, sl, lane, vh, vl);
+            const int row = r0 + halving_row_R<RW>(lane);
+            if (halving_owner<RW>(lane) && row < nr) atomicAdd(out0 + row, (double)vh + (double)vl);
         }
         if (opT) {
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
+            for (int i = 0; i < RW; i++) {
                 const int r = min(r0 + i, kChunkRows - 1);
                 const float x1h = sx1h[r], x1l = sx1l[r];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    if (FMT == FMT_F32) cacc1(ch[k], cl[k], ahi[i][k], x1h, x1l);
-                    else cacc(ch[k], cl[k], ahi[i][k], alo[i][k], x1h, x1l);
+                for (int c = 0; c < 4; c++) {
+                    if (FMT == FMT_F32) cacc1(ch[c], cl[c], ahi[i][c], x1h, x1l);
+                    else cacc(ch[c], cl[c], ahi[i][c], alo[i][c], x1h, x1l);
                 }
             }
         }
@@ -326,9 +497,9 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
         float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw);
         float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw + 8 * kTileCols * 4);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            rh[warp][lane_col<FMT>(lane, k)] = ch[k];
-            rl[warp][lane_col<FMT>(lane, k)] = cl[k];
+        for (int c = 0; c < 4; c++) {
+            rh[warp][lane_col<FMT>(lane, c)] = ch[c];
+            rl[warp][lane_col<FMT>(lane, c)] = cl[c];
         }
         __syncthreads();
         double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
@@ -721,6 +892,9 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaMalloc(&d->con_map, std::max<size_t>(con.size(), 1) * sizeof(int)));
     CUDA_TRY(cudaMemcpy(d->con_map, con.data(), con.size() * sizeof(int), cudaMemcpyHostToDevice));
 
+    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
     CUDA_TRY(cudaStreamCreateWithFlags(&d->s_main, cudaStreamNonBlocking));
     CUDA_TRY(cudaStreamCreateWithFlags(&d->s_aux, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming));
@@ -791,11 +965,11 @@ static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int
     if (r.count == 0) return;
     dim3 grid(r.count, nvec);
     if (d->precision == H2ERI_GPU_FP64)
-        k_tile<FMT_F64><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena, va);
+        k_tile<FMT_F64><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena, va);
     else if (r.pair)
-        k_tile<FMT_F32X2><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena32x2, va);
+        k_tile<FMT_F32X2><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena32x2, va);
     else
-        k_tile<FMT_F32><<<grid, kTileThreads, 0, s>>>(d->tiles + r.first, d->arena32, va);
+        k_tile<FMT_F32><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena32, va);
 }
 
 /* Fill the mixed arenas from the host blocks (first use of mixed mode). */
