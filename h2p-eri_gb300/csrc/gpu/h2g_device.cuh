@@ -109,7 +109,7 @@ struct DevRep {
     double *dbuf = nullptr, *jbuf = nullptr;   /* density / J staging, nden_cap matrices */
     int nden_cap = 0;
     cudaStream_t s_main = nullptr, s_aux = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_zero = nullptr, ev_done = nullptr;
     cudaEvent_t ev_t[8] = {nullptr};
     float last_ms[5] = {0, 0, 0, 0, 0};   /* fwd, mid, bwd, den, total */
     int precision = 0;

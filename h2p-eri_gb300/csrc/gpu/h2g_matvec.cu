@@ -231,7 +231,7 @@ template <int R>
 __device__ __forceinline__ double reduceR_f64(double *s, int lane)
 {
     const bool b16 = lane & 16, b8 = lane & 8;
-    if (R == 8) {
+    if constexpr (R == 8) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             double send = b16 ? s[k] : s[k + 4];
@@ -250,26 +250,27 @@ __device__ __forceinline__ double reduceR_f64(double *s, int lane)
         val += __shfl_xor_sync(0xffffffffu, val, 2);
         val += __shfl_xor_sync(0xffffffffu, val, 1);
         return val;
-    }
+    } else {
 #pragma unroll
-    for (int k = 0; k < 2; k++) {
-        double send = b16 ? s[k] : s[k + 2];
-        double keep = b16 ? s[k + 2] : s[k];
-        s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        for (int k = 0; k < 2; k++) {
+            double send = b16 ? s[k] : s[k + 2];
+            double keep = b16 ? s[k + 2] : s[k];
+            s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+        double send = b8 ? s[0] : s[1];
+        double val = (b8 ? s[1] : s[0]) + __shfl_xor_sync(0xffffffffu, send, 8);
+        val += __shfl_xor_sync(0xffffffffu, val, 4);
+        val += __shfl_xor_sync(0xffffffffu, val, 2);
+        val += __shfl_xor_sync(0xffffffffu, val, 1);
+        return val;
     }
-    double send = b8 ? s[0] : s[1];
-    double val = (b8 ? s[1] : s[0]) + __shfl_xor_sync(0xffffffffu, send, 8);
-    val += __shfl_xor_sync(0xffffffffu, val, 4);
-    val += __shfl_xor_sync(0xffffffffu, val, 2);
-    val += __shfl_xor_sync(0xffffffffu, val, 1);
-    return val;
 }
 
 template <int R>
 __device__ __forceinline__ void reduceR_df(float *h, float *l, int lane, float &vh, float &vl)
 {
     const bool b16 = lane & 16, b8 = lane & 8;
-    if (R == 8) {
+    if constexpr (R == 8) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             float sh = b16 ? h[k] : h[k + 4], sl = b16 ? l[k] : l[k + 4];
@@ -688,6 +689,8 @@ static void free_rep(DevRep *d)
     if (d->s_aux) cudaStreamDestroy(d->s_aux);
     if (d->ev_fork) cudaEventDestroy(d->ev_fork);
     if (d->ev_join) cudaEventDestroy(d->ev_join);
+    if (d->ev_zero) cudaEventDestroy(d->ev_zero);
+    if (d->ev_done) cudaEventDestroy(d->ev_done);
     for (auto &e : d->ev_t)
         if (e) cudaEventDestroy(e);
     free_exchange_state(d);
@@ -895,10 +898,18 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
-    CUDA_TRY(cudaStreamCreateWithFlags(&d->s_main, cudaStreamNonBlocking));
-    CUDA_TRY(cudaStreamCreateWithFlags(&d->s_aux, cudaStreamNonBlocking));
+    /* The tree sweeps are a chain of dependent launches (the critical path);
+     * the near field is one large independent batch. Giving the chain's
+     * stream the higher priority lets near-field tiles fill only the SMs the
+     * chain leaves idle. */
+    int prio_lo = 0, prio_hi = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    CUDA_TRY(cudaStreamCreateWithPriority(&d->s_main, cudaStreamNonBlocking, prio_hi));
+    CUDA_TRY(cudaStreamCreateWithPriority(&d->s_aux, cudaStreamNonBlocking, prio_lo));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&d->ev_zero, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&d->ev_done, cudaEventDisableTiming));
     for (auto &e : d->ev_t) CUDA_TRY(cudaEventCreate(&e));
 
     d->krnl = krnl;
@@ -1031,24 +1042,31 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     va.stride[VK_Y1] = d->rank_total;
     va.base[VK_T] = d->work + 2 * per_r;
     va.stride[VK_T] = d->lr_total;
-    CUDA_TRY(cudaMemsetAsync(d->work, 0, (2 * per_r + per_t) * sizeof(double), s));
-    CUDA_TRY(cudaMemsetAsync(y, 0, (size_t)d->krnl * nvec * sizeof(double), s));
+    /* fork from the caller's stream onto the library's streams: the tree
+     * chain on the high-priority stream, the near field on the other */
+    cudaStream_t sm = d->s_main, sa = d->s_aux;
     CUDA_TRY(cudaEventRecord(d->ev_fork, s));
-    CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_fork, 0));
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], d->s_aux));
-    for (const Range &r : d->den) launch_range(d, r, va, nvec, d->s_aux);
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[7], d->s_aux));
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], s));
-    for (const Range &r : d->fwd) launch_range(d, r, va, nvec, s);
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[1], s));
-    launch_range(d, d->mid1, va, nvec, s);
-    launch_range(d, d->mid2, va, nvec, s);
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[2], s));
-    for (const Range &r : d->bwd) launch_range(d, r, va, nvec, s);
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[3], s));
-    CUDA_TRY(cudaEventRecord(d->ev_join, d->s_aux));
-    CUDA_TRY(cudaStreamWaitEvent(s, d->ev_join, 0));
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[4], s));
+    CUDA_TRY(cudaStreamWaitEvent(sm, d->ev_fork, 0));
+    CUDA_TRY(cudaMemsetAsync(d->work, 0, (2 * per_r + per_t) * sizeof(double), sm));
+    CUDA_TRY(cudaMemsetAsync(y, 0, (size_t)d->krnl * nvec * sizeof(double), sm));
+    CUDA_TRY(cudaEventRecord(d->ev_zero, sm));
+    CUDA_TRY(cudaStreamWaitEvent(sa, d->ev_zero, 0));
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], sa));
+    for (const Range &r : d->den) launch_range(d, r, va, nvec, sa);
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[7], sa));
+    CUDA_TRY(cudaEventRecord(d->ev_join, sa));
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], sm));
+    for (const Range &r : d->fwd) launch_range(d, r, va, nvec, sm);
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[1], sm));
+    launch_range(d, d->mid1, va, nvec, sm);
+    launch_range(d, d->mid2, va, nvec, sm);
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[2], sm));
+    for (const Range &r : d->bwd) launch_range(d, r, va, nvec, sm);
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[3], sm));
+    CUDA_TRY(cudaStreamWaitEvent(sm, d->ev_join, 0));
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[4], sm));
+    CUDA_TRY(cudaEventRecord(d->ev_done, sm));
+    CUDA_TRY(cudaStreamWaitEvent(s, d->ev_done, 0));
     CUDA_TRY(cudaGetLastError());
     return 0;
 }
