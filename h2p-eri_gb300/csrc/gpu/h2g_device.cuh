@@ -53,10 +53,11 @@ enum MatFmt : int {
 /* One matrix to copy into the mixed arenas when mixed mode is first used. */
 struct PackItem {
     const double *src;
-    int nrow, ncol, lds;
+    int nrow, ncol, lds;  /* source matrix (row-major) */
+    int trans;            /* 1: store the ncol x nrow transpose */
     int fmt;              /* FMT_F32 or FMT_F32X2 */
     size_t off;           /* element offset in the float (F32) or float2 (F32X2) arena */
-    int ld;
+    int ld;               /* leading dimension of the stored matrix */
 };
 
 constexpr int kTileRows = 64;      /* rows per sub-tile (8 warps x 8 rows)    */
@@ -94,8 +95,8 @@ struct DevRep {
     int n_tiles = 0;
     std::vector<Range> fwd;     /* deepest level first */
     std::vector<Range> bwd;     /* shallowest level first */
-    Range mid1, mid2;
-    std::vector<Range> den;     /* near field: stage-1 ranges, then stage-2 ranges */
+    std::vector<Range> mid;     /* coupling blocks, stages 1..3 */
+    std::vector<Range> den;     /* near field, stages 1..3 (diagonal-pair, then single-float range per stage) */
     int rank_total = 0, lr_total = 0;
     /* algorithmic bytes / flops of one matvec (per vector), for reports */
     double alg_bytes_matrix = 0.0, alg_bytes_vec = 0.0, alg_flops = 0.0;

@@ -560,31 +560,39 @@ struct MatLoc {
 };
 
 /* Packs matrices into the FP64 arena now and records where each goes in the
- * mixed arenas (filled on first use of mixed mode). Leading dimensions are
- * padded to 16-byte multiples and every matrix starts 32-byte aligned, so
- * rows can be read with 16-byte vector loads; padding is zero. */
+ * mixed arenas (filled on first use of mixed mode). With trans set the
+ * ncol x nrow transpose is stored: tall, narrow matrices (nested bases,
+ * low-rank factors, ranks ~50-450) become wide ones that fill 128-column
+ * tile strips. Leading dimensions are padded to 16-byte multiples and every
+ * matrix starts 32-byte aligned, so rows can be read with 16-byte vector
+ * loads; padding is zero. */
 struct Packer {
     std::vector<double> host;
     size_t n32 = 0, n32x2 = 0;
     std::vector<PackItem> items;
-    MatLoc put(const double *src, int nrow, int ncol, int lds, int mixed_fmt)
+    MatLoc put(const double *src, int nrow, int ncol, int lds, int mixed_fmt, bool trans = false)
     {
+        const int sr = trans ? ncol : nrow, sc = trans ? nrow : ncol;   /* stored shape */
         MatLoc m;
-        m.ld = (ncol + 1) & ~1;
+        m.ld = (sc + 1) & ~1;
         m.a = (host.size() + 3) & ~size_t(3);
-        host.resize(m.a + (size_t)nrow * m.ld, 0.0);
+        host.resize(m.a + (size_t)sr * m.ld, 0.0);
         for (int r = 0; r < nrow; r++)
-            std::memcpy(host.data() + m.a + (size_t)r * m.ld, src + (size_t)r * lds, sizeof(double) * ncol);
+            for (int c = 0; c < ncol; c++) {
+                const double x = src[(size_t)r * lds + c];
+                if (trans) host[m.a + (size_t)c * m.ld + r] = x;
+                else host[m.a + (size_t)r * m.ld + c] = x;
+            }
         if (mixed_fmt == FMT_F32) {
-            m.ld2 = (ncol + 3) & ~3;
+            m.ld2 = (sc + 3) & ~3;
             m.a2 = (n32 + 7) & ~size_t(7);
-            n32 = m.a2 + (size_t)nrow * m.ld2;
+            n32 = m.a2 + (size_t)sr * m.ld2;
         } else {
-            m.ld2 = (ncol + 1) & ~1;
+            m.ld2 = (sc + 1) & ~1;
             m.a2 = (n32x2 + 3) & ~size_t(3);
-            n32x2 = m.a2 + (size_t)nrow * m.ld2;
+            n32x2 = m.a2 + (size_t)sr * m.ld2;
         }
-        items.push_back(PackItem{src, nrow, ncol, lds, mixed_fmt, m.a2, m.ld2});
+        items.push_back(PackItem{src, nrow, ncol, lds, trans ? 1 : 0, mixed_fmt, m.a2, m.ld2});
         return m;
     }
 };
@@ -611,12 +619,13 @@ struct Planner {
     }
 };
 
-/* A stored B/D block, dense or low-rank. */
+/* A stored B/D block: dense, or low-rank U V with U stored transposed
+ * (Ut, rank x nrow) and V stored as is (rank x ncol), both wide. */
 struct BlockLoc {
     bool lowrank = false;
     int nrow = 0, ncol = 0, rank = 0;
-    MatLoc a, u, vt;               /* dense data, or U and V^T factors */
-    int t_off = 0, s_off = 0;      /* scratch for V x_in0 and U^T x_in1 */
+    MatLoc a, ut, v;
+    int t_off = 0, s_off = 0;      /* scratch for t = V in0 and s = U^T in1 */
 };
 
 BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total, int fmt)
@@ -627,8 +636,8 @@ BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total, int fmt)
     if (m->ld < 0) {
         b.lowrank = true;
         b.rank = -m->ld;
-        b.u = pk.put(m->data, b.nrow, b.rank, b.rank, fmt);
-        b.vt = pk.put(m->data + (size_t)b.nrow * b.rank, b.ncol, b.rank, b.rank, fmt);
+        b.ut = pk.put(m->data, b.nrow, b.rank, b.rank, fmt, true);
+        b.v = pk.put(m->data + (size_t)b.nrow * b.rank, b.ncol, b.rank, b.rank, fmt, true);
         b.t_off = lr_total;
         b.s_off = lr_total + b.rank;
         lr_total += 2 * b.rank;
@@ -639,31 +648,37 @@ BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total, int fmt)
 }
 
 /* Products of one block: N-side (out0 += A in0) and T-side (out1 += A^T in1);
- * kinds VK_NONE disable a side. Low-rank blocks use two stages. */
-void plan_block(Planner &stage1, Planner &stage2, const BlockLoc &b, uint8_t kin0, int in0, uint8_t kout0,
-                int out0, uint8_t kin1, int in1, uint8_t kout1, int out1)
+ * kinds VK_NONE disable a side. Dense blocks are one bi-product pass. A
+ * low-rank block A = U V takes three stages:
+ *   1. t = V in0                    (N on V)
+ *   2. s = U^T in1, out0 += U t     (one pass over Ut: N and T)
+ *   3. out1 += V^T s                (T on V)
+ * so U is read once and V twice (once when only the N side is wanted).
+ * Returns the number of stored elements read. */
+double plan_block(Planner *st, const BlockLoc &b, uint8_t kin0, int in0, uint8_t kout0, int out0, uint8_t kin1,
+                  int in1, uint8_t kout1, int out1)
 {
-    if (b.nrow == 0 || b.ncol == 0) return;
+    if (b.nrow == 0 || b.ncol == 0) return 0.0;
     if (!b.lowrank) {
-        stage1.add(b.a, b.nrow, b.ncol, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
-        return;
+        st[0].add(b.a, b.nrow, b.ncol, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
+        return (double)b.nrow * b.ncol;
     }
-    if (b.rank == 0) return;
-    if (kout0 != VK_NONE) {
-        /* t = V in0 = (V^T)^T in0 ; out0 += U t */
-        stage1.add(b.vt, b.ncol, b.rank, VK_NONE, 0, VK_NONE, 0, kin0, in0, VK_T, b.t_off);
-        stage2.add(b.u, b.nrow, b.rank, VK_T, b.t_off, kout0, out0, VK_NONE, 0, VK_NONE, 0);
+    const int r = b.rank;
+    if (r == 0) return 0.0;
+    double elems = 0.0;
+    const bool wantN = kout0 != VK_NONE, wantT = kout1 != VK_NONE;
+    if (wantN) {
+        st[0].add(b.v, r, b.ncol, kin0, in0, VK_T, b.t_off, VK_NONE, 0, VK_NONE, 0);
+        elems += (double)r * b.ncol;
     }
-    if (kout1 != VK_NONE) {
-        /* s = U^T in1 ; out1 += V^T s */
-        stage1.add(b.u, b.nrow, b.rank, VK_NONE, 0, VK_NONE, 0, kin1, in1, VK_T, b.s_off);
-        stage2.add(b.vt, b.ncol, b.rank, VK_T, b.s_off, kout1, out1, VK_NONE, 0, VK_NONE, 0);
+    st[1].add(b.ut, r, b.nrow, wantT ? kin1 : VK_NONE, in1, wantT ? VK_T : VK_NONE, b.s_off,
+              wantN ? VK_T : VK_NONE, b.t_off, wantN ? kout0 : VK_NONE, out0);
+    elems += (double)r * b.nrow;
+    if (wantT) {
+        st[2].add(b.v, r, b.ncol, VK_NONE, 0, VK_NONE, 0, VK_T, b.s_off, kout1, out1);
+        elems += (double)r * b.ncol;
     }
-}
-
-double block_elems(const BlockLoc &b)
-{
-    return b.lowrank ? (double)(b.nrow + b.ncol) * b.rank : (double)b.nrow * b.ncol;
+    return elems;
 }
 
 }  // namespace
@@ -743,7 +758,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
             need_down[node] = wrote_y1[node] || (pin && need_down[p] && rank[p] > 0);
         }
 
-    Planner mid1, mid2, den1d, den2d, den1o, den2o;
+    Planner midst[3], dend[3], deno[3];
     std::vector<Tile> all;
     double mat_bytes = 0.0, mat_bytes_mixed = 0.0, vec_bytes = 0.0, flops = 0.0;
     d->fwd.clear();
@@ -753,7 +768,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
     std::vector<MatLoc> uloc(n_node);
     for (int i = 0; i < n_node; i++) {
         H2E_dense_mat_p U = h->U[i];
-        if (U->nrow > 0 && U->ncol > 0) uloc[i] = pk.put(U->data, U->nrow, U->ncol, U->ld, FMT_F32X2);
+        /* stored transposed (rank x rows): wide, fills the 128-column strips */
+        if (U->nrow > 0 && U->ncol > 0) uloc[i] = pk.put(U->data, U->nrow, U->ncol, U->ld, FMT_F32X2, true);
     }
     d->bytes_U = pk.host.size() * sizeof(double);
 
@@ -766,8 +782,9 @@ static int build_rep(H2ERI_p h, DevRep *d)
             if (!need_up[node] || U->nrow == 0 || U->ncol == 0) continue;
             bool leaf = h->n_child[node] == 0;
             int in_off = leaf ? h->mat_cluster[2 * node] : voff[h->children[node * h->max_child]];
-            p.add(uloc[node], U->nrow, U->ncol, VK_NONE, 0, VK_NONE, 0, leaf ? VK_X : VK_Y0, in_off,
-                  VK_Y0, voff[node]);
+            /* y0 = U^T in = Ut in: N side of the stored transpose */
+            p.add(uloc[node], U->ncol, U->nrow, leaf ? VK_X : VK_Y0, in_off, VK_Y0, voff[node], VK_NONE, 0,
+                  VK_NONE, 0);
             mat_bytes += 8.0 * U->nrow * U->ncol;
             mat_bytes_mixed += 8.0 * U->nrow * U->ncol;
             vec_bytes += 8.0 * (U->nrow + U->ncol);
@@ -796,17 +813,18 @@ static int build_rep(H2ERI_p h, DevRep *d)
             kin0 = VK_Y0; in0 = voff[n1]; kout0 = VK_Y; out0 = h->mat_cluster[2 * n0];
             kin1 = VK_X; in1 = h->mat_cluster[2 * n0]; kout1 = VK_Y1; out1 = voff[n1];
         }
-        plan_block(mid1, mid2, b, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
-        mat_bytes += 8.0 * block_elems(b);
-        mat_bytes_mixed += 4.0 * block_elems(b);
+        double el = plan_block(midst, b, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
+        mat_bytes += 8.0 * el;
+        mat_bytes_mixed += 4.0 * el;
         vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
-        flops += 4.0 * block_elems(b);
+        flops += 2.0 * el + 2.0 * (b.lowrank ? 0.0 : el);
     }
     d->bytes_B = (pk.host.size() - b_start) * sizeof(double);
-    d->mid1 = {(int)all.size(), (int)mid1.tiles.size()};
-    all.insert(all.end(), mid1.tiles.begin(), mid1.tiles.end());
-    d->mid2 = {(int)all.size(), (int)mid2.tiles.size()};
-    all.insert(all.end(), mid2.tiles.begin(), mid2.tiles.end());
+    d->mid.clear();
+    for (int k = 0; k < 3; k++) {
+        d->mid.push_back(Range{(int)all.size(), (int)midst[k].tiles.size(), false});
+        all.insert(all.end(), midst[k].tiles.begin(), midst[k].tiles.end());
+    }
 
     /* downward sweep, shallowest level first (src/H2ERI_matvec.c:679-738) */
     for (int lv = h->min_adm_level; lv <= h->max_level; lv++) {
@@ -817,8 +835,9 @@ static int build_rep(H2ERI_p h, DevRep *d)
             if (!need_down[node] || U->nrow == 0 || U->ncol == 0) continue;
             bool leaf = h->n_child[node] == 0;
             int out_off = leaf ? h->mat_cluster[2 * node] : voff[h->children[node * h->max_child]];
-            p.add(uloc[node], U->nrow, U->ncol, VK_Y1, voff[node], leaf ? VK_Y : VK_Y1, out_off, VK_NONE,
-                  0, VK_NONE, 0);
+            /* out += U y1 = Ut^T y1: T side of the stored transpose */
+            p.add(uloc[node], U->ncol, U->nrow, VK_NONE, 0, VK_NONE, 0, VK_Y1, voff[node], leaf ? VK_Y : VK_Y1,
+                  out_off);
             mat_bytes += 8.0 * U->nrow * U->ncol;
             mat_bytes_mixed += 8.0 * U->nrow * U->ncol;
             vec_bytes += 8.0 * (U->nrow + U->ncol);
@@ -835,30 +854,32 @@ static int build_rep(H2ERI_p h, DevRep *d)
         /* mixed mode keeps the leaf self-interaction blocks as float pairs */
         const bool diag = i < h->n_leaf_node;
         BlockLoc b = pack_block(pk, h->c_D_blks[i], d->lr_total, diag ? FMT_F32X2 : FMT_F32);
+        double el = 0.0;
         if (diag) {
             int node = h->height_nodes[i];
             int off = h->mat_cluster[2 * node];
-            plan_block(den1d, den2d, b, VK_X, off, VK_Y, off, VK_NONE, 0, VK_NONE, 0);
+            el = plan_block(dend, b, VK_X, off, VK_Y, off, VK_NONE, 0, VK_NONE, 0);
             vec_bytes += 8.0 * (b.nrow + b.ncol);
-            flops += 2.0 * block_elems(b);
+            flops += 2.0 * el;
         } else {
             int k = i - h->n_leaf_node;
             int n0 = h->r_inadm_pairs[2 * k], n1 = h->r_inadm_pairs[2 * k + 1];
             int o0 = h->mat_cluster[2 * n0], o1 = h->mat_cluster[2 * n1];
-            plan_block(den1o, den2o, b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
+            el = plan_block(deno, b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
             vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
-            flops += 4.0 * block_elems(b);
+            flops += 2.0 * el + 2.0 * (b.lowrank ? 0.0 : el);
         }
-        mat_bytes += 8.0 * block_elems(b);
-        mat_bytes_mixed += (diag ? 8.0 : 4.0) * block_elems(b);
+        mat_bytes += 8.0 * el;
+        mat_bytes_mixed += (diag ? 8.0 : 4.0) * el;
     }
     d->bytes_D = (pk.host.size() - d_start) * sizeof(double);
     d->den.clear();
-    for (Planner *p : {&den1d, &den1o, &den2d, &den2o}) {
-        bool pair = (p == &den1d || p == &den2d);
-        d->den.push_back(Range{(int)all.size(), (int)p->tiles.size(), pair});
-        all.insert(all.end(), p->tiles.begin(), p->tiles.end());
-    }
+    for (int k = 0; k < 3; k++)
+        for (int pair = 1; pair >= 0; pair--) {
+            Planner &p = pair ? dend[k] : deno[k];
+            d->den.push_back(Range{(int)all.size(), (int)p.tiles.size(), pair == 1});
+            all.insert(all.end(), p.tiles.begin(), p.tiles.end());
+        }
 
     d->alg_bytes_matrix = mat_bytes;
     d->alg_bytes_matrix_mixed = mat_bytes_mixed;
@@ -992,14 +1013,14 @@ static int pack_mixed(DevRep *d)
     for (const PackItem &it : d->mixed_items) {
         for (int r = 0; r < it.nrow; r++) {
             const double *src = it.src + (size_t)r * it.lds;
-            if (it.fmt == FMT_F32) {
-                float *dst = h32.data() + it.off + (size_t)r * it.ld;
-                for (int c = 0; c < it.ncol; c++) dst[c] = (float)src[c];
-            } else {
-                float2 *dst = h32x2.data() + it.off + (size_t)r * it.ld;
-                for (int c = 0; c < it.ncol; c++) {
-                    float hi = (float)src[c];
-                    dst[c] = make_float2(hi, (float)(src[c] - (double)hi));
+            for (int c = 0; c < it.ncol; c++) {
+                /* position of source element (r, c) in the stored matrix */
+                const size_t pos = it.off + (it.trans ? (size_t)c * it.ld + r : (size_t)r * it.ld + c);
+                if (it.fmt == FMT_F32) {
+                    h32[pos] = (float)src[c];
+                } else {
+                    const float hi = (float)src[c];
+                    h32x2[pos] = make_float2(hi, (float)(src[c] - (double)hi));
                 }
             }
         }
@@ -1058,8 +1079,7 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], sm));
     for (const Range &r : d->fwd) launch_range(d, r, va, nvec, sm);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[1], sm));
-    launch_range(d, d->mid1, va, nvec, sm);
-    launch_range(d, d->mid2, va, nvec, sm);
+    for (const Range &r : d->mid) launch_range(d, r, va, nvec, sm);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[2], sm));
     for (const Range &r : d->bwd) launch_range(d, r, va, nvec, sm);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[3], sm));
@@ -1238,7 +1258,7 @@ extern "C" int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n)
     for (const Range &r : d->fwd) launches += r.count > 0;
     for (const Range &r : d->bwd) launches += r.count > 0;
     for (const Range &r : d->den) launches += r.count > 0;
-    launches += (d->mid1.count > 0) + (d->mid2.count > 0);
+    for (const Range &r : d->mid) launches += r.count > 0;
     double mbytes = d->precision == H2ERI_GPU_MIXED ? d->alg_bytes_matrix_mixed : d->alg_bytes_matrix;
     double vals[13] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
                        (double)d->bytes_U, (double)d->bytes_B, (double)d->bytes_D,
