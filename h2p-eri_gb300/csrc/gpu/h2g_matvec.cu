@@ -1283,3 +1283,123 @@ extern "C" void h2g_gpu_print_statistic(H2ERI_p h2eri)
         std::printf("  * Last matvec (ms) fwd/mid/bwd/dense/total : %.4f %.4f %.4f %.4f %.4f\n", d->last_ms[0],
                     d->last_ms[1], d->last_ms[2], d->last_ms[3], d->last_ms[4]);
 }
+
+/* ======================================================================== */
+/* Matvec without allocation                                                 */
+/* ======================================================================== */
+
+namespace h2g {
+
+/* Scratch of H2ERI_matvec_device_noalloc: the upward and downward
+ * coefficients and the low-rank intermediates of one vector
+ * (2 * rank_total + lr_total doubles; about 0.33 M for C30H62 at QR tol
+ * 1e-8). 16 MiB, held by every GPU that loads this library until the process
+ * exits. Every call uses the same array, and each call clears it before use,
+ * so calls whose GPU work overlaps (different streams, or several structures
+ * at once) race on it. */
+constexpr size_t kNoAllocScratchDoubles = (size_t)1 << 21;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+static std::mutex g_noalloc_mu;
+static std::unordered_map<int, double *> g_noalloc_addr;   /* device -> address of the array */
+
+/* Device address of the scratch array on the current device. The host-side
+ * name g_noalloc_scratch is only a stand-in and must never be passed to a
+ * kernel; the address is looked up once per device, with that device
+ * current, and cached. */
+static int noalloc_scratch(int dev, double **out)
+{
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    auto it = g_noalloc_addr.find(dev);
+    if (it != g_noalloc_addr.end()) {
+        *out = it->second;
+        return 0;
+    }
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        return 10;
+    }
+    g_noalloc_addr[dev] = static_cast<double *>(p);
+    *out = static_cast<double *>(p);
+    return 0;
+}
+
+}  // namespace h2g
+
+/* y = A x for one vector on device arrays, without allocating device memory:
+ * the representation must already be on the GPU (H2ERI_gpu_upload, or any
+ * earlier hot-path call) and the intermediates use the library's fixed
+ * scratch array. For callers that must not allocate after set-up: a host
+ * application that hands the library a fixed device-memory budget, or one
+ * whose memory pool is owned elsewhere, and latency-critical loops where
+ * cudaMalloc/cudaFree would synchronise the device. The first call on a
+ * device looks up the scratch array's address (see noalloc_scratch); make
+ * that first call before any stream capture. */
+extern "C" int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, void *stream)
+{
+    if (h2eri == nullptr) { set_error("null H2ERI handle"); return 1; }
+    DevRep *d = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_reps.find(h2eri);
+        if (it == g_reps.end()) {
+            set_error("H2ERI_matvec_device_noalloc: no device copy of this structure; call H2ERI_gpu_upload first");
+            return 2;
+        }
+        d = it->second;
+        if (d->krnl != h2eri->krnl_mat_size || d->n_node != h2eri->n_node || d->fp_U != h2eri->U ||
+            d->fp_B != h2eri->c_B_blks || d->fp_D != h2eri->c_D_blks) {
+            set_error("H2ERI_matvec_device_noalloc: the structure changed since upload; call H2ERI_gpu_upload");
+            return 2;
+        }
+    }
+    const size_t need = (size_t)2 * d->rank_total + d->lr_total;
+    if (need > kNoAllocScratchDoubles) {
+        set_error("H2ERI_matvec_device_noalloc: needs " + std::to_string(need) + " doubles of scratch, limit " +
+                  std::to_string(kNoAllocScratchDoubles));
+        return 4;
+    }
+    int dev = -1;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev != d->device) {
+        set_error("H2ERI_matvec_device_noalloc: current device differs from the device holding the structure");
+        return 5;
+    }
+    double *work = nullptr;
+    int rc = noalloc_scratch(dev, &work);
+    if (rc) return rc;
+
+    const size_t per_r = (size_t)d->rank_total;
+    VecArgs va;
+    std::memset(&va, 0, sizeof(va));
+    va.base[VK_X] = const_cast<double *>(d_x);
+    va.stride[VK_X] = d->krnl;
+    va.base[VK_Y] = d_y;
+    va.stride[VK_Y] = d->krnl;
+    va.base[VK_Y0] = work;
+    va.stride[VK_Y0] = d->rank_total;
+    va.base[VK_Y1] = work + per_r;
+    va.stride[VK_Y1] = d->rank_total;
+    va.base[VK_T] = work + 2 * per_r;
+    va.stride[VK_T] = d->lr_total;
+    cudaStream_t s = stream ? (cudaStream_t)stream : d->s_main;
+    cudaStream_t sm = d->s_main, sa = d->s_aux;
+    CUDA_TRY(cudaEventRecord(d->ev_fork, s));
+    CUDA_TRY(cudaStreamWaitEvent(sm, d->ev_fork, 0));
+    CUDA_TRY(cudaMemsetAsync(work, 0, need * sizeof(double), sm));      /* scratch keeps the last call's values */
+    CUDA_TRY(cudaMemsetAsync(d_y, 0, (size_t)d->krnl * sizeof(double), sm));
+    CUDA_TRY(cudaEventRecord(d->ev_zero, sm));
+    CUDA_TRY(cudaStreamWaitEvent(sa, d->ev_zero, 0));
+    for (const Range &r : d->den) launch_range(d, r, va, 1, sa);
+    CUDA_TRY(cudaEventRecord(d->ev_join, sa));
+    for (const Range &r : d->fwd) launch_range(d, r, va, 1, sm);
+    for (const Range &r : d->mid) launch_range(d, r, va, 1, sm);
+    for (const Range &r : d->bwd) launch_range(d, r, va, 1, sm);
+    CUDA_TRY(cudaStreamWaitEvent(sm, d->ev_join, 0));
+    CUDA_TRY(cudaEventRecord(d->ev_done, sm));
+    CUDA_TRY(cudaStreamWaitEvent(s, d->ev_done, 0));
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}

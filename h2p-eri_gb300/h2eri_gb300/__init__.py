@@ -90,6 +90,7 @@ SIGNATURES = {
     "H2ERI_build_Coulomb_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     "H2ERI_build_exchange_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "H2ERI_gpu_report": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    "H2ERI_matvec_device_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "H2ERI_save_representation": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "H2ERI_load_representation": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
 }

@@ -93,6 +93,19 @@ int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double *d_den, do
 /* K on device arrays, enqueued on a stream. Returns 0 on success. */
 int H2ERI_build_exchange_device(H2ERI_p h2eri, const double *d_den, double *d_K, void *stream);
 
+/* y = A x for one vector on device arrays, allocating no device memory.
+ * No counterpart in the reference. For callers that must not allocate after
+ * set-up (a fixed device-memory budget or a memory pool owned by the host
+ * application, or loops where cudaMalloc/cudaFree would synchronise the
+ * device). Requires the structure to be on the GPU already
+ * (H2ERI_gpu_upload). The intermediates live in one fixed 16 MiB device
+ * array shared by all calls; larger representations (2 * sum of ranks +
+ * low-rank intermediates > 2^21 doubles) are rejected with an error. Each
+ * call clears the array first; calls whose GPU work overlaps race on it. The
+ * first call on a device looks up the array's address and should come before
+ * any stream capture. Returns 0 on success. */
+int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, void *stream);
+
 /* Figures of the device copy, for reports. out[0] kernel launches per matvec
  * call (one vector block), out[1] algorithmic matrix bytes read per matvec,
  * out[2] algorithmic vector bytes per vector, out[3] flops per vector,
