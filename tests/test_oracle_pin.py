@@ -69,3 +69,28 @@ def test_oracle_linearity(alk26, oracle_lib):
     oracle_lib.oracle_matvec(alk26.handle, b.ctypes.data, yb.ctypes.data)
     oracle_lib.oracle_matvec(alk26.handle, ab.ctypes.data, yab.ctypes.data)
     assert relerr(yab, ya + c * yb) < 1e-13
+
+
+def test_oracle_K_equals_reference_on_reference_rep(oracle_lib):
+    """Exchange: oracle restatement vs the reference's own H2ERI_build_exchange
+    on the representation built by the reference's set-up."""
+    ref = ref_lib_or_skip()
+    rh = ref.oref_build(os.path.join(GOLDEN, "alk26_ccpvdz.mol").encode(), 1e-10, 1e-10, 1e-6, 0)
+    n = 210
+    D = np.fromfile(os.path.join(GOLDEN, "D_alk26_ccpvdz.bin")).reshape(n, n)
+    K_o = np.zeros_like(D)
+    K_r = np.zeros_like(D)
+    oracle_lib.oracle_build_exchange(rh, D.ctypes.data, K_o.ctypes.data)
+    ref.H2ERI_build_exchange(rh, D.ctypes.data, K_r.ctypes.data)
+    assert relerr(K_o, K_r) < 1e-13
+
+
+def test_oracle_K_matches_golden(alk26, oracle_lib):
+    """K of the reference test suite (tests/test_K_input_mat.c inputs), on the
+    native representation at QR tol 1e-6."""
+    n = alk26.num_bf
+    D = np.fromfile(os.path.join(GOLDEN, "D_alk26_ccpvdz.bin")).reshape(n, n)
+    Kg = np.fromfile(os.path.join(GOLDEN, "K_alk26_ccpvdz.bin")).reshape(n, n)
+    K = np.zeros_like(D)
+    oracle_lib.oracle_build_exchange(alk26.handle, D.ctypes.data, K.ctypes.data)
+    assert relerr(K, Kg) < 5e-6
