@@ -88,7 +88,11 @@ SIGNATURES = {
     "H2ERI_matvec_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     "H2ERI_build_Coulomb_multi": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
     "H2ERI_build_Coulomb_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
+    "H2ERI_build_exchange_multi": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
     "H2ERI_build_exchange_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "H2ERI_gpu_exchange_report": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    "H2ERI_exchange_plan_check": (ctypes.c_int, [_vp, ctypes.c_double, _vp, ctypes.c_int]),
+    "H2ERI_gpu_set_exchange_memory": (ctypes.c_int, [_vp, ctypes.c_double]),
     "H2ERI_gpu_report": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     "H2ERI_matvec_device_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "H2ERI_save_representation": (ctypes.c_int, [_vp, ctypes.c_char_p]),
@@ -225,12 +229,20 @@ class H2ERI:
         return J
 
     def build_exchange(self, D):
-        import torch
-        D = torch.as_tensor(_f64(D), device="cuda")
-        K = torch.empty_like(D)
-        _check(lib().H2ERI_build_exchange_device(self.handle, D.data_ptr(), K.data_ptr(), None), "build_exchange")
-        torch.cuda.synchronize()
-        return K.cpu().numpy()
+        D = _f64(D)
+        n_den = 1 if D.ndim == 2 else D.shape[0]
+        K = np.empty_like(D)
+        _check(lib().H2ERI_build_exchange_multi(self.handle, n_den, D.ctypes.data, K.ctypes.data), "build_exchange")
+        return K
+
+    def exchange_report(self):
+        """Exchange-plan figures (see H2ERI_gpu_exchange_report)."""
+        out = np.zeros(8)
+        n = lib().H2ERI_gpu_exchange_report(self.handle, out.ctypes.data, 8)
+        if n < 0:
+            _check(-n, "gpu_exchange_report")
+        keys = ["flops", "ms_last", "n_ranges", "work_bytes", "near_items", "launches"]
+        return dict(zip(keys, out[:n].tolist()))
 
     def report(self):
         """Device-copy figures (see H2ERI_gpu_report in include/h2eri_gb300.h)."""

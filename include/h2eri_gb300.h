@@ -90,8 +90,28 @@ int H2ERI_matvec_device(H2ERI_p h2eri, int nvec, const double *d_x, double *d_y,
 int H2ERI_build_Coulomb_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *J_mats);
 /* Same on device arrays, enqueued on a stream. */
 int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double *d_den, double *d_J, void *stream);
+/* K for n_den densities stored back to back ([n_den][num_bf][num_bf]) on the
+ * host, one after the other. Returns 0 on success. */
+int H2ERI_build_exchange_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *K_mats);
 /* K on device arrays, enqueued on a stream. Returns 0 on success. */
 int H2ERI_build_exchange_device(H2ERI_p h2eri, const double *d_den, double *d_K, void *stream);
+/* Figures of the exchange plan: out[0] flops per K build, out[1] device time
+ * of the last host-array K build (ms), out[2] number of n ranges the build is
+ * split into, out[3] bytes of the G/H work tensors, out[4] near-field work
+ * items, out[5] kernel launches per K build. Returns the number of values
+ * written (<= n), or < 0. */
+int H2ERI_gpu_exchange_report(H2ERI_p h2eri, double *out, int n);
+/* Cap the device memory of the exchange work tensors (bytes; 0 = 40 % of
+ * the free memory, at most 16 GB). K is then built in more ranges of the
+ * density's column index, with the same result. Returns 0 on success. */
+int H2ERI_gpu_set_exchange_memory(H2ERI_p h2eri, double bytes);
+/* Build the exchange plan on the host only (no device calls), sized as if
+ * device_bytes of device memory were free, and check that every access of
+ * every planned kernel stays inside its buffer. out[0] flops per K build,
+ * out[1] number of n ranges, out[2] bytes of the work tensors, out[3]
+ * near-field work items, out[4] GEMM tiles. Returns 0 if the plan is
+ * consistent. */
+int H2ERI_exchange_plan_check(H2ERI_p h2eri, double device_bytes, double *out, int n);
 
 /* y = A x for one vector on device arrays, allocating no device memory.
  * No counterpart in the reference. For callers that must not allocate after

@@ -5,6 +5,9 @@ import glob
 import os
 import re
 
+import numpy as np
+import pytest
+
 from conftest import REPO
 
 DECL = re.compile(r"^\s*(?:void|int|const char \*|double|size_t)\s+\*?\s*(\w+)\s*\(", re.M)
@@ -38,3 +41,14 @@ def test_library_loads_without_gpu_and_reports_errors(library):
     rc = library.H2ERI_gpu_upload(None)
     assert rc != 0
     assert library.H2ERI_gpu_last_error()
+
+
+@pytest.mark.parametrize("device_bytes", [100e9, 2e6])
+def test_exchange_plan_in_bounds(small_mols, alk26, library, device_bytes):
+    """The exchange plan (built on the host, no GPU) keeps every access of
+    every planned kernel inside its buffer, with one or many n ranges."""
+    for h in list(small_mols.values()) + [alk26]:
+        out = np.zeros(5)
+        rc = library.H2ERI_exchange_plan_check(h.handle, device_bytes, out.ctypes.data, 5)
+        assert rc == 0, library.H2ERI_gpu_last_error()
+        assert out[0] > 0 and out[1] >= 1 and out[4] > 0
