@@ -40,14 +40,17 @@ WORKLOADS = {
     # the headline configuration (fits one GPU)
     "c30": {"workload": "J build C30H62 cc-pVDZ (760 bf, cartesian), QR tol 1e-8, 1 density n_occ=121",
             "molecule": "C30H62", "n_carbon": 30, "qr_tol": 1e-8, "n_occ": 121, "seed": 2000,
-            "inputs_vs_L2": "H2 representation ~1.8 GB read per step > 129 MB L2 (no flush needed)"},
+            "inputs_vs_L2": "H2 representation ~1.8 GB read per step > 129 MB L2 (no flush needed)",
+            "k_cpu_stride": 16},
     # small case for profiler captures (the reference's CPU-runnable size)
     "c10": {"workload": "J build C10H22 cc-pVDZ (260 bf, cartesian), QR tol 1e-6, 1 density n_occ=41",
             "molecule": "C10H22", "n_carbon": 10, "qr_tol": 1e-6, "n_occ": 41, "seed": 1000,
-            "inputs_vs_L2": "H2 representation ~0.28 GB read per step > 129 MB L2"},
+            "inputs_vs_L2": "H2 representation ~0.28 GB read per step > 129 MB L2",
+            "k_cpu_stride": 2, "k_check_full": True},
 }
 WORKLOAD = dict(WORKLOADS["c30"])
 METRIC = "J builds/s C30H62 (mixed vs FP64) at relerr<=1e-8"
+METRIC_K = "K builds/s (H2ERI_build_exchange path)"
 CACHE_DIR = os.path.join(tempfile.gettempdir(), "h2eri_gb300_cache")
 
 
@@ -164,16 +167,35 @@ def cpu_baseline(orc, h, D, budget_s=12.0, max_builds=100000):
 def load_oracle():
     from oracle import build_oracle
     orc = ctypes.CDLL(build_oracle.build())
-    for f in ("oracle_matvec", "oracle_build_Coulomb"):
+    for f in ("oracle_matvec", "oracle_build_Coulomb", "oracle_build_exchange"):
         getattr(orc, f).argtypes = [ctypes.c_void_p] * 3
         getattr(orc, f).restype = None
+    orc.oracle_build_exchange_shells.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int]
+    orc.oracle_build_exchange_shells.restype = None
     return orc
+
+
+def exchange_cpu_sample(orc, h, D, stride, reps=1):
+    """Oracle restatement of H2ERI_build_exchange on the host cores, over every
+    stride-th outer shell N (the reference's outer loop); returns K builds/s
+    scaled by the sampled share of shells and a description."""
+    nsh = h.s.nshell
+    shells = np.arange(0, nsh, max(1, stride), dtype=np.int32)
+    K = np.zeros_like(D)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        orc.oracle_build_exchange_shells(h.handle, D.ctypes.data, K.ctypes.data, shells.ctypes.data, len(shells))
+    dt = (time.perf_counter() - t0) / reps
+    frac = len(shells) / nsh
+    return frac / dt, f"{len(shells)} of {nsh} outer shells N (every {stride}-th) in {dt:.1f} s, scaled by {frac:.4f}"
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    if args.path == "exchange":
+        return run_reference_exchange(args)
     import h2eri_gb300 as hg
     from h2eri_gb300 import build as hb, molecules
     hb.build()
@@ -200,7 +222,137 @@ def run_reference(args):
     h.destroy()
 
 
+def run_reference_exchange(args):
+    import h2eri_gb300 as hg
+    from h2eri_gb300 import build as hb, molecules
+    hb.build()
+    orc = load_oracle()
+    h, _ = representation(hg, molecules, 0, 1, lambda: None)
+    D = molecules.seeded_density(h.num_bf, WORKLOAD["n_occ"], WORKLOAD["seed"])
+    stride = WORKLOAD.get("k_cpu_stride", 1)
+    for _ in range(args.warmup):
+        exchange_cpu_sample(orc, h, D, stride * 4)
+    vals = []
+    for _ in range(args.steps):
+        v, sample = exchange_cpu_sample(orc, h, D, stride)
+        vals.append(v)
+    v = len(vals) / sum(1.0 / x for x in vals)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    out = {"impl": "reference", "metric": METRIC_K, "value": v, "unit": "K builds/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (generated alkane geometry, seeded density)", "config": dict(WORKLOAD, path="exchange"),
+           "cpu_baseline": {"value": v, "unit": "K builds/s", "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": v, "unit": "K builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    h.destroy()
+
+
+def run_gpu_exchange(args):
+    """K builds/s: the exchange path (H2ERI_build_exchange) on one GPU."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    import h2eri_gb300 as hg
+    from h2eri_gb300 import build as hb, molecules
+    if rank == 0:
+        hb.build()
+    h, setup_s = representation(hg, molecules, rank, ws, lambda: None)
+    L = hg.lib()
+    nbf = h.num_bf
+    D = molecules.seeded_density(nbf, WORKLOAD["n_occ"], WORKLOAD["seed"])
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    dD = torch.tensor(D, device="cuda")
+    dK = torch.empty_like(dD)
+    torch.cuda.synchronize()
+    t_plan = time.perf_counter()
+    if L.H2ERI_build_exchange_device(h.handle, dD.data_ptr(), dK.data_ptr(), sp) != 0:
+        raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+    torch.cuda.synchronize()
+    plan_s = time.perf_counter() - t_plan
+    modes = ["fp64"] if args.precision in ("auto", "fp64") else []
+    if args.precision in ("auto", "mixed"):
+        modes.append("mixed")
+
+    def device_run(mode):
+        L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if mode == "mixed" else hg.FP64)
+        for _ in range(args.warmup):
+            if L.H2ERI_build_exchange_device(h.handle, dD.data_ptr(), dK.data_ptr(), sp) != 0:
+                raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                L.H2ERI_build_exchange_device(h.handle, dD.data_ptr(), dK.data_ptr(), sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        return e0.elapsed_time(e1), dK.cpu().numpy(), clk.summary()
+
+    res = {m: device_run(m) for m in modes}
+    best = "mixed" if "mixed" in res else "fp64"
+    L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if best == "mixed" else hg.FP64)
+    ms, K, c = res[best]
+    hD = torch.from_numpy(D).pin_memory()
+    hK = torch.empty_like(hD).pin_memory()
+    L.H2ERI_build_exchange_multi(h.handle, 1, hD.data_ptr(), hK.data_ptr())
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.H2ERI_build_exchange_multi(h.handle, 1, hD.data_ptr(), hK.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    xr = h.exchange_report()
+    step_s = ms / 1e3 / args.steps
+    orc = load_oracle()
+    cpu = None
+    if not args.skip_cpu:
+        v, sample = exchange_cpu_sample(orc, h, D, WORKLOAD.get("k_cpu_stride", 1))
+        cpu = {"value": v, "unit": "K builds/s", "cores": os.cpu_count(), "kind": "port", "sample": sample}
+    K_ref = None
+    if WORKLOAD.get("k_check_full", False):
+        K_ref = np.zeros_like(D)
+        orc.oracle_build_exchange(h.handle, D.ctypes.data, K_ref.ctypes.data)
+    elif "fp64" in res:
+        K_ref = res["fp64"][1]   # FP64 GPU K (equal to the oracle's to ~1e-15 where checked)
+
+    def rel(X):
+        return None if K_ref is None else float(np.linalg.norm(X - K_ref) / np.linalg.norm(K_ref))
+
+    achieved = xr["flops"] / step_s / 1e12
+    peak = 1.25 if best == "fp64" else 74.0
+    out = {
+        "metric": METRIC_K, "value": args.steps / (ms / 1e3), "unit": "K builds/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if best == "fp64" else "f32+f64",
+        "data": "synthetic (generated alkane geometry, seeded density)",
+        "config": dict(WORKLOAD, path="exchange", precision=best, parallelism="replicas x1"),
+        "relerr_vs_fp64": rel(K),
+        "relerr_reference": "FP64 CPU oracle" if WORKLOAD.get("k_check_full", False) else "FP64 GPU path",
+        "fp64": ({"value": args.steps / (res["fp64"][0] / 1e3), "unit": "K builds/s",
+                  "ms_per_step": res["fp64"][0] / args.steps, "relerr_vs_fp64_oracle":
+                  rel(res["fp64"][1]) if WORKLOAD.get("k_check_full", False) else None}
+                 if "fp64" in res and best != "fp64" else None),
+        "e2e": {"value": args.steps / e2e_s, "unit": "K builds/s", "h2d_bytes_per_step": 8 * nbf * nbf,
+                "d2h_bytes_per_step": 8 * nbf * nbf},
+        "roofline": {"bound": "fp64" if best == "fp64" else "fp32-simt", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "kernel": "k_gemm + k_near (all launches of one K build)",
+                     "alg_flops_per_step": xr["flops"],
+                     "peak_kind": "nominal (no measured FP64 / FP32-SIMT peak): FP64 1.25, FP32 FMA 152 SMs x 128 x 2 x 1.9 GHz"},
+        "cpu_baseline": cpu,
+        "clocks": {"sm_mhz": c["sm_mhz"], "sm_max_mhz": c["sm_max_mhz"], "reasons": c["reasons"]},
+        "gpu_launches": int(xr["launches"]) * args.steps,
+        "plan": {"first_call_s": plan_s, "n_ranges": xr["n_ranges"], "work_bytes": xr["work_bytes"],
+                 "near_items": xr["near_items"]},
+        "setup_s": setup_s,
+    }
+    print(json.dumps(out), flush=True)
+    h.destroy()
+
+
 def run_gpu(args):
+    if args.path == "exchange":
+        return run_gpu_exchange(args)
     import torch
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -352,6 +504,8 @@ def main():
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--workload", default="c30", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg (profiler runs)")
+    ap.add_argument("--path", default="coulomb", choices=["coulomb", "exchange"],
+                    help="coulomb: J builds (the headline); exchange: K builds (H2ERI_build_exchange)")
     args = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[args.workload])

@@ -36,6 +36,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -62,96 +63,153 @@ constexpr double kDensityTol = 1e-10;
 /* ======================================================================== */
 
 /* Operand element (r, c, z) = p[G(z) * sz + G(r) * sr + G(c) * sc], each G an
- * optional gather list (nullptr = identity). */
+ * optional gather list (nullptr = identity). p points to doubles or floats
+ * (the kernel's element type); c64 marks an FP64 output (K) of an FP32
+ * product. */
 struct Opnd {
-    const double *p;
+    const void *p;
     const int *gr, *gc, *gz;
     long long sr, sc, sz;
 };
 
-/* C(i, j, z) += sum_k A(i, k, z) B(k, j, z), i < M, j < N, k < K, z < Z;
- * C is updated with atomics (tasks of one launch may share outputs). */
+/* C(i, (z, j)) += sum_k A(i, k) B(k, j, z), i < M, j < N, k < K, z < Z. The
+ * batch index z is folded into the columns (column jz = z * N + j), so a tile
+ * spans several batch entries when N is small; A does not depend on z. C is
+ * updated with atomics (tasks of one launch may share outputs). */
 struct GemmTask {
     Opnd a, b, c;
     int M, N, K, Z;
+    int c64;
 };
 
-constexpr int kGM = 64, kGN = 64, kGK = 16, kGThreads = 256;
+constexpr int kGThreads = 256;
 
-__device__ __forceinline__ double opnd_ld(const Opnd &o, int r, int c, long long zo)
+/* Tile shapes: FP64 64 x 64 (4 x 4 per thread, FP64-pipe bound), FP32
+ * 128 x 128 (8 x 8 per thread, so shared-memory traffic stays at one byte
+ * per FMA). 16 x 16 threads, k-steps of 16. */
+template <typename T> struct GemmCfg;
+template <> struct GemmCfg<double> { static constexpr int TM = 64, TN = 64; };
+template <> struct GemmCfg<float> { static constexpr int TM = 128, TN = 128; };
+constexpr int kGK = 16;
+
+template <typename T>
+__host__ __device__ constexpr long long gemm_tiles(int M, int N, int Z)
 {
-    long long ro = o.gr ? (long long)o.gr[r] : (long long)r;
-    long long co = o.gc ? (long long)o.gc[c] : (long long)c;
-    return o.p[zo + ro * o.sr + co * o.sc];
+    return (long long)((M + GemmCfg<T>::TM - 1) / GemmCfg<T>::TM) *
+           (((long long)N * Z + GemmCfg<T>::TN - 1) / GemmCfg<T>::TN);
 }
 
-/* One CTA per 64 x 64 output tile of one (task, z); tile_start[t] is the
- * first tile of task t (prefix sums, tile_start[n_task] = total). */
-__global__ void __launch_bounds__(kGThreads) k_gemm_f64(const GemmTask *__restrict__ tasks,
-                                                         const long long *__restrict__ tile_start, int n_task)
+/* One CTA per TM x TN output tile; tile_start[t] is the first tile of task t
+ * (prefix sums, tile_start[n_task] = total). */
+template <typename T>
+__global__ void __launch_bounds__(kGThreads) k_gemm(const GemmTask *__restrict__ tasks,
+                                                     const long long *__restrict__ tile_start, int n_task)
 {
-    __shared__ double As[kGK][kGM + 1];
-    __shared__ double Bs[kGK][kGN + 1];
-    const long long tile = blockIdx.x + (long long)blockIdx.y * gridDim.x;
+    constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN, RM = TM / 16, RN = TN / 16;
+    constexpr int UA = TM * kGK / kGThreads, UB = TN * kGK / kGThreads;
+    __shared__ T As[kGK][TM + 4];
+    __shared__ T Bs[kGK][TN + 4];
+    const long long tile = blockIdx.x;
     if (tile >= tile_start[n_task]) return;
     int lo = 0, hi = n_task - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (tile_start[mid] <= tile) lo = mid; else hi = mid - 1;
     }
-    const GemmTask &T = tasks[lo];
-    long long loc = tile - tile_start[lo];
-    const int tm_n = (T.M + kGM - 1) / kGM, tn_n = (T.N + kGN - 1) / kGN;
-    const int z = (int)(loc / ((long long)tm_n * tn_n));
-    loc -= (long long)z * tm_n * tn_n;
-    const int m0 = (int)(loc / tn_n) * kGM, n0 = (int)(loc % tn_n) * kGN;
-    const long long za = (T.a.gz ? (long long)T.a.gz[z] : z) * T.a.sz;
-    const long long zb = (T.b.gz ? (long long)T.b.gz[z] : z) * T.b.sz;
-    const long long zc = (T.c.gz ? (long long)T.c.gz[z] : z) * T.c.sz;
+    const GemmTask &Tk = tasks[lo];
+    const long long loc = tile - tile_start[lo];
+    const long long NZ = (long long)Tk.N * Tk.Z;
+    const long long tn_n = (NZ + TN - 1) / TN;
+    const int m0 = (int)(loc / tn_n) * TM;
+    const long long n0 = (loc % tn_n) * TN;
+    const T *Ap = reinterpret_cast<const T *>(Tk.a.p);
+    const T *Bp = reinterpret_cast<const T *>(Tk.b.p);
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    double acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int b = 0; b < 4; b++) acc[a][b] = 0.0;
 
-    for (int k0 = 0; k0 < T.K; k0 += kGK) {
+    /* operand offsets that stay fixed over k */
+    const int ka = tid % kGK;                       /* k of this thread's A loads  */
+    long long aro[UA];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            int e = tid + u * kGThreads;
-            int kk = e & 15, ii = e >> 4;       /* A tile: 64 rows x 16 k */
-            int gi = m0 + ii, gk = k0 + kk;
-            As[kk][ii] = (gi < T.M && gk < T.K) ? opnd_ld(T.a, gi, gk, za) : 0.0;
-            int jj = e & 63, kb = e >> 6;        /* B tile: 16 k x 64 cols */
-            int gj = n0 + jj, gk2 = k0 + kb;
-            Bs[kb][jj] = (gj < T.N && gk2 < T.K) ? opnd_ld(T.b, gk2, gj, zb) : 0.0;
+    for (int u = 0; u < UA; u++) {
+        int gi = m0 + (tid + u * kGThreads) / kGK;
+        aro[u] = gi < Tk.M ? (Tk.a.gr ? (long long)Tk.a.gr[gi] : (long long)gi) * Tk.a.sr : -1;
+    }
+    const int jb = tid % TN;                        /* column of this thread's B loads */
+    long long bco;
+    {
+        long long jz = n0 + jb;
+        if (jz < NZ) {
+            int z = (int)(jz / Tk.N), c = (int)(jz % Tk.N);
+            bco = (Tk.b.gz ? (long long)Tk.b.gz[z] : (long long)z) * Tk.b.sz +
+                  (Tk.b.gc ? (long long)Tk.b.gc[c] : (long long)c) * Tk.b.sc;
+        } else {
+            bco = -1;
+        }
+    }
+    T acc[RM][RN];
+#pragma unroll
+    for (int a = 0; a < RM; a++)
+#pragma unroll
+        for (int b = 0; b < RN; b++) acc[a][b] = T(0);
+
+    for (int k0 = 0; k0 < Tk.K; k0 += kGK) {
+        {
+            const int gk = k0 + ka;
+            const long long kc = gk < Tk.K ? (Tk.a.gc ? (long long)Tk.a.gc[gk] : (long long)gk) * Tk.a.sc : 0;
+#pragma unroll
+            for (int u = 0; u < UA; u++) {
+                const int ii = (tid + u * kGThreads) / kGK;
+                As[ka][ii] = (aro[u] >= 0 && gk < Tk.K) ? Ap[aro[u] + kc] : T(0);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < UB; u++) {
+            const int kb = (tid + u * kGThreads) / TN;
+            const int gk = k0 + kb;
+            T v = T(0);
+            if (bco >= 0 && gk < Tk.K)
+                v = Bp[bco + (Tk.b.gr ? (long long)Tk.b.gr[gk] : (long long)gk) * Tk.b.sr];
+            Bs[kb][jb] = v;
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < kGK; kk++) {
-            double av[4], bv[4];
+            T av[RM], bv[RN];
 #pragma unroll
-            for (int a = 0; a < 4; a++) av[a] = As[kk][ty + 16 * a];
+            for (int a = 0; a < RM; a++) av[a] = As[kk][ty + 16 * a];
 #pragma unroll
-            for (int b = 0; b < 4; b++) bv[b] = Bs[kk][tx + 16 * b];
+            for (int b = 0; b < RN; b++) bv[b] = Bs[kk][tx + 16 * b];
 #pragma unroll
-            for (int a = 0; a < 4; a++)
+            for (int a = 0; a < RM; a++)
 #pragma unroll
-                for (int b = 0; b < 4; b++) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+                for (int b = 0; b < RN; b++) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
         }
         __syncthreads();
     }
+    long long cco[RN];
 #pragma unroll
-    for (int a = 0; a < 4; a++) {
+    for (int b = 0; b < RN; b++) {
+        long long jz = n0 + tx + 16 * b;
+        if (jz < NZ) {
+            int z = (int)(jz / Tk.N), c = (int)(jz % Tk.N);
+            cco[b] = (Tk.c.gz ? (long long)Tk.c.gz[z] : (long long)z) * Tk.c.sz +
+                     (Tk.c.gc ? (long long)Tk.c.gc[c] : (long long)c) * Tk.c.sc;
+        } else {
+            cco[b] = -1;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < RM; a++) {
         int gi = m0 + ty + 16 * a;
-        if (gi >= T.M) continue;
-        long long ro = (T.c.gr ? (long long)T.c.gr[gi] : (long long)gi) * T.c.sr;
+        if (gi >= Tk.M) continue;
+        long long ro = (Tk.c.gr ? (long long)Tk.c.gr[gi] : (long long)gi) * Tk.c.sr;
 #pragma unroll
-        for (int b = 0; b < 4; b++) {
-            int gj = n0 + tx + 16 * b;
-            if (gj >= T.N) continue;
-            long long co = (T.c.gc ? (long long)T.c.gc[gj] : (long long)gj) * T.c.sc;
-            atomicAdd(const_cast<double *>(T.c.p) + zc + ro + co, acc[a][b]);
+        for (int b = 0; b < RN; b++) {
+            if (cco[b] < 0) continue;
+            if (Tk.c64)
+                atomicAdd(reinterpret_cast<double *>(const_cast<void *>(Tk.c.p)) + ro + cco[b], (double)acc[a][b]);
+            else
+                atomicAdd(reinterpret_cast<T *>(const_cast<void *>(Tk.c.p)) + ro + cco[b], acc[a][b]);
         }
     }
 }
@@ -177,13 +235,15 @@ __global__ void k_density_sig(const double *__restrict__ den, int nbf, int nsh, 
 
 /* D'[p][n] = D[p][n] if the block (shell(n), shell(p)) is significant, else 0:
  * the reference reads D[p][n] for P in dlist[N] only (:590-650). */
+template <typename T>
 __global__ void k_density_masked(const double *__restrict__ den, int nbf, int nsh, const int *__restrict__ bf_shell,
-                                 const int *__restrict__ sig, double *__restrict__ dp)
+                                 const int *__restrict__ sig, T *__restrict__ dp)
 {
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)nbf * nbf) return;
     int p = (int)(t / nbf), n = (int)(t % nbf);
-    dp[t] = sig[(long long)bf_shell[n] * nsh + bf_shell[p]] ? den[t] : 0.0;
+    double v = sig[(long long)bf_shell[n] * nsh + bf_shell[p]] ? den[t] : 0.0;
+    dp[t] = (T)v;
 }
 
 /* Near-field block use: rows = oriented pairs e of leaf i (local row, m, n),
@@ -191,7 +251,7 @@ __global__ void k_density_masked(const double *__restrict__ den, int nbf, int ns
  *   K[m_e][q_g] += sum_{f in g} Dblk(row_e, row_f) * D'[p_f][n_e]
  * with Dblk(r, c) = blk[r * ld + c], or blk[c * ld + r] when trans. */
 struct NearTask {
-    const double *blk;
+    long long off;  /* element offset of the block in the arena */
     int ld, trans;
     int e0, ne;     /* oriented rows of leaf i: ext arrays [e0, e0 + ne) */
     int g0, ng;     /* q-groups of leaf j: group arrays [g0, g0 + ng)    */
@@ -205,9 +265,11 @@ struct ExtArrays {
     const int *gc;    /* group count                                */
 };
 
+template <typename T>
 __global__ void __launch_bounds__(256) k_near(const NearTask *__restrict__ tasks,
                                               const long long *__restrict__ item_start, int n_task, ExtArrays ex,
-                                              const double *__restrict__ dp, int nbf, double *__restrict__ K)
+                                              const T *__restrict__ arena, const T *__restrict__ dp, int nbf,
+                                              double *__restrict__ K)
 {
     long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (it >= item_start[n_task]) return;
@@ -216,21 +278,29 @@ __global__ void __launch_bounds__(256) k_near(const NearTask *__restrict__ tasks
         int mid = (lo + hi + 1) >> 1;
         if (item_start[mid] <= it) lo = mid; else hi = mid - 1;
     }
-    const NearTask &T = tasks[lo];
+    const NearTask &Tk = tasks[lo];
     long long loc = it - item_start[lo];
-    int e = T.e0 + (int)(loc / T.ng), g = T.g0 + (int)(loc % T.ng);
+    int e = Tk.e0 + (int)(loc / Tk.ng), g = Tk.g0 + (int)(loc % Tk.ng);
     const int re = ex.row[e], n = ex.y[e];
     const int f0 = ex.gs[g], nf = ex.gc[g];
-    const double *drow = dp + n;  /* D'[p][n] = drow[p * nbf] */
-    double s = 0.0;
-    if (!T.trans) {
-        const double *b = T.blk + (long long)re * T.ld;
+    const T *blk = arena + Tk.off;
+    const T *drow = dp + n;  /* D'[p][n] = drow[p * nbf] */
+    T s = T(0);
+    if (!Tk.trans) {
+        const T *b = blk + (long long)re * Tk.ld;
         for (int f = f0; f < f0 + nf; f++) s = fma(b[ex.row[f]], drow[(long long)ex.x[f] * nbf], s);
     } else {
         for (int f = f0; f < f0 + nf; f++)
-            s = fma(T.blk[(long long)ex.row[f] * T.ld + re], drow[(long long)ex.x[f] * nbf], s);
+            s = fma(blk[(long long)ex.row[f] * Tk.ld + re], drow[(long long)ex.x[f] * nbf], s);
     }
-    if (s != 0.0) atomicAdd(K + (long long)ex.x[e] * nbf + ex.y[f0], s);
+    if (s != T(0)) atomicAdd(K + (long long)ex.x[e] * nbf + ex.y[f0], (double)s);
+}
+
+/* FP32 copies of the arena and of the masked density (mixed mode) */
+__global__ void k_to_f32(const double *__restrict__ src, float *__restrict__ dst, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = __double2float_rn(src[i]);
 }
 
 /* ======================================================================== */
@@ -264,13 +334,22 @@ struct KChunk {
     std::vector<KGroup> groups;   /* launch order */
 };
 
+/* Launch data of one arithmetic precision (tile shapes differ). */
+struct KVariant {
+    GemmTask *tasks = nullptr;
+    long long *tile_start = nullptr;   /* per group: nt + 1 prefix sums, concatenated */
+    std::vector<long long> group_pre;  /* offset of each group's prefix array, launch order */
+    std::vector<long long> group_tiles;
+};
+
 struct KState {
     int nbf = 0, nsh = 0;
     double *arena = nullptr;      /* U (row-major, ld = rank), B and D dense (row-major, ld = ncol) */
+    float *arena32 = nullptr;     /* FP32 copy (mixed mode, made on first use) */
+    size_t arena_elems = 0;
     int *pool = nullptr;          /* every index list of the plan */
-    GemmTask *tasks = nullptr;
-    long long *tile_start = nullptr;   /* per group: nt + 1 prefix sums, concatenated */
-    std::vector<long long> group_pre;  /* offset of each group's prefix array */
+    std::vector<HTask> htasks;    /* host copy of the tasks (the FP32 variant is made from it) */
+    KVariant v64, v32;
     NearTask *near = nullptr;
     long long *near_start = nullptr;
     int n_near = 0;
@@ -278,6 +357,7 @@ struct KState {
     ExtArrays ext{};
     int *sb = nullptr, *bf_shell = nullptr, *sig = nullptr;
     double *dp = nullptr, *gh = nullptr, *kbuf = nullptr;
+    float *dp32 = nullptr;
     size_t gh_elems = 0;
     std::vector<KChunk> chunks;
     double flops = 0.0;           /* per K build */
@@ -289,7 +369,8 @@ void free_exchange_state(DevRep *d)
 {
     KState *k = (KState *)d->kstate;
     if (k == nullptr) return;
-    cudaFree(k->arena); cudaFree(k->pool); cudaFree(k->tasks); cudaFree(k->tile_start);
+    cudaFree(k->arena); cudaFree(k->arena32); cudaFree(k->pool); cudaFree(k->dp32);
+    for (KVariant *v : {&k->v64, &k->v32}) { cudaFree(v->tasks); cudaFree(v->tile_start); }
     cudaFree(k->near); cudaFree(k->near_start);
     cudaFree(k->sb); cudaFree(k->bf_shell); cudaFree(k->sig);
     cudaFree(k->dp); cudaFree(k->gh); cudaFree(k->kbuf);
@@ -342,6 +423,73 @@ static bool opnd_in_bounds(const HOpnd &o, int R, int C, int Z, size_t size, con
     if (rl < 0 || cl < 0 || zl < 0 || o.sr < 0 || o.sc < 0 || o.sz < 0 || o.off < 0) return false;
     long long hi = o.off + zh * o.sz + rh * o.sr + ch * o.sc;
     return hi < (long long)size;
+}
+
+/* Device task list and tile prefix sums of one precision: operands point
+ * into the FP64 or the FP32 arena, density and work tensors; K stays FP64. */
+template <typename T>
+static int upload_variant(KState *ks)
+{
+    KVariant &v = std::is_same<T, double>::value ? ks->v64 : ks->v32;
+    auto base = [&](int buf) -> const void * {
+        switch (buf) {
+        case KB_ARENA: return std::is_same<T, double>::value ? (const void *)ks->arena : (const void *)ks->arena32;
+        case KB_GH: return ks->gh;
+        case KB_K: return ks->kbuf;
+        default: return std::is_same<T, double>::value ? (const void *)ks->dp : (const void *)ks->dp32;
+        }
+    };
+    auto conv = [&](const HOpnd &o) {
+        Opnd r;
+        const size_t es = o.buf == KB_K ? sizeof(double) : sizeof(T);
+        r.p = (const char *)base(o.buf) + o.off * (long long)es;
+        r.gr = o.gr >= 0 ? ks->pool + o.gr : nullptr;
+        r.gc = o.gc >= 0 ? ks->pool + o.gc : nullptr;
+        r.gz = o.gz >= 0 ? ks->pool + o.gz : nullptr;
+        r.sr = o.sr; r.sc = o.sc; r.sz = o.sz;
+        return r;
+    };
+    std::vector<GemmTask> dt(ks->htasks.size() + 1);
+    for (size_t t = 0; t < ks->htasks.size(); t++) {
+        const HTask &Tk = ks->htasks[t];
+        dt[t].a = conv(Tk.a); dt[t].b = conv(Tk.b); dt[t].c = conv(Tk.c);
+        dt[t].M = Tk.M; dt[t].N = Tk.N; dt[t].K = Tk.K; dt[t].Z = Tk.Z;
+        dt[t].c64 = Tk.c.buf == KB_K;
+    }
+    std::vector<long long> pre;
+    v.group_pre.clear();
+    v.group_tiles.clear();
+    for (const KChunk &ch : ks->chunks)
+        for (const KGroup &g : ch.groups) {
+            v.group_pre.push_back((long long)pre.size());
+            long long acc = 0;
+            pre.push_back(0);
+            for (int t = g.t0; t < g.t0 + g.nt; t++) {
+                const HTask &Tk = ks->htasks[t];
+                acc += gemm_tiles<T>(Tk.M, Tk.N, Tk.Z);
+                pre.push_back(acc);
+            }
+            if (acc > 0x7fffffffLL) { set_error("exchange: launch too large"); return 4; }
+            v.group_tiles.push_back(acc);
+        }
+    pre.push_back(0);
+    KCUDA_TRY(cudaMalloc(&v.tasks, dt.size() * sizeof(GemmTask)));
+    KCUDA_TRY(cudaMemcpy(v.tasks, dt.data(), dt.size() * sizeof(GemmTask), cudaMemcpyHostToDevice));
+    KCUDA_TRY(cudaMalloc(&v.tile_start, pre.size() * sizeof(long long)));
+    KCUDA_TRY(cudaMemcpy(v.tile_start, pre.data(), pre.size() * sizeof(long long), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+/* FP32 arena, density and task list, made on the first mixed-mode K build. */
+static int ensure_f32(KState *ks)
+{
+    if (ks->v32.tasks != nullptr) return 0;
+    KCUDA_TRY(cudaMalloc(&ks->arena32, ks->arena_elems * sizeof(float)));
+    k_to_f32<<<1216, 256>>>(ks->arena, ks->arena32, (long long)ks->arena_elems);
+    KCUDA_TRY(cudaGetLastError());
+    KCUDA_TRY(cudaMalloc(&ks->dp32, (size_t)ks->nbf * ks->nbf * sizeof(float)));
+    KCUDA_TRY(cudaDeviceSynchronize());
+    return upload_variant<float>(ks);
 }
 
 /* free_bytes: device memory the G / H work tensors may be sized against;
@@ -481,7 +629,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
             int di = (pi > 0 ? pi : -pi) - 1;
             if (ext_cnt[i] == 0 || grp_cnt[j] == 0) continue;
             NearTask t;
-            t.blk = (const double *)(uintptr_t)doff[di];   /* patched to a device address at upload */
+            t.off = (long long)doff[di];
             t.ld = h->c_D_blks[di]->ncol;
             t.trans = pi < 0;
             t.e0 = ext_off[i]; t.ne = ext_cnt[i];
@@ -684,21 +832,15 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
     }
 
     /* ---- tile counts and flops ---- */
-    std::vector<long long> pre;
     for (KChunk &ch : ks->chunks)
-        for (KGroup &g : ch.groups) {
-            ks->group_pre.push_back((long long)pre.size());
-            long long acc = 0;
-            pre.push_back(0);
+        for (KGroup &g : ch.groups)
             for (int t = g.t0; t < g.t0 + g.nt; t++) {
                 const HTask &T = pb.tasks[t];
-                acc += (long long)((T.M + kGM - 1) / kGM) * ((T.N + kGN - 1) / kGN) * T.Z;
-                pre.push_back(acc);
                 flops += 2.0 * T.M * (double)T.N * T.K * T.Z;
+                g.tiles += gemm_tiles<double>(T.M, T.N, T.Z);
             }
-            g.tiles = acc;
-        }
     ks->flops = flops;
+    ks->arena_elems = arena_elems;
     for (const KChunk &ch : ks->chunks) ks->gh_elems = std::max(ks->gh_elems, ch.gh_elems);
 
     ks->near_items = near_pre.back();
@@ -729,7 +871,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
     for (const NearTask &t : hnear) {
         int di = -1;
         for (int b = 0; b < h->n_D; b++)
-            if ((size_t)(uintptr_t)t.blk == doff[b]) { di = b; break; }
+            if ((size_t)t.off == doff[b]) { di = b; break; }
         if (di < 0 || t.e0 < 0 || t.e0 + t.ne > (int)e_row.size() || t.g0 < 0 || t.g0 + t.ng > (int)g_start.size()) {
             set_error("exchange plan: bad near-field task");
             return 5;
@@ -787,12 +929,13 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
             auto cv = [&](const HOpnd &o) {
                 Opnd r{};
                 r.p = (o.buf == KB_FACT ? fact : ks->arena) + o.off;
+                r.gr = r.gc = r.gz = nullptr;
                 r.sr = o.sr; r.sc = o.sc; r.sz = o.sz;
                 return r;
             };
             et[t].a = cv(T.a); et[t].b = cv(T.b); et[t].c = cv(T.c);
             et[t].M = T.M; et[t].N = T.N; et[t].K = T.K; et[t].Z = 1;
-            epre.push_back(epre.back() + (long long)((T.M + kGM - 1) / kGM) * ((T.N + kGN - 1) / kGN));
+            epre.push_back(epre.back() + gemm_tiles<double>(T.M, T.N, 1));
         }
         GemmTask *dtask = nullptr;
         long long *dpre = nullptr;
@@ -801,7 +944,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
         KCUDA_TRY(cudaMemcpy(dtask, et.data(), et.size() * sizeof(GemmTask), cudaMemcpyHostToDevice));
         KCUDA_TRY(cudaMemcpy(dpre, epre.data(), epre.size() * sizeof(long long), cudaMemcpyHostToDevice));
         if (epre.back() > 0x7fffffffLL) { set_error("exchange: expansion launch too large"); return 4; }
-        k_gemm_f64<<<(unsigned)epre.back(), kGThreads>>>(dtask, dpre, (int)et.size());
+        k_gemm<double><<<(unsigned)epre.back(), kGThreads>>>(dtask, dpre, (int)et.size());
         KCUDA_TRY(cudaGetLastError());
         KCUDA_TRY(cudaDeviceSynchronize());
         cudaFree(dtask);
@@ -820,36 +963,8 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
     KCUDA_TRY(cudaMalloc(&ks->kbuf, (size_t)nbf * nbf * sizeof(double)));
     KCUDA_TRY(cudaMalloc(&ks->gh, std::max<size_t>(ks->gh_elems, 1) * sizeof(double)));
 
-    auto base = [&](int buf) -> const double * {
-        switch (buf) {
-        case KB_ARENA: return ks->arena;
-        case KB_GH: return ks->gh;
-        case KB_K: return ks->kbuf;
-        default: return ks->dp;
-        }
-    };
-    auto conv = [&](const HOpnd &o) {
-        Opnd r;
-        r.p = base(o.buf) + o.off;
-        r.gr = o.gr >= 0 ? ks->pool + o.gr : nullptr;
-        r.gc = o.gc >= 0 ? ks->pool + o.gc : nullptr;
-        r.gz = o.gz >= 0 ? ks->pool + o.gz : nullptr;
-        r.sr = o.sr; r.sc = o.sc; r.sz = o.sz;
-        return r;
-    };
-    std::vector<GemmTask> dt(pb.tasks.size() + 1);
-    for (size_t t = 0; t < pb.tasks.size(); t++) {
-        const HTask &T = pb.tasks[t];
-        dt[t].a = conv(T.a); dt[t].b = conv(T.b); dt[t].c = conv(T.c);
-        dt[t].M = T.M; dt[t].N = T.N; dt[t].K = T.K; dt[t].Z = T.Z;
-    }
-    KCUDA_TRY(cudaMalloc(&ks->tasks, dt.size() * sizeof(GemmTask)));
-    KCUDA_TRY(cudaMemcpy(ks->tasks, dt.data(), dt.size() * sizeof(GemmTask), cudaMemcpyHostToDevice));
-    pre.push_back(0);
-    KCUDA_TRY(cudaMalloc(&ks->tile_start, pre.size() * sizeof(long long)));
-    KCUDA_TRY(cudaMemcpy(ks->tile_start, pre.data(), pre.size() * sizeof(long long), cudaMemcpyHostToDevice));
-
-    for (NearTask &t : hnear) t.blk = ks->arena + (size_t)(uintptr_t)t.blk;
+    ks->htasks.swap(pb.tasks);
+    if (upload_variant<double>(ks) != 0) return 10;
     ks->n_near = (int)hnear.size();
     ks->near_items = near_pre.back();
     hnear.emplace_back();
@@ -871,30 +986,45 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
 /* Launch                                                                    */
 /* ======================================================================== */
 
-static int enqueue_exchange(KState *ks, const double *den, double *K, cudaStream_t s, bool timed)
+template <typename T>
+static int enqueue_typed(KState *ks, const double *den, cudaStream_t s)
 {
     const int nbf = ks->nbf, nsh = ks->nsh;
-    if (timed) KCUDA_TRY(cudaEventRecord(ks->ev0, s));
+    const KVariant &v = std::is_same<T, double>::value ? ks->v64 : ks->v32;
+    T *dp = std::is_same<T, double>::value ? (T *)ks->dp : (T *)ks->dp32;
+    const T *arena = std::is_same<T, double>::value ? (const T *)ks->arena : (const T *)ks->arena32;
     KCUDA_TRY(cudaMemsetAsync(ks->kbuf, 0, (size_t)nbf * nbf * sizeof(double), s));
     long long n = (long long)nsh * nsh;
     k_density_sig<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(den, nbf, nsh, ks->sb, ks->sig);
     n = (long long)nbf * nbf;
-    k_density_masked<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(den, nbf, nsh, ks->bf_shell, ks->sig, ks->dp);
+    k_density_masked<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(den, nbf, nsh, ks->bf_shell, ks->sig, dp);
     if (ks->near_items > 0)
-        k_near<<<(unsigned)((ks->near_items + 255) / 256), 256, 0, s>>>(ks->near, ks->near_start, ks->n_near, ks->ext,
-                                                                        ks->dp, nbf, ks->kbuf);
+        k_near<T><<<(unsigned)((ks->near_items + 255) / 256), 256, 0, s>>>(ks->near, ks->near_start, ks->n_near, ks->ext,
+                                                                           arena, dp, nbf, ks->kbuf);
     size_t gi = 0;
     for (const KChunk &ch : ks->chunks) {
-        KCUDA_TRY(cudaMemsetAsync(ks->gh, 0, ch.gh_elems * sizeof(double), s));
+        KCUDA_TRY(cudaMemsetAsync(ks->gh, 0, ch.gh_elems * sizeof(T), s));
         for (const KGroup &g : ch.groups) {
-            if (g.tiles > 0) {
-                if (g.tiles > 0x7fffffffLL) { set_error("exchange: launch too large"); return 4; }
-                k_gemm_f64<<<(unsigned)g.tiles, kGThreads, 0, s>>>(ks->tasks + g.t0, ks->tile_start + ks->group_pre[gi],
-                                                                   g.nt);
-            }
+            const long long tiles = v.group_tiles[gi];
+            if (tiles > 0)
+                k_gemm<T><<<(unsigned)tiles, kGThreads, 0, s>>>(v.tasks + g.t0, v.tile_start + v.group_pre[gi], g.nt);
             gi++;
         }
     }
+    return 0;
+}
+
+/* K of one density on device arrays; mixed = FP32 contractions (FP64 K). */
+static int enqueue_exchange(KState *ks, const double *den, double *K, cudaStream_t s, bool timed, bool mixed)
+{
+    const int nbf = ks->nbf;
+    if (mixed) {
+        int rc = ensure_f32(ks);
+        if (rc) return rc;
+    }
+    if (timed) KCUDA_TRY(cudaEventRecord(ks->ev0, s));
+    int rc = mixed ? enqueue_typed<float>(ks, den, s) : enqueue_typed<double>(ks, den, s);
+    if (rc) return rc;
     if (K != ks->kbuf)
         KCUDA_TRY(cudaMemcpyAsync(K, ks->kbuf, (size_t)nbf * nbf * sizeof(double), cudaMemcpyDeviceToDevice, s));
     if (timed) KCUDA_TRY(cudaEventRecord(ks->ev1, s));
@@ -953,7 +1083,7 @@ extern "C" int H2ERI_build_exchange_device(H2ERI_p h2eri, const double *d_den, d
     if (rc) return rc;
     if (d_den == nullptr || d_K == nullptr) { set_error("null density or K pointer"); return 3; }
     cudaStream_t s = stream ? (cudaStream_t)stream : d->s_main;
-    return enqueue_exchange(ks, d_den, d_K, s, false);
+    return enqueue_exchange(ks, d_den, d_K, s, false, d->precision == H2ERI_GPU_MIXED);
 }
 
 extern "C" int H2ERI_build_exchange_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *K_mats)
@@ -969,7 +1099,7 @@ extern "C" int H2ERI_build_exchange_multi(H2ERI_p h2eri, int n_den, const double
         /* the masked-density buffer doubles as the staging copy of the input:
          * k_density_masked reads element t before it writes element t */
         KCUDA_TRY(cudaMemcpyAsync(ks->dp, den_mats + i * nn, bytes, cudaMemcpyHostToDevice, d->s_main));
-        rc = enqueue_exchange(ks, ks->dp, ks->kbuf, d->s_main, true);
+        rc = enqueue_exchange(ks, ks->dp, ks->kbuf, d->s_main, true, d->precision == H2ERI_GPU_MIXED);
         if (rc) return rc;
         KCUDA_TRY(cudaMemcpyAsync(K_mats + i * nn, ks->kbuf, bytes, cudaMemcpyDeviceToHost, d->s_main));
         KCUDA_TRY(cudaStreamSynchronize(d->s_main));

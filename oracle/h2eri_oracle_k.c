@@ -278,9 +278,10 @@ static void partial_product(const H2ERI_p h, const side_sel *rs, const side_sel 
     }
 }
 
-/* K = exchange matrix of the symmetric density den (both num_bf^2, row-major);
- * src/H2ERI_build_exchange.c:1356-1450 */
-void oracle_build_exchange(H2ERI_p h, const double *den, double *K)
+/* The contributions of the outer shells N in Nlist[0..nN) to K (the
+ * reference's N loop, src/H2ERI_build_exchange.c:1386-1425); all shells give
+ * the full K. */
+void oracle_build_exchange_shells(H2ERI_p h, const double *den, double *K, const int *Nlist, int n_list)
 {
     const int nbf = h->num_bf, nsh = h->nshell, n_node = h->n_node, krnl = h->krnl_mat_size;
     const int *sb = h->shell_bf_sidx;
@@ -335,7 +336,8 @@ void oracle_build_exchange(H2ERI_p h, const double *den, double *K)
         double *tmp = (double *)malloc(sizeof(double) * ((size_t)rmax * nvmax + 1));
 
         #pragma omp for schedule(dynamic)
-        for (int N = 0; N < nsh; N++) {
+        for (int iN = 0; iN < n_list; iN++) {
+            const int N = Nlist[iN];
             const int nN = sb[N + 1] - sb[N];
             /* row side: (m, n) for M in plist[N] (:248-350) */
             int n = 0;
@@ -395,4 +397,14 @@ void oracle_build_exchange(H2ERI_p h, const double *den, double *K)
         K[i] = s;
     }
     free(Kt); free(voff); free(row_leaf); free(sig);
+}
+
+/* K = exchange matrix of the symmetric density den (both num_bf^2, row-major);
+ * src/H2ERI_build_exchange.c:1356-1450 */
+void oracle_build_exchange(H2ERI_p h, const double *den, double *K)
+{
+    int *all = (int *)malloc(sizeof(int) * (size_t)(h->nshell + 1));
+    for (int i = 0; i < h->nshell; i++) all[i] = i;
+    oracle_build_exchange_shells(h, den, K, all, h->nshell);
+    free(all);
 }

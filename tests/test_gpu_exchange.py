@@ -88,3 +88,22 @@ def test_exchange_report(alk26):
     alk26.build_exchange(np.eye(alk26.num_bf))
     r = alk26.exchange_report()
     assert r["flops"] > 0 and r["ms_last"] > 0 and r["launches"] >= 3
+
+
+TOL_MIXED_K = 1e-5
+
+
+def test_exchange_mixed_precision(alk26, oracle_lib):
+    """FP32 contractions (FP32 blocks, density and work tensors) with FP64
+    K assembly, against the FP64 oracle."""
+    n = alk26.num_bf
+    D = np.fromfile(os.path.join(GOLDEN, "D_alk26_ccpvdz.bin")).reshape(n, n)
+    K64 = oracle_K(oracle_lib, alk26, D)
+    alk26.set_precision(hg.MIXED)
+    try:
+        K32 = alk26.build_exchange(D)
+    finally:
+        alk26.set_precision(hg.FP64)
+    err = relerr(K32, K64)
+    print(f"mixed K relerr vs FP64 oracle: {err:.3e}")
+    assert err < TOL_MIXED_K
