@@ -27,6 +27,7 @@
 
 #include "h2eri_gb300.h"
 #include "h2g_device.cuh"
+#include "h2g_farith.cuh"
 #include "h2g_gpu_stats.h"
 #include "h2g_gpu_api.h"
 
@@ -58,115 +59,12 @@ __device__ __forceinline__ double *vec_ptr(const VecArgs &va, uint8_t kind, int 
     return va.base[kind] + (long long)v * va.stride[kind] + off;
 }
 
-/* Compensated FP32 arithmetic (mixed mode). A product a * x with a = a_hi +
- * a_lo and x = x_hi + x_lo is accumulated into a float pair (sh, sl):
- * p = fl(a_hi x_hi) with its exact rounding error e from an FMA, the small
- * cross terms folded into e, and p added to sh with an error-free two-sum
- * whose error goes to sl. Explicit _rn intrinsics keep the compiler from
- * contracting the two-sum into FMAs. Only the stored-matrix rounding remains
- * (2^-24 relative for single floats, ~2^-48 for float pairs). */
-__device__ __forceinline__ void cacc(float &sh, float &sl, float ah, float al, float xh, float xl)
-{
-    const float p = __fmul_rn(ah, xh);
-    const float e = fmaf(ah, xh, -p);
-    const float c = fmaf(ah, xl, fmaf(al, xh, e));
-    const float s = __fadd_rn(sh, p);
-    const float bp = __fsub_rn(s, sh);
-    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bp)), __fsub_rn(p, bp));
-    sh = s;
-    sl = __fadd_rn(sl, __fadd_rn(err, c));
-}
-
-/* cacc for a single-float matrix entry (a_lo = 0) */
-__device__ __forceinline__ void cacc1(float &sh, float &sl, float ah, float xh, float xl)
-{
-    const float p = __fmul_rn(ah, xh);
-    const float c = fmaf(ah, xl, fmaf(ah, xh, -p));
-    const float s = __fadd_rn(sh, p);
-    const float bp = __fsub_rn(s, sh);
-    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bp)), __fsub_rn(p, bp));
-    sh = s;
-    sl = __fadd_rn(sl, __fadd_rn(err, c));
-}
-
-__device__ __forceinline__ void split(double x, float &hi, float &lo)
-{
-    hi = __double2float_rn(x);
-    lo = __double2float_rn(x - (double)hi);
-}
-
-/* Float-pair addition (a_h + a_l) += (b_h + b_l) with an error-free two-sum
- * on the high parts; the pair is left unnormalised. */
-__device__ __forceinline__ void dfadd(float &ah, float &al, float bh, float bl)
-{
-    const float s = __fadd_rn(ah, bh);
-    const float bp = __fsub_rn(s, ah);
-    const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bp)), __fsub_rn(bh, bp));
-    ah = s;
-    al = __fadd_rn(__fadd_rn(al, bl), err);
-}
-
 /* Column owned by lane `lane` in slot k (0..3) of a 128-column tile strip. */
 template <int FMT>
 __device__ __forceinline__ int lane_col(int lane, int k)
 {
     if (FMT == FMT_F32) return 4 * lane + k;
     return (k < 2) ? 2 * lane + k : 64 + 2 * lane + (k - 2);
-}
-
-/* Warp reduction of 8 per-lane row partials (rows r0..r0+7) by recursive
- * halving; afterwards lanes with (lane & 3) == 0 hold the full sum of row
- * r0 + row_of_lane(lane). T is double, or float pairs given as (h, l). */
-__device__ __forceinline__ int halving_row(int lane)
-{
-    return ((lane & 16) ? 4 : 0) + ((lane & 8) ? 2 : 0) + ((lane & 4) ? 1 : 0);
-}
-
-__device__ __forceinline__ double reduce8_f64(double s[8], int lane)
-{
-    const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        double send = b16 ? s[k] : s[k + 4];
-        double keep = b16 ? s[k + 4] : s[k];
-        s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        double send = b8 ? s[k] : s[k + 2];
-        double keep = b8 ? s[k + 2] : s[k];
-        s[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-    double send = b4 ? s[0] : s[1];
-    double val = (b4 ? s[1] : s[0]) + __shfl_xor_sync(0xffffffffu, send, 4);
-    val += __shfl_xor_sync(0xffffffffu, val, 2);
-    val += __shfl_xor_sync(0xffffffffu, val, 1);
-    return val;
-}
-
-__device__ __forceinline__ double reduce8_df(float h[8], float l[8], int lane)
-{
-    const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        float sh = b16 ? h[k] : h[k + 4], sl = b16 ? l[k] : l[k + 4];
-        float kh = b16 ? h[k + 4] : h[k], kl = b16 ? l[k + 4] : l[k];
-        dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 16), __shfl_xor_sync(0xffffffffu, sl, 16));
-        h[k] = kh; l[k] = kl;
-    }
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        float sh = b8 ? h[k] : h[k + 2], sl = b8 ? l[k] : l[k + 2];
-        float kh = b8 ? h[k + 2] : h[k], kl = b8 ? l[k + 2] : l[k];
-        dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 8), __shfl_xor_sync(0xffffffffu, sl, 8));
-        h[k] = kh; l[k] = kl;
-    }
-    float sh = b4 ? h[0] : h[1], sl = b4 ? l[0] : l[1];
-    float vh = b4 ? h[1] : h[0], vl = b4 ? l[1] : l[0];
-    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, sh, 4), __shfl_xor_sync(0xffffffffu, sl, 4));
-    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 2), __shfl_xor_sync(0xffffffffu, vl, 2));
-    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 1), __shfl_xor_sync(0xffffffffu, vl, 1));
-    return (double)vh + (double)vl;
 }
 
 /* ---- shared-memory staging with cp.async ---- */
@@ -438,10 +336,12 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
         sx1h[r] = h; sx1l[r] = l;
     }
     __syncthreads();
-    float xh[4], xl[4];
+    XIn xv[4];
 #pragma unroll
-    for (int c = 0; c < 4; c++) { xh[c] = sx0h[lane_col<FMT>(lane, c)]; xl[c] = sx0l[lane_col<FMT>(lane, c)]; }
-    float ch[4] = {0.f, 0.f, 0.f, 0.f}, cl[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int c = 0; c < 4; c++) xv[c] = xin(sx0h[lane_col<FMT>(lane, c)], sx0l[lane_col<FMT>(lane, c)]);
+    /* T-side column sums, columns paired (slots 0,1 and 2,3) */
+    float2 ch[2], cl[2];
+    ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
     for (int k = 0; k < nstage; k++) {
         cp_async_wait1();
         __syncthreads();
@@ -466,30 +366,40 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
             }
         }
         if (opN) {
-            float sh[RW], sl[RW];
+            /* rows paired: halves of a float2 are rows 2u and 2u+1 */
+            float2 sh2[RW / 2], sl2[RW / 2];
 #pragma unroll
-            for (int i = 0; i < RW; i++) {
-                sh[i] = 0.f; sl[i] = 0.f;
+            for (int u = 0; u < RW / 2; u++) {
+                sh2[u] = sl2[u] = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
-                    if (FMT == FMT_F32) cacc1(sh[i], sl[i], ahi[i][c], xh[c], xl[c]);
-                    else cacc(sh[i], sl[i], ahi[i][c], alo[i][c], xh[c], xl[c]);
+                    const float2 a = make_float2(ahi[2 * u][c], ahi[2 * u + 1][c]);
+                    if (FMT == FMT_F32) pk_cacc1(sh2[u], sl2[u], a, xv[c]);
+                    else pk_cacc2(sh2[u], sl2[u], a, make_float2(alo[2 * u][c], alo[2 * u + 1][c]), xv[c]);
                 }
+            }
+            float sh[RW], sl[RW];
+#pragma unroll
+            for (int u = 0; u < RW / 2; u++) {
+                sh[2 * u] = sh2[u].x; sh[2 * u + 1] = sh2[u].y;
+                sl[2 * u] = sl2[u].x; sl[2 * u + 1] = sl2[u].y;
             }
             float vh, vl;
             reduceR_df<RW>(sh, sl, lane, vh, vl);
             const int row = r0 + halving_row_R<RW>(lane);
-            if (halving_owner<RW>(lane) && row < nr) atomicAdd(out0 + row, (double)vh + (double)vl);
+            if (halving_owner<RW>(lane) && row < nr) atomic_add_pair(out0 + row, vh, vl);
         }
         if (opT) {
 #pragma unroll
             for (int i = 0; i < RW; i++) {
                 const int r = min(r0 + i, kChunkRows - 1);
-                const float x1h = sx1h[r], x1l = sx1l[r];
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    if (FMT == FMT_F32) cacc1(ch[c], cl[c], ahi[i][c], x1h, x1l);
-                    else cacc(ch[c], cl[c], ahi[i][c], alo[i][c], x1h, x1l);
+                const XIn x1 = xin(sx1h[r], sx1l[r]);
+                if (FMT == FMT_F32) {
+                    pk_cacc1(ch[0], cl[0], make_float2(ahi[i][0], ahi[i][1]), x1);
+                    pk_cacc1(ch[1], cl[1], make_float2(ahi[i][2], ahi[i][3]), x1);
+                } else {
+                    pk_cacc2(ch[0], cl[0], make_float2(ahi[i][0], ahi[i][1]), make_float2(alo[i][0], alo[i][1]), x1);
+                    pk_cacc2(ch[1], cl[1], make_float2(ahi[i][2], ahi[i][3]), make_float2(alo[i][2], alo[i][3]), x1);
                 }
             }
         }
@@ -497,18 +407,21 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     if (opT) {
         float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw);
         float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw + 8 * kTileCols * 4);
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            rh[warp][lane_col<FMT>(lane, c)] = ch[c];
-            rl[warp][lane_col<FMT>(lane, c)] = cl[c];
-        }
+        rh[warp][lane_col<FMT>(lane, 0)] = ch[0].x;
+        rh[warp][lane_col<FMT>(lane, 1)] = ch[0].y;
+        rh[warp][lane_col<FMT>(lane, 2)] = ch[1].x;
+        rh[warp][lane_col<FMT>(lane, 3)] = ch[1].y;
+        rl[warp][lane_col<FMT>(lane, 0)] = cl[0].x;
+        rl[warp][lane_col<FMT>(lane, 1)] = cl[0].y;
+        rl[warp][lane_col<FMT>(lane, 2)] = cl[1].x;
+        rl[warp][lane_col<FMT>(lane, 3)] = cl[1].y;
         __syncthreads();
         double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
         for (int c = tid; c < nc; c += kTileThreads) {
             float h = rh[0][c], l = rl[0][c];
 #pragma unroll
             for (int w = 1; w < 8; w++) dfadd(h, l, rh[w][c], rl[w][c]);
-            atomicAdd(out1 + c, (double)h + (double)l);
+            atomic_add_pair(out1 + c, h, l);
         }
     }
 }
@@ -647,38 +560,37 @@ BlockLoc pack_block(Packer &pk, H2E_dense_mat_p m, int &lr_total, int fmt)
     return b;
 }
 
+/* Stored elements of a block, the reference's block size (nrow ncol, or
+ * (nrow + ncol) rank for a low-rank block; src/H2ERI_build_H2.c:869-900):
+ * the algorithmic traffic counts every stored element once per matvec. */
+double stored_elems(const BlockLoc &b)
+{
+    if (b.nrow == 0 || b.ncol == 0) return 0.0;
+    return b.lowrank ? (double)b.rank * (b.nrow + b.ncol) : (double)b.nrow * b.ncol;
+}
+
 /* Products of one block: N-side (out0 += A in0) and T-side (out1 += A^T in1);
  * kinds VK_NONE disable a side. Dense blocks are one bi-product pass. A
  * low-rank block A = U V takes three stages:
  *   1. t = V in0                    (N on V)
  *   2. s = U^T in1, out0 += U t     (one pass over Ut: N and T)
  *   3. out1 += V^T s                (T on V)
- * so U is read once and V twice (once when only the N side is wanted).
- * Returns the number of stored elements read. */
-double plan_block(Planner *st, const BlockLoc &b, uint8_t kin0, int in0, uint8_t kout0, int out0, uint8_t kin1,
-                  int in1, uint8_t kout1, int out1)
+ * so U is read once and V twice (once when only the N side is wanted). */
+void plan_block(Planner *st, const BlockLoc &b, uint8_t kin0, int in0, uint8_t kout0, int out0, uint8_t kin1,
+                int in1, uint8_t kout1, int out1)
 {
-    if (b.nrow == 0 || b.ncol == 0) return 0.0;
+    if (b.nrow == 0 || b.ncol == 0) return;
     if (!b.lowrank) {
         st[0].add(b.a, b.nrow, b.ncol, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
-        return (double)b.nrow * b.ncol;
+        return;
     }
     const int r = b.rank;
-    if (r == 0) return 0.0;
-    double elems = 0.0;
+    if (r == 0) return;
     const bool wantN = kout0 != VK_NONE, wantT = kout1 != VK_NONE;
-    if (wantN) {
-        st[0].add(b.v, r, b.ncol, kin0, in0, VK_T, b.t_off, VK_NONE, 0, VK_NONE, 0);
-        elems += (double)r * b.ncol;
-    }
+    if (wantN) st[0].add(b.v, r, b.ncol, kin0, in0, VK_T, b.t_off, VK_NONE, 0, VK_NONE, 0);
     st[1].add(b.ut, r, b.nrow, wantT ? kin1 : VK_NONE, in1, wantT ? VK_T : VK_NONE, b.s_off,
               wantN ? VK_T : VK_NONE, b.t_off, wantN ? kout0 : VK_NONE, out0);
-    elems += (double)r * b.nrow;
-    if (wantT) {
-        st[2].add(b.v, r, b.ncol, VK_NONE, 0, VK_NONE, 0, VK_T, b.s_off, kout1, out1);
-        elems += (double)r * b.ncol;
-    }
-    return elems;
+    if (wantT) st[2].add(b.v, r, b.ncol, VK_NONE, 0, VK_NONE, 0, VK_T, b.s_off, kout1, out1);
 }
 
 }  // namespace
@@ -813,11 +725,12 @@ static int build_rep(H2ERI_p h, DevRep *d)
             kin0 = VK_Y0; in0 = voff[n1]; kout0 = VK_Y; out0 = h->mat_cluster[2 * n0];
             kin1 = VK_X; in1 = h->mat_cluster[2 * n0]; kout1 = VK_Y1; out1 = voff[n1];
         }
-        double el = plan_block(midst, b, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
+        plan_block(midst, b, kin0, in0, kout0, out0, kin1, in1, kout1, out1);
+        const double el = stored_elems(b);
         mat_bytes += 8.0 * el;
         mat_bytes_mixed += 4.0 * el;
         vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
-        flops += 2.0 * el + 2.0 * (b.lowrank ? 0.0 : el);
+        flops += 4.0 * el;
     }
     d->bytes_B = (pk.host.size() - b_start) * sizeof(double);
     d->mid.clear();
@@ -854,20 +767,20 @@ static int build_rep(H2ERI_p h, DevRep *d)
         /* mixed mode keeps the leaf self-interaction blocks as float pairs */
         const bool diag = i < h->n_leaf_node;
         BlockLoc b = pack_block(pk, h->c_D_blks[i], d->lr_total, diag ? FMT_F32X2 : FMT_F32);
-        double el = 0.0;
+        const double el = stored_elems(b);
         if (diag) {
             int node = h->height_nodes[i];
             int off = h->mat_cluster[2 * node];
-            el = plan_block(dend, b, VK_X, off, VK_Y, off, VK_NONE, 0, VK_NONE, 0);
+            plan_block(dend, b, VK_X, off, VK_Y, off, VK_NONE, 0, VK_NONE, 0);
             vec_bytes += 8.0 * (b.nrow + b.ncol);
             flops += 2.0 * el;
         } else {
             int k = i - h->n_leaf_node;
             int n0 = h->r_inadm_pairs[2 * k], n1 = h->r_inadm_pairs[2 * k + 1];
             int o0 = h->mat_cluster[2 * n0], o1 = h->mat_cluster[2 * n1];
-            el = plan_block(deno, b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
+            plan_block(deno, b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
             vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
-            flops += 2.0 * el + 2.0 * (b.lowrank ? 0.0 : el);
+            flops += 4.0 * el;
         }
         mat_bytes += 8.0 * el;
         mat_bytes_mixed += (diag ? 8.0 : 4.0) * el;
