@@ -98,7 +98,6 @@ struct DevRep {
     std::vector<Range> mid;     /* coupling blocks, stages 1..3 */
     std::vector<Range> den;     /* near field, stages 1..3 (diagonal-pair, then single-float range per stage) */
     int rank_total = 0, lr_total = 0;
-    int tile_ctas[3] = {0, 0, 0};   /* resident k_tile CTAs per format (persistent grid) */
     /* algorithmic bytes / flops of one matvec (per vector), for reports */
     double alg_bytes_matrix = 0.0, alg_bytes_vec = 0.0, alg_flops = 0.0;
     /* J assembly maps */

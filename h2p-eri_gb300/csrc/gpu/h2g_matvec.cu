@@ -79,7 +79,6 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 template <int FMT> struct FmtInfo;
 template <> struct FmtInfo<FMT_F64> { static constexpr int ebytes = 8; };
@@ -207,168 +206,83 @@ __device__ __forceinline__ void reduceR_df(float *h, float *l, int lane, float &
     dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 1), __shfl_xor_sync(0xffffffffu, vl, 1));
 }
 
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem, int src_bytes)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
-}
-
-constexpr int kDescRing = 8;   /* tile descriptors in shared memory, prefetched two tiles ahead */
-
-/* Persistent tile kernel. CTA b of a launch with G CTAs takes tiles b,
- * b + G, b + 2G, ... of its range (sorted largest first). A tile is a chunk
- * of up to kChunkRows rows and kTileCols columns; its rows stream through a
- * kStages-deep ring of 32 KB shared-memory stages filled with cp.async
- * (16-byte copies, any leading dimension, zero fill past the tile edge). The
- * ring runs across tile boundaries: while stage c is multiplied, stages
- * c + 1 and c + 2 are in flight, whichever tiles they belong to, and with
- * the first stage of a tile go its input slices (raw doubles) and the
- * descriptor of the tile two ahead, so a CTA never waits on a cold start.
- * A stage holds SR = 64 rows of single floats or 32 rows of 8-byte
- * elements; warp w multiplies rows [w*SR/8, (w+1)*SR/8) and each lane owns
- * 4 columns (lane_col). N-side row sums are added per stage; T-side column
- * sums stay in registers over the whole tile and are added once.
+/* One CTA per (tile, vector). A tile is a chunk of up to kChunkRows rows and
+ * kTileCols columns. The chunk streams through a kStages-deep ring of 32 KB
+ * shared-memory stages filled with cp.async (16-byte copies, any leading
+ * dimension, zero fill past the tile edge), so the next stages are in flight
+ * while the current one is multiplied. A stage holds SR = 64 rows of single
+ * floats or 32 rows of 8-byte elements; warp w multiplies rows
+ * [w*SR/8, (w+1)*SR/8) and each lane owns 4 columns (lane_col).
+ * N-side row sums are added per stage; T-side column sums stay in registers
+ * over the whole chunk and are added once (few atomics per coefficient).
  *   FMT_F64   : FP64 FMAs, FP64 reductions.
  *   FMT_F32X2 : matrix stored as float pairs; products are error-free
- *               (pk_cacc2) and partial sums are float pairs, so the result
- *               keeps ~2^-48 relative accuracy while running on the FP32 pipe.
+ *               (cacc) and partial sums are float pairs, so the result keeps
+ *               ~2^-48 relative accuracy while running on the FP32 pipe.
  *   FMT_F32   : matrix stored as single floats (2^-24 storage rounding),
  *               products and sums as for float pairs, so the storage
  *               rounding is the only error (plain FP32 FMA chains roughly
  *               double it, measured 1.2e-8 vs 5e-9 on C10H22).
  * Inputs are split into float pairs once per tile in shared memory; every
- * output element is added to its FP64 vector with FP64 atomics. */
+ * output element is converted to FP64 once and added with an FP64 atomic. */
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
-k_tile(const Tile *__restrict__ tiles, int n_tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va)
+k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va)
 {
     constexpr int EB = FmtInfo<FMT>::ebytes;
     constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage   */
     constexpr int RW = SR / 8;                            /* rows per warp    */
     constexpr int RB = kTileCols * EB;                    /* bytes per row    */
-    constexpr int NX = kTileCols + kChunkRows;            /* input doubles per tile */
     extern __shared__ __align__(128) unsigned char stage_raw[];
-    __shared__ __align__(16) Tile sdesc[kDescRing];
-    __shared__ __align__(16) double xraw[2][NX];
-    /* inputs of the tile being multiplied: float pairs (FP32 formats) or the
-     * T-side doubles (FP64), copied out of xraw at the tile's first stage */
-    __shared__ __align__(16) float sxbuf[2 * kTileCols + 2 * kChunkRows];
-    float *sx0h = sxbuf, *sx0l = sxbuf + kTileCols, *sx1h = sxbuf + 2 * kTileCols,
-          *sx1l = sxbuf + 2 * kTileCols + kChunkRows;
-    double *x1d = reinterpret_cast<double *>(sxbuf);
+    __shared__ float sx0h[kTileCols], sx0l[kTileCols], sx1h[kChunkRows], sx1l[kChunkRows];
+    __shared__ __align__(16) unsigned char red_raw[8 * kTileCols * 8];
 
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const Tile t = tiles[blockIdx.x];
     const int v = blockIdx.y;
-    const int G = gridDim.x, b0 = blockIdx.x;
-    if (b0 >= n_tiles) return;
-    const int ntl = (n_tiles - b0 + G - 1) / G;   /* tiles of this CTA */
-    const unsigned char *arena = reinterpret_cast<const unsigned char *>(arena_v);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
+    const int nr = t.nr, nc = t.nc;
+    const int nstage = (nr + SR - 1) / SR;
+    const unsigned char *base = (FMT == FMT_F64)
+        ? reinterpret_cast<const unsigned char *>(reinterpret_cast<const double *>(arena_v) + t.a)
+        : (FMT == FMT_F32) ? reinterpret_cast<const unsigned char *>(reinterpret_cast<const float *>(arena_v) + t.a2)
+                           : reinterpret_cast<const unsigned char *>(reinterpret_cast<const float2 *>(arena_v) + t.a2);
+    const size_t ld_bytes = (size_t)((FMT == FMT_F64) ? t.ld : t.ld2) * EB;
+    const int nc_bytes16 = ((nc * EB) + 15) & ~15;
 
-    if (tid < 2 && tid < ntl) sdesc[tid] = tiles[b0 + tid * G];
-    __syncthreads();
+    /* prologue: first two stages in flight */
+    issue_stage<FMT>(stage_raw, base, ld_bytes, 0, nr, nc_bytes16, tid);
+    cp_async_commit();
+    if (nstage > 1) issue_stage<FMT>(stage_raw + kStageBytes, base, ld_bytes, SR, nr, nc_bytes16, tid);
+    cp_async_commit();
 
-    auto nstage_of = [&](const Tile &t) { return (t.nr + SR - 1) / SR; };
-    auto base_of = [&](const Tile &t) {
-        return arena + (FMT == FMT_F64 ? (size_t)t.a : (size_t)t.a2) * EB;
-    };
-    auto ldb_of = [&](const Tile &t) { return (size_t)((FMT == FMT_F64) ? t.ld : t.ld2) * EB; };
-
-    /* issue cursor: tile ik (local index), stage is; position pi */
-    int ik = 0, is = 0, pi = 0;
-    auto issue_next = [&]() {
-        if (ik < ntl) {
-            const Tile &t = sdesc[ik & (kDescRing - 1)];
-            if (is == 0) {
-                /* input slices of tile ik (zero outside the tile) */
-                double *xr = xraw[ik & 1];
-                const bool n0 = t.k_out0 != VK_NONE, n1 = t.k_out1 != VK_NONE;
-                const double *in0 = n0 ? vec_ptr(va, t.k_in0, t.in0, v) : nullptr;
-                const double *in1 = n1 ? vec_ptr(va, t.k_in1, t.in1, v) : nullptr;
-                for (int e = tid; e < NX; e += kTileThreads) {
-                    const double *src = in0;
-                    int ok = 0;
-                    if (e < kTileCols) {
-                        ok = n0 && e < t.nc;
-                        if (ok) src = in0 + e;
-                    } else {
-                        ok = n1 && e - kTileCols < t.nr;
-                        if (ok) src = in1 + (e - kTileCols);
-                    }
-                    cp_async8(&xr[e], ok ? (const void *)src : (const void *)tiles, ok ? 8 : 0);
-                }
-                /* descriptor of the tile two ahead */
-                if (ik + 2 < ntl && tid < (int)(sizeof(Tile) / 16))
-                    cp_async16(reinterpret_cast<unsigned char *>(&sdesc[(ik + 2) & (kDescRing - 1)]) + 16 * tid,
-                               reinterpret_cast<const unsigned char *>(&tiles[b0 + (ik + 2) * G]) + 16 * tid, 16);
-            }
-            const int nc_bytes16 = ((t.nc * EB) + 15) & ~15;
-            issue_stage<FMT>(stage_raw + (pi % kStages) * kStageBytes, base_of(t), ldb_of(t), is * SR, t.nr,
-                             nc_bytes16, tid);
-            if (++is == nstage_of(t)) {
-                is = 0;
-                ik++;
-            }
-        }
-        cp_async_commit();   /* possibly empty: one group per position keeps wait_group counts exact */
-        pi++;
-    };
-    issue_next();
-    issue_next();
-
-    /* consume cursor */
-    int ck = 0, cs = 0, cpos = 0;
-    /* per-tile state */
-    XIn xv[4];
-    double xd[4];
-    float2 ch[2], cl[2];
-    double acc[4];
-
-    while (ck < ntl) {
-        cp_async_wait1();
-        __syncthreads();
-        const Tile t = sdesc[ck & (kDescRing - 1)];
-        const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
-        const int nr = t.nr, nc = t.nc;
-        const int nstage = nstage_of(t);
-        const double *xr = xraw[ck & 1];
-        if (cs == 0) {
-            /* the raw inputs may be overwritten from the next position on:
-             * take what the tile needs out of xraw now */
-            if (FMT == FMT_F64) {
+    double *out0 = opN ? vec_ptr(va, t.k_out0, t.out0, v) : nullptr;
+    bool ok[4];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    xd[k] = xr[lane_col<FMT>(lane, k)];
-                    acc[k] = 0.0;
-                }
-                if (opT)
-                    for (int r = tid; r < kChunkRows; r += kTileThreads) x1d[r] = xr[kTileCols + r];
-            } else {
-                if (tid < kTileCols) {
-                    float h = 0.f, l = 0.f;
-                    if (opN && tid < nc) split(xr[tid], h, l);
-                    sx0h[tid] = h; sx0l[tid] = l;
-                }
-                if (opT)
-                    for (int r = tid; r < kChunkRows; r += kTileThreads) {
-                        float h = 0.f, l = 0.f;
-                        if (r < nr) split(xr[kTileCols + r], h, l);
-                        sx1h[r] = h; sx1l[r] = l;
-                    }
-            }
+    for (int k = 0; k < 4; k++) ok[k] = lane_col<FMT>(lane, k) < nc;
+    /* byte offsets of this lane's two 16-byte pieces inside a stage row */
+    const int offA = (FMT == FMT_F32) ? 16 * lane : 16 * lane;
+    const int offB = 512 + 16 * lane;   /* used by the 8-byte formats only */
+
+    if (FMT == FMT_F64) {
+        double xv[4] = {0.0, 0.0, 0.0, 0.0};
+        if (opN) {
+            const double *in0 = vec_ptr(va, t.k_in0, t.in0, v);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (ok[k]) xv[k] = in0[lane_col<FMT>(lane, k)];
+        }
+        const double *in1 = opT ? vec_ptr(va, t.k_in1, t.in1, v) : nullptr;
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int k = 0; k < nstage; k++) {
+            cp_async_wait1();
             __syncthreads();
-            if (FMT != FMT_F64) {
-#pragma unroll
-                for (int k = 0; k < 4; k++) xv[k] = xin(sx0h[lane_col<FMT>(lane, k)], sx0l[lane_col<FMT>(lane, k)]);
-                ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
-            }
-        }
-        issue_next();   /* position cpos + 2 (its ring slot was freed by the barrier above) */
-
-        unsigned char *buf = stage_raw + (cpos % kStages) * kStageBytes;
-        const int r0 = cs * SR + warp * RW;
-        double *out0 = opN ? vec_ptr(va, t.k_out0, t.out0, v) : nullptr;
-        const int offA = 16 * lane, offB = 512 + 16 * lane;
-        if (FMT == FMT_F64) {
+            if (k + 2 < nstage)
+                issue_stage<FMT>(stage_raw + ((k + 2) % kStages) * kStageBytes, base, ld_bytes, (k + 2) * SR, nr,
+                                 nc_bytes16, tid);
+            cp_async_commit();
+            const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
+            const int r0 = k * SR + warp * RW;
             double a[RW][4];
 #pragma unroll
             for (int i = 0; i < RW; i++) {
@@ -380,7 +294,7 @@ k_tile(const Tile *__restrict__ tiles, int n_tiles, const void *__restrict__ are
             if (opN) {
                 double sr[RW];
 #pragma unroll
-                for (int i = 0; i < RW; i++) sr[i] = a[i][0] * xd[0] + a[i][1] * xd[1] + a[i][2] * xd[2] + a[i][3] * xd[3];
+                for (int i = 0; i < RW; i++) sr[i] = a[i][0] * xv[0] + a[i][1] * xv[1] + a[i][2] * xv[2] + a[i][3] * xv[3];
                 const double val = reduceR_f64<RW>(sr, lane);
                 const int row = r0 + halving_row_R<RW>(lane);
                 if (halving_owner<RW>(lane) && row < nr) atomicAdd(out0 + row, val);
@@ -388,109 +302,128 @@ k_tile(const Tile *__restrict__ tiles, int n_tiles, const void *__restrict__ are
             if (opT) {
 #pragma unroll
                 for (int i = 0; i < RW; i++) {
-                    const double x1 = x1d[min(r0 + i, kChunkRows - 1)];
+                    const double x1 = (r0 + i < nr) ? in1[r0 + i] : 0.0;
 #pragma unroll
                     for (int c = 0; c < 4; c++) acc[c] += a[i][c] * x1;
                 }
             }
-        } else {
-            float ahi[RW][4], alo[RW][4];
-#pragma unroll
-            for (int i = 0; i < RW; i++) {
-                const unsigned char *row = buf + (warp * RW + i) * RB;
-                if (FMT == FMT_F32) {
-                    const float4 q = *reinterpret_cast<const float4 *>(row + offA);
-                    ahi[i][0] = q.x; ahi[i][1] = q.y; ahi[i][2] = q.z; ahi[i][3] = q.w;
-                } else {
-                    const float4 qa = *reinterpret_cast<const float4 *>(row + offA);
-                    const float4 qb = *reinterpret_cast<const float4 *>(row + offB);
-                    ahi[i][0] = qa.x; alo[i][0] = qa.y; ahi[i][1] = qa.z; alo[i][1] = qa.w;
-                    ahi[i][2] = qb.x; alo[i][2] = qb.y; ahi[i][3] = qb.z; alo[i][3] = qb.w;
-                }
-            }
-            if (opN) {
-                /* rows paired: halves of a float2 are rows 2u and 2u+1 */
-                float2 sh2[RW / 2], sl2[RW / 2];
-#pragma unroll
-                for (int u = 0; u < RW / 2; u++) {
-                    sh2[u] = sl2[u] = make_float2(0.f, 0.f);
-#pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        const float2 a = make_float2(ahi[2 * u][c], ahi[2 * u + 1][c]);
-                        if (FMT == FMT_F32) pk_cacc1(sh2[u], sl2[u], a, xv[c]);
-                        else pk_cacc2(sh2[u], sl2[u], a, make_float2(alo[2 * u][c], alo[2 * u + 1][c]), xv[c]);
-                    }
-                }
-                float sh[RW], sl[RW];
-#pragma unroll
-                for (int u = 0; u < RW / 2; u++) {
-                    sh[2 * u] = sh2[u].x; sh[2 * u + 1] = sh2[u].y;
-                    sl[2 * u] = sl2[u].x; sl[2 * u + 1] = sl2[u].y;
-                }
-                float vh, vl;
-                reduceR_df<RW>(sh, sl, lane, vh, vl);
-                const int row = r0 + halving_row_R<RW>(lane);
-                if (halving_owner<RW>(lane) && row < nr) atomic_add_pair(out0 + row, vh, vl);
-            }
-            if (opT) {
-#pragma unroll
-                for (int i = 0; i < RW; i++) {
-                    const int r = min(r0 + i, kChunkRows - 1);
-                    const XIn x1 = xin(sx1h[r], sx1l[r]);
-                    if (FMT == FMT_F32) {
-                        pk_cacc1(ch[0], cl[0], make_float2(ahi[i][0], ahi[i][1]), x1);
-                        pk_cacc1(ch[1], cl[1], make_float2(ahi[i][2], ahi[i][3]), x1);
-                    } else {
-                        pk_cacc2(ch[0], cl[0], make_float2(ahi[i][0], ahi[i][1]), make_float2(alo[i][0], alo[i][1]), x1);
-                        pk_cacc2(ch[1], cl[1], make_float2(ahi[i][2], ahi[i][3]), make_float2(alo[i][2], alo[i][3]), x1);
-                    }
-                }
-            }
         }
-
-        if (cs == nstage - 1 && opT) {
-            /* T-side column sums of the tile: reduce over the warps through
-             * the stage slot just consumed (next written two positions on) */
+        if (opT) {
+            double (*red)[kTileCols] = reinterpret_cast<double (*)[kTileCols]>(red_raw);
+#pragma unroll
+            for (int c = 0; c < 4; c++) red[warp][lane_col<FMT>(lane, c)] = acc[c];
             __syncthreads();
             double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
-            if (FMT == FMT_F64) {
-                double (*red)[kTileCols] = reinterpret_cast<double (*)[kTileCols]>(buf);
+            for (int c = tid; c < nc; c += kTileThreads) {
+                double sum = 0.0;
 #pragma unroll
-                for (int c = 0; c < 4; c++) red[warp][lane_col<FMT>(lane, c)] = acc[c];
-                __syncthreads();
-                for (int c = tid; c < nc; c += kTileThreads) {
-                    double sum = 0.0;
+                for (int w = 0; w < 8; w++) sum += red[w][c];
+                atomicAdd(out1 + c, sum);
+            }
+        }
+        return;
+    }
+
+    /* ---- FP32 formats: split the tile's input slices once ---- */
+    if (tid < kTileCols) {
+        float h = 0.f, l = 0.f;
+        if (opN && tid < nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
+        sx0h[tid] = h; sx0l[tid] = l;
+    }
+    for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
+        float h = 0.f, l = 0.f;
+        if (opT && r < nr) split(vec_ptr(va, t.k_in1, t.in1, v)[r], h, l);
+        sx1h[r] = h; sx1l[r] = l;
+    }
+    __syncthreads();
+    XIn xv[4];
 #pragma unroll
-                    for (int w = 0; w < 8; w++) sum += red[w][c];
-                    atomicAdd(out1 + c, sum);
-                }
+    for (int c = 0; c < 4; c++) xv[c] = xin(sx0h[lane_col<FMT>(lane, c)], sx0l[lane_col<FMT>(lane, c)]);
+    /* T-side column sums, columns paired (slots 0,1 and 2,3) */
+    float2 ch[2], cl[2];
+    ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
+    for (int k = 0; k < nstage; k++) {
+        cp_async_wait1();
+        __syncthreads();
+        if (k + 2 < nstage)
+            issue_stage<FMT>(stage_raw + ((k + 2) % kStages) * kStageBytes, base, ld_bytes, (k + 2) * SR, nr,
+                             nc_bytes16, tid);
+        cp_async_commit();
+        const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
+        const int r0 = k * SR + warp * RW;
+        float ahi[RW][4], alo[RW][4];
+#pragma unroll
+        for (int i = 0; i < RW; i++) {
+            const unsigned char *row = buf + (warp * RW + i) * RB;
+            if (FMT == FMT_F32) {
+                const float4 q = *reinterpret_cast<const float4 *>(row + offA);
+                ahi[i][0] = q.x; ahi[i][1] = q.y; ahi[i][2] = q.z; ahi[i][3] = q.w;
             } else {
-                float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(buf);
-                float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(buf + 8 * kTileCols * 4);
-                rh[warp][lane_col<FMT>(lane, 0)] = ch[0].x;
-                rh[warp][lane_col<FMT>(lane, 1)] = ch[0].y;
-                rh[warp][lane_col<FMT>(lane, 2)] = ch[1].x;
-                rh[warp][lane_col<FMT>(lane, 3)] = ch[1].y;
-                rl[warp][lane_col<FMT>(lane, 0)] = cl[0].x;
-                rl[warp][lane_col<FMT>(lane, 1)] = cl[0].y;
-                rl[warp][lane_col<FMT>(lane, 2)] = cl[1].x;
-                rl[warp][lane_col<FMT>(lane, 3)] = cl[1].y;
-                __syncthreads();
-                for (int c = tid; c < nc; c += kTileThreads) {
-                    float h = rh[0][c], l = rl[0][c];
+                const float4 qa = *reinterpret_cast<const float4 *>(row + offA);
+                const float4 qb = *reinterpret_cast<const float4 *>(row + offB);
+                ahi[i][0] = qa.x; alo[i][0] = qa.y; ahi[i][1] = qa.z; alo[i][1] = qa.w;
+                ahi[i][2] = qb.x; alo[i][2] = qb.y; ahi[i][3] = qb.z; alo[i][3] = qb.w;
+            }
+        }
+        if (opN) {
+            /* rows paired: halves of a float2 are rows 2u and 2u+1 */
+            float2 sh2[RW / 2], sl2[RW / 2];
 #pragma unroll
-                    for (int w = 1; w < 8; w++) dfadd(h, l, rh[w][c], rl[w][c]);
-                    atomic_add_pair(out1 + c, h, l);
+            for (int u = 0; u < RW / 2; u++) {
+                sh2[u] = sl2[u] = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float2 a = make_float2(ahi[2 * u][c], ahi[2 * u + 1][c]);
+                    if (FMT == FMT_F32) pk_cacc1(sh2[u], sl2[u], a, xv[c]);
+                    else pk_cacc2(sh2[u], sl2[u], a, make_float2(alo[2 * u][c], alo[2 * u + 1][c]), xv[c]);
+                }
+            }
+            float sh[RW], sl[RW];
+#pragma unroll
+            for (int u = 0; u < RW / 2; u++) {
+                sh[2 * u] = sh2[u].x; sh[2 * u + 1] = sh2[u].y;
+                sl[2 * u] = sl2[u].x; sl[2 * u + 1] = sl2[u].y;
+            }
+            float vh, vl;
+            reduceR_df<RW>(sh, sl, lane, vh, vl);
+            const int row = r0 + halving_row_R<RW>(lane);
+            if (halving_owner<RW>(lane) && row < nr) atomic_add_pair(out0 + row, vh, vl);
+        }
+        if (opT) {
+#pragma unroll
+            for (int i = 0; i < RW; i++) {
+                const int r = min(r0 + i, kChunkRows - 1);
+                const XIn x1 = xin(sx1h[r], sx1l[r]);
+                if (FMT == FMT_F32) {
+                    pk_cacc1(ch[0], cl[0], make_float2(ahi[i][0], ahi[i][1]), x1);
+                    pk_cacc1(ch[1], cl[1], make_float2(ahi[i][2], ahi[i][3]), x1);
+                } else {
+                    pk_cacc2(ch[0], cl[0], make_float2(ahi[i][0], ahi[i][1]), make_float2(alo[i][0], alo[i][1]), x1);
+                    pk_cacc2(ch[1], cl[1], make_float2(ahi[i][2], ahi[i][3]), make_float2(alo[i][2], alo[i][3]), x1);
                 }
             }
         }
-        cpos++;
-        if (++cs == nstage) {
-            cs = 0;
-            ck++;
+    }
+    if (opT) {
+        float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw);
+        float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw + 8 * kTileCols * 4);
+        rh[warp][lane_col<FMT>(lane, 0)] = ch[0].x;
+        rh[warp][lane_col<FMT>(lane, 1)] = ch[0].y;
+        rh[warp][lane_col<FMT>(lane, 2)] = ch[1].x;
+        rh[warp][lane_col<FMT>(lane, 3)] = ch[1].y;
+        rl[warp][lane_col<FMT>(lane, 0)] = cl[0].x;
+        rl[warp][lane_col<FMT>(lane, 1)] = cl[0].y;
+        rl[warp][lane_col<FMT>(lane, 2)] = cl[1].x;
+        rl[warp][lane_col<FMT>(lane, 3)] = cl[1].y;
+        __syncthreads();
+        double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
+        for (int c = tid; c < nc; c += kTileThreads) {
+            float h = rh[0][c], l = rl[0][c];
+#pragma unroll
+            for (int w = 1; w < 8; w++) dfadd(h, l, rh[w][c], rl[w][c]);
+            atomic_add_pair(out1 + c, h, l);
         }
     }
-    cp_async_wait0();
 }
 
 /* x[v][i] = c_i * D[v][map_i >> 1], c_i = 2 for off-diagonal shell pairs
@@ -576,18 +509,6 @@ struct Packer {
         return m;
     }
 };
-
-/* Append a planner's tiles as one launch range, largest first (CTAs of the
- * persistent tile kernel take every G-th tile). */
-Range append_range(std::vector<Tile> &all, std::vector<Tile> &tiles, bool pair)
-{
-    std::stable_sort(tiles.begin(), tiles.end(), [](const Tile &x, const Tile &y) {
-        return (int)x.nr * x.nc > (int)y.nr * y.nc;
-    });
-    Range r{(int)all.size(), (int)tiles.size(), pair};
-    all.insert(all.end(), tiles.begin(), tiles.end());
-    return r;
-}
 
 struct Planner {
     std::vector<Tile> tiles;
@@ -781,7 +702,9 @@ static int build_rep(H2ERI_p h, DevRep *d)
             vec_bytes += 8.0 * (U->nrow + U->ncol);
             flops += 2.0 * U->nrow * U->ncol;
         }
-        d->fwd.push_back(append_range(all, p.tiles, true));
+        Range r{(int)all.size(), (int)p.tiles.size(), true};
+        all.insert(all.end(), p.tiles.begin(), p.tiles.end());
+        d->fwd.push_back(r);
     }
 
     /* coupling blocks (src/H2ERI_matvec.c:299-407) */
@@ -812,7 +735,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
     d->bytes_B = (pk.host.size() - b_start) * sizeof(double);
     d->mid.clear();
     for (int k = 0; k < 3; k++) {
-        d->mid.push_back(append_range(all, midst[k].tiles, false));
+        d->mid.push_back(Range{(int)all.size(), (int)midst[k].tiles.size(), false});
+        all.insert(all.end(), midst[k].tiles.begin(), midst[k].tiles.end());
     }
 
     /* downward sweep, shallowest level first (src/H2ERI_matvec.c:679-738) */
@@ -832,7 +756,9 @@ static int build_rep(H2ERI_p h, DevRep *d)
             vec_bytes += 8.0 * (U->nrow + U->ncol);
             flops += 2.0 * U->nrow * U->ncol;
         }
-        d->bwd.push_back(append_range(all, p.tiles, true));
+        Range r{(int)all.size(), (int)p.tiles.size(), true};
+        all.insert(all.end(), p.tiles.begin(), p.tiles.end());
+        d->bwd.push_back(r);
     }
 
     /* near field (src/H2ERI_matvec.c:572-660) */
@@ -864,7 +790,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
     for (int k = 0; k < 3; k++)
         for (int pair = 1; pair >= 0; pair--) {
             Planner &p = pair ? dend[k] : deno[k];
-            d->den.push_back(append_range(all, p.tiles, pair == 1));
+            d->den.push_back(Range{(int)all.size(), (int)p.tiles.size(), pair == 1});
+            all.insert(all.end(), p.tiles.begin(), p.tiles.end());
         }
 
     d->alg_bytes_matrix = mat_bytes;
@@ -905,20 +832,6 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
-    {
-        int nsm = 0, per[3] = {0, 0, 0};
-        CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, d->device));
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[FMT_F64], k_tile<FMT_F64>, kTileThreads, kTileSmem));
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[FMT_F32], k_tile<FMT_F32>, kTileThreads, kTileSmem));
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[FMT_F32X2], k_tile<FMT_F32X2>, kTileThreads, kTileSmem));
-        for (int f = 0; f < 3; f++) {
-            if (per[f] < 1) {
-                set_error("k_tile does not fit on an SM");
-                return 10;
-            }
-            d->tile_ctas[f] = per[f] * nsm;
-        }
-    }
     /* The tree sweeps are a chain of dependent launches (the critical path);
      * the near field is one large independent batch. Giving the chain's
      * stream the higher priority lets near-field tiles fill only the SMs the
@@ -995,15 +908,13 @@ static int ensure_work(DevRep *d, int nvec)
 static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s)
 {
     if (r.count == 0) return;
-    const int fmt = d->precision == H2ERI_GPU_FP64 ? FMT_F64 : (r.pair ? FMT_F32X2 : FMT_F32);
-    /* persistent: at most as many CTAs as are resident at once */
-    dim3 grid(std::min(r.count, std::max(1, d->tile_ctas[fmt])), nvec);
-    if (fmt == FMT_F64)
-        k_tile<FMT_F64><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, r.count, d->arena, va);
-    else if (fmt == FMT_F32X2)
-        k_tile<FMT_F32X2><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, r.count, d->arena32x2, va);
+    dim3 grid(r.count, nvec);
+    if (d->precision == H2ERI_GPU_FP64)
+        k_tile<FMT_F64><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena, va);
+    else if (r.pair)
+        k_tile<FMT_F32X2><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena32x2, va);
     else
-        k_tile<FMT_F32><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, r.count, d->arena32, va);
+        k_tile<FMT_F32><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena32, va);
 }
 
 /* Fill the mixed arenas from the host blocks (first use of mixed mode). */
