@@ -114,11 +114,33 @@ __device__ __forceinline__ void dfadd(float &ah, float &al, float bh, float bl)
     al = __fadd_rn(__fadd_rn(al, bl), err);
 }
 
-/* double -> float pair (hi = nearest float, lo = nearest float of the rest). */
+/* Two float-pair additions at once (halves independent). */
+__device__ __forceinline__ void pk_dfadd(float2 &ah, float2 &al, float2 bh, float2 bl)
+{
+    const float2 s = pk_add(ah, bh);
+    const float2 bp = pk_sub(s, ah);
+    const float2 err = pk_add(pk_sub(ah, pk_sub(s, bp)), pk_sub(bh, bp));
+    ah = s;
+    al = pk_add(pk_add(al, bl), err);
+}
+
+/* double -> float pair without FP64 arithmetic: hi keeps the sign, the
+ * exponent and the leading 24 significant bits of x (truncated), lo is the
+ * remaining 29 bits of the significand rounded to a float and scaled by a
+ * power of two, so |x - (hi + lo)| <= 2^-47 |x|. Magnitudes below 2^-126
+ * (hi) or 2^-74 (lo) are flushed to zero; no value here comes near either. */
 __device__ __forceinline__ void split(double x, float &hi, float &lo)
 {
-    hi = __double2float_rn(x);
-    lo = __double2float_rn(x - (double)hi);
+    const unsigned bh = (unsigned)__double2hiint(x), bl = (unsigned)__double2loint(x);
+    const unsigned sign = bh & 0x80000000u;
+    const int e = (int)((bh >> 20) & 0x7ffu);     /* biased double exponent */
+    const int fe = e - 896;                        /* biased float exponent of hi */
+    const bool ok = fe >= 1 && fe <= 254;
+    hi = __uint_as_float(ok ? (sign | ((unsigned)fe << 23) | ((bh & 0xfffffu) << 3) | (bl >> 29)) : sign);
+    const int le = e - 948;                        /* biased float exponent of 2^(e - 1075) */
+    const float m = __uint2float_rn(bl & 0x1fffffffu);
+    const float l = (ok && le >= 1) ? m * __uint_as_float((unsigned)le << 23) : 0.0f;
+    lo = __uint_as_float(__float_as_uint(l) | sign);
 }
 
 /* Exact float -> double by integer operations (keeps the conversion off the

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -374,8 +375,11 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
                     const float2 a = make_float2(ahi[2 * u][c], ahi[2 * u + 1][c]);
-                    if (FMT == FMT_F32) pk_cacc1(sh2[u], sl2[u], a, xv[c]);
-                    else pk_cacc2(sh2[u], sl2[u], a, make_float2(alo[2 * u][c], alo[2 * u + 1][c]), xv[c]);
+                    if (FMT == FMT_F32) {
+                        pk_cacc1(sh2[u], sl2[u], a, xv[c]);
+                    } else {
+                        pk_cacc2(sh2[u], sl2[u], a, make_float2(alo[2 * u][c], alo[2 * u + 1][c]), xv[c]);
+                    }
                 }
             }
             float sh[RW], sl[RW];
