@@ -88,7 +88,8 @@ template <> struct FmtInfo<FMT_F32X2> { static constexpr int ebytes = 8; };
 
 /* Issue the copies of one stage: rows [row0, row0 + SR) of the tile, all
  * kTileCols columns, into a dense SR x (kTileCols * ebytes) smem block. Rows
- * at or beyond nr and columns beyond the tile are zero-filled. */
+ * at or beyond nr that a warp with rows inside the tile reads, and columns
+ * beyond the tile, are zero-filled. */
 template <int FMT>
 __device__ __forceinline__ void issue_stage(unsigned char *buf, const unsigned char *base, size_t ld_bytes, int row0,
                                             int nr, int nc_bytes16, int tid)
@@ -101,6 +102,9 @@ __device__ __forceinline__ void issue_stage(unsigned char *buf, const unsigned c
         const int c = tid + j * kTileThreads;
         const int row = c / CPR, cc = c - row * CPR;
         const int grow = row0 + row;
+        /* rows of warps that have no row inside the tile are never read */
+        constexpr int RW = kStageBytes / RB / 8;
+        if (row0 + (row / RW) * RW >= nr) continue;
         int valid = 0;
         const unsigned char *src = base;
         if (grow < nr) {
@@ -284,6 +288,7 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
             cp_async_commit();
             const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
             const int r0 = k * SR + warp * RW;
+            if (r0 >= nr) continue;   /* no row of this warp in the tile (warp-uniform) */
             double a[RW][4];
 #pragma unroll
             for (int i = 0; i < RW; i++) {
@@ -352,6 +357,7 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
         cp_async_commit();
         const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
         const int r0 = k * SR + warp * RW;
+        if (r0 >= nr) continue;   /* no row of this warp in the tile (warp-uniform) */
         float ahi[RW][4], alo[RW][4];
 #pragma unroll
         for (int i = 0; i < RW; i++) {
