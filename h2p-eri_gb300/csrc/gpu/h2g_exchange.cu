@@ -82,15 +82,15 @@ struct GemmTask {
     int c64;
 };
 
-constexpr int kGThreads = 256;
-
-/* Tile shapes: FP64 64 x 64 (4 x 4 per thread, FP64-pipe bound), FP32
- * 128 x 128 (8 x 8 per thread, so shared-memory traffic stays at one byte
- * per FMA). 16 x 16 threads, k-steps of 16. */
+/* Tile shapes: FP64 64 x 64 (256 threads as 16 x 16, 4 x 4 per thread,
+ * FP64-pipe bound), FP32 128 x 128 (512 threads as 16 x 32, 4 x 8 per
+ * thread: twice the warps of an 8 x 8 layout, for more loads in flight).
+ * k-steps of 16. */
 template <typename T> struct GemmCfg;
-template <> struct GemmCfg<double> { static constexpr int TM = 64, TN = 64; };
-template <> struct GemmCfg<float> { static constexpr int TM = 128, TN = 128; };
+template <> struct GemmCfg<double> { static constexpr int TM = 64, TN = 64, NT = 256; };
+template <> struct GemmCfg<float> { static constexpr int TM = 128, TN = 128, NT = 512; };
 constexpr int kGK = 16;
+constexpr int kGThreads = 256;   /* threads of the FP64 variant */
 
 template <typename T>
 __host__ __device__ constexpr long long gemm_tiles(int M, int N, int Z)
@@ -100,13 +100,18 @@ __host__ __device__ constexpr long long gemm_tiles(int M, int N, int Z)
 }
 
 /* One CTA per TM x TN output tile; tile_start[t] is the first tile of task t
- * (prefix sums, tile_start[n_task] = total). */
+ * (prefix sums, tile_start[n_task] = total). The operands are gathered
+ * through index lists, so every k-step costs two dependent trips to L2
+ * (index, then value): the indices are loaded two k-steps ahead and the
+ * values one k-step ahead, both while the current step's FMAs run. */
 template <typename T>
-__global__ void __launch_bounds__(kGThreads) k_gemm(const GemmTask *__restrict__ tasks,
-                                                     const long long *__restrict__ tile_start, int n_task)
+__global__ void __launch_bounds__(GemmCfg<T>::NT) k_gemm(const GemmTask *__restrict__ tasks,
+                                                          const long long *__restrict__ tile_start, int n_task)
 {
-    constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN, RM = TM / 16, RN = TN / 16;
-    constexpr int UA = TM * kGK / kGThreads, UB = TN * kGK / kGThreads;
+    constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN, NT = GemmCfg<T>::NT;
+    constexpr int TY = NT / 16;                      /* thread rows */
+    constexpr int RM = TM / TY, RN = TN / 16;
+    constexpr int UA = TM * kGK / NT, UB = TN * kGK / NT;
     __shared__ T As[kGK][TM + 4];
     __shared__ T Bs[kGK][TN + 4];
     const long long tile = blockIdx.x;
@@ -125,13 +130,14 @@ __global__ void __launch_bounds__(kGThreads) k_gemm(const GemmTask *__restrict__
     const T *Ap = reinterpret_cast<const T *>(Tk.a.p);
     const T *Bp = reinterpret_cast<const T *>(Tk.b.p);
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int K = Tk.K;
 
     /* operand offsets that stay fixed over k */
     const int ka = tid % kGK;                       /* k of this thread's A loads  */
     long long aro[UA];
 #pragma unroll
     for (int u = 0; u < UA; u++) {
-        int gi = m0 + (tid + u * kGThreads) / kGK;
+        int gi = m0 + (tid + u * NT) / kGK;
         aro[u] = gi < Tk.M ? (Tk.a.gr ? (long long)Tk.a.gr[gi] : (long long)gi) * Tk.a.sr : -1;
     }
     const int jb = tid % TN;                        /* column of this thread's B loads */
@@ -146,37 +152,53 @@ __global__ void __launch_bounds__(kGThreads) k_gemm(const GemmTask *__restrict__
             bco = -1;
         }
     }
+    /* gather offsets of one k-step: A column (one per thread), B rows */
+    auto load_idx = [&](int k0, long long &ia, long long (&ib)[UB]) {
+        const int gk = k0 + ka;
+        ia = gk < K ? (Tk.a.gc ? (long long)Tk.a.gc[gk] : (long long)gk) * Tk.a.sc : -1;
+#pragma unroll
+        for (int u = 0; u < UB; u++) {
+            const int gkb = k0 + (tid + u * NT) / TN;
+            ib[u] = gkb < K ? (Tk.b.gr ? (long long)Tk.b.gr[gkb] : (long long)gkb) * Tk.b.sr : -1;
+        }
+    };
+    auto load_val = [&](const long long ia, const long long (&ib)[UB], T (&ra)[UA], T (&rb)[UB]) {
+#pragma unroll
+        for (int u = 0; u < UA; u++) ra[u] = (aro[u] >= 0 && ia >= 0) ? Ap[aro[u] + ia] : T(0);
+#pragma unroll
+        for (int u = 0; u < UB; u++) rb[u] = (bco >= 0 && ib[u] >= 0) ? Bp[bco + ib[u]] : T(0);
+    };
+
     T acc[RM][RN];
 #pragma unroll
     for (int a = 0; a < RM; a++)
 #pragma unroll
         for (int b = 0; b < RN; b++) acc[a][b] = T(0);
 
-    for (int k0 = 0; k0 < Tk.K; k0 += kGK) {
-        {
-            const int gk = k0 + ka;
-            const long long kc = gk < Tk.K ? (Tk.a.gc ? (long long)Tk.a.gc[gk] : (long long)gk) * Tk.a.sc : 0;
+    long long ia0, ib0[UB], ia1, ib1[UB];
+    T ra[UA], rb[UB];
+    load_idx(0, ia0, ib0);
+    load_idx(kGK, ia1, ib1);
+    load_val(ia0, ib0, ra, rb);
+    for (int k0 = 0; k0 < K; k0 += kGK) {
 #pragma unroll
-            for (int u = 0; u < UA; u++) {
-                const int ii = (tid + u * kGThreads) / kGK;
-                As[ka][ii] = (aro[u] >= 0 && gk < Tk.K) ? Ap[aro[u] + kc] : T(0);
-            }
-        }
+        for (int u = 0; u < UA; u++) As[ka][(tid + u * NT) / kGK] = ra[u];
 #pragma unroll
-        for (int u = 0; u < UB; u++) {
-            const int kb = (tid + u * kGThreads) / TN;
-            const int gk = k0 + kb;
-            T v = T(0);
-            if (bco >= 0 && gk < Tk.K)
-                v = Bp[bco + (Tk.b.gr ? (long long)Tk.b.gr[gk] : (long long)gk) * Tk.b.sr];
-            Bs[kb][jb] = v;
-        }
+        for (int u = 0; u < UB; u++) Bs[(tid + u * NT) / TN][jb] = rb[u];
         __syncthreads();
+        /* next step's values (indices already here), the step after's indices */
+        if (k0 + kGK < K) {
+            load_val(ia1, ib1, ra, rb);
+            ia0 = ia1;
+#pragma unroll
+            for (int u = 0; u < UB; u++) ib0[u] = ib1[u];
+            load_idx(k0 + 2 * kGK, ia1, ib1);
+        }
 #pragma unroll
         for (int kk = 0; kk < kGK; kk++) {
             T av[RM], bv[RN];
 #pragma unroll
-            for (int a = 0; a < RM; a++) av[a] = As[kk][ty + 16 * a];
+            for (int a = 0; a < RM; a++) av[a] = As[kk][ty + TY * a];
 #pragma unroll
             for (int b = 0; b < RN; b++) bv[b] = Bs[kk][tx + 16 * b];
 #pragma unroll
@@ -200,7 +222,7 @@ __global__ void __launch_bounds__(kGThreads) k_gemm(const GemmTask *__restrict__
     }
 #pragma unroll
     for (int a = 0; a < RM; a++) {
-        int gi = m0 + ty + 16 * a;
+        int gi = m0 + ty + TY * a;
         if (gi >= Tk.M) continue;
         long long ro = (Tk.c.gr ? (long long)Tk.c.gr[gi] : (long long)gi) * Tk.c.sr;
 #pragma unroll
@@ -1007,7 +1029,7 @@ static int enqueue_typed(KState *ks, const double *den, cudaStream_t s)
         for (const KGroup &g : ch.groups) {
             const long long tiles = v.group_tiles[gi];
             if (tiles > 0)
-                k_gemm<T><<<(unsigned)tiles, kGThreads, 0, s>>>(v.tasks + g.t0, v.tile_start + v.group_pre[gi], g.nt);
+                k_gemm<T><<<(unsigned)tiles, GemmCfg<T>::NT, 0, s>>>(v.tasks + g.t0, v.tile_start + v.group_pre[gi], g.nt);
             gi++;
         }
     }
