@@ -50,6 +50,9 @@ WORKLOADS = {
 }
 WORKLOAD = dict(WORKLOADS["c30"])
 METRIC = "J builds/s C30H62 (mixed vs FP64) at relerr<=1e-8"
+# DRAM bytes (read + write) of all tile-kernel launches of one mixed C30H62 J
+# build, from one ncu capture (profiles/k_tile_C30H62_mixed_launches_traffic.md)
+TRAFFIC_J_MIXED_C30 = 1739.5e6
 METRIC_K = "K builds/s (H2ERI_build_exchange path)"
 CACHE_DIR = os.path.join(tempfile.gettempdir(), "h2eri_gb300_cache")
 
@@ -479,8 +482,11 @@ def run_gpu(args):
         "e2e": {"value": ws * args.steps / e2e_s, "unit": "J builds/s", "h2d_bytes_per_step": 8 * nbf * nbf,
                 "d2h_bytes_per_step": 8 * nbf * nbf},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "k_tile (all tile launches of one J build)",
-                     "alg_bytes_per_step": alg_bytes, "peak_kind": peak_kind},
+                     "traffic": (TRAFFIC_J_MIXED_C30 if best == "mixed" and WORKLOAD["n_carbon"] == 30 else None),
+                     "kernel": "k_tile (all tile launches of one J build)",
+                     "alg_bytes_per_step": alg_bytes, "peak_kind": peak_kind,
+                     "note": "achieved and traffic are per J build (all tile launches); the mixed tile kernels "
+                             "are FP32-pipe bound (compensated products), see profiles/"},
         "cpu_baseline": {"value": cpu_v, "unit": "J builds/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": f"{cpu_n} J builds of the workload in {cpu_dt:.1f} s (oracle, OpenMP)"},
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
