@@ -89,7 +89,10 @@ template <> struct FmtInfo<FMT_F32X2> { static constexpr int ebytes = 8; };
 /* Issue the copies of one stage: rows [row0, row0 + SR) of the tile, all
  * kTileCols columns, into a dense SR x (kTileCols * ebytes) smem block. Rows
  * at or beyond nr that a warp with rows inside the tile reads, and columns
- * beyond the tile, are zero-filled. */
+ * beyond the tile, are zero-filled. In the FP32 formats the 16-byte chunk cc
+ * of stage row r goes to chunk position cc ^ (r & 31) of that row, so that
+ * 32 lanes reading one chunk column of 32 rows hit distinct banks (the
+ * lane-per-row N side) as well as 32 lanes reading one row. */
 template <int FMT>
 __device__ __forceinline__ void issue_stage(unsigned char *buf, const unsigned char *base, size_t ld_bytes, int row0,
                                             int nr, int nc_bytes16, int tid)
@@ -97,21 +100,23 @@ __device__ __forceinline__ void issue_stage(unsigned char *buf, const unsigned c
     constexpr int RB = kTileCols * FmtInfo<FMT>::ebytes;   /* bytes per stage row */
     constexpr int CPR = RB / 16;                            /* 16-byte chunks per row */
     constexpr int NCH = kStageBytes / 16;
+    /* rows never read (their warps have no row in the tile) are not copied:
+     * FP64 reads 8-row blocks per warp, the FP32 formats 32-row groups */
+    constexpr int RGRP = (FMT == FMT_F64) ? kStageBytes / RB / 8 : 32;
 #pragma unroll
     for (int j = 0; j < NCH / kTileThreads; j++) {
         const int c = tid + j * kTileThreads;
         const int row = c / CPR, cc = c - row * CPR;
         const int grow = row0 + row;
-        /* rows of warps that have no row inside the tile are never read */
-        constexpr int RW = kStageBytes / RB / 8;
-        if (row0 + (row / RW) * RW >= nr) continue;
+        if (row0 + (row / RGRP) * RGRP >= nr) continue;
+        const int pos = (FMT == FMT_F64) ? cc : (cc ^ (row & 31));
         int valid = 0;
         const unsigned char *src = base;
         if (grow < nr) {
             valid = min(16, max(0, nc_bytes16 - cc * 16));
             if (valid > 0) src = base + (size_t)grow * ld_bytes + cc * 16;
         }
-        cp_async16(buf + c * 16, src, valid);
+        cp_async16(buf + (size_t)row * RB + pos * 16, src, valid);
     }
 }
 
@@ -239,8 +244,10 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     constexpr int RW = SR / 8;                            /* rows per warp    */
     constexpr int RB = kTileCols * EB;                    /* bytes per row    */
     extern __shared__ __align__(128) unsigned char stage_raw[];
-    __shared__ float sx0h[kTileCols], sx0l[kTileCols], sx1h[kChunkRows], sx1l[kChunkRows];
-    __shared__ __align__(16) unsigned char red_raw[8 * kTileCols * 8];
+    __shared__ __align__(16) float sx0h[kTileCols], sx0l[kTileCols], sx0n[kTileCols];
+    __shared__ float sx1h[kChunkRows], sx1l[kChunkRows];
+    /* N-side row partials of the FP32 formats, [stage parity][column group * SR + row] */
+    __shared__ __align__(16) float2 npart[2][256];
 
     const Tile t = tiles[blockIdx.x];
     const int v = blockIdx.y;
@@ -315,7 +322,10 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
             }
         }
         if (opT) {
-            double (*red)[kTileCols] = reinterpret_cast<double (*)[kTileCols]>(red_raw);
+            /* reduce over the warps through the last stage's slot (no copy is pending into it) */
+            __syncthreads();
+            double (*red)[kTileCols] =
+                reinterpret_cast<double (*)[kTileCols]>(stage_raw + ((nstage - 1) % kStages) * kStageBytes);
 #pragma unroll
             for (int c = 0; c < 4; c++) red[warp][lane_col<FMT>(lane, c)] = acc[c];
             __syncthreads();
@@ -334,89 +344,109 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     if (tid < kTileCols) {
         float h = 0.f, l = 0.f;
         if (opN && tid < nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
-        sx0h[tid] = h; sx0l[tid] = l;
+        sx0h[tid] = h; sx0l[tid] = l; sx0n[tid] = -h;
     }
-    for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
-        float h = 0.f, l = 0.f;
-        if (opT && r < nr) split(vec_ptr(va, t.k_in1, t.in1, v)[r], h, l);
-        sx1h[r] = h; sx1l[r] = l;
-    }
+    if (opT)
+        for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
+            float h = 0.f, l = 0.f;
+            if (r < nr) split(vec_ptr(va, t.k_in1, t.in1, v)[r], h, l);
+            sx1h[r] = h; sx1l[r] = l;
+        }
     __syncthreads();
-    XIn xv[4];
+
+    /* N side: lane-per-row. A stage's SR rows form NG groups of 32; the
+     * warps of a group split the row's 16-byte chunks (CPW each), every lane
+     * accumulates its row over its chunks as even/odd column pairs, and the
+     * NCG column-group partials of a row are merged once per stage. */
+    constexpr int RC = RB / 16;        /* chunks per row: 32 (F32) or 64 (pairs) */
+    constexpr int NG = SR / 32;        /* 32-row groups per stage               */
+    constexpr int NCG = 8 / NG;        /* column groups (warps) per row group   */
+    constexpr int CPW = RC / NCG;      /* chunks per warp: 8                    */
+    const int ng = warp % NG, cg = warp / NG;
+    auto merge_rows = [&](int k) {     /* partials of stage k -> out0 */
+        if (tid < SR) {
+            const int grow = k * SR + tid;
+            if (grow < nr) {
+                const float2 *P = npart[k & 1];
+                float h = P[tid].x, l = P[tid].y;
 #pragma unroll
-    for (int c = 0; c < 4; c++) xv[c] = xin(sx0h[lane_col<FMT>(lane, c)], sx0l[lane_col<FMT>(lane, c)]);
-    /* T-side column sums, columns paired (slots 0,1 and 2,3) */
+                for (int g = 1; g < NCG; g++) dfadd(h, l, P[g * SR + tid].x, P[g * SR + tid].y);
+                atomic_add_pair(out0 + grow, h, l);
+            }
+        }
+    };
+
+    /* T side: warp w takes rows [w*RW, (w+1)*RW) of a stage, each lane 4 columns
+     * (lane_col); column pairs (slots 0,1 and 2,3) accumulate as float pairs */
     float2 ch[2], cl[2];
     ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
     for (int k = 0; k < nstage; k++) {
         cp_async_wait1();
         __syncthreads();
+        if (opN && k > 0) merge_rows(k - 1);
         if (k + 2 < nstage)
             issue_stage<FMT>(stage_raw + ((k + 2) % kStages) * kStageBytes, base, ld_bytes, (k + 2) * SR, nr,
                              nc_bytes16, tid);
         cp_async_commit();
         const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
-        const int r0 = k * SR + warp * RW;
-        if (r0 >= nr) continue;   /* no row of this warp in the tile (warp-uniform) */
-        float ahi[RW][4], alo[RW][4];
+
+        if (opN && k * SR + ng * 32 < nr) {
+            const int rr = ng * 32 + lane;
+            const unsigned char *rowp = buf + (size_t)rr * RB;
+            float2 sh = make_float2(0.f, 0.f), sl = sh;
 #pragma unroll
-        for (int i = 0; i < RW; i++) {
-            const unsigned char *row = buf + (warp * RW + i) * RB;
-            if (FMT == FMT_F32) {
-                const float4 q = *reinterpret_cast<const float4 *>(row + offA);
-                ahi[i][0] = q.x; ahi[i][1] = q.y; ahi[i][2] = q.z; ahi[i][3] = q.w;
-            } else {
-                const float4 qa = *reinterpret_cast<const float4 *>(row + offA);
-                const float4 qb = *reinterpret_cast<const float4 *>(row + offB);
-                ahi[i][0] = qa.x; alo[i][0] = qa.y; ahi[i][1] = qa.z; alo[i][1] = qa.w;
-                ahi[i][2] = qb.x; alo[i][2] = qb.y; ahi[i][3] = qb.z; alo[i][3] = qb.w;
-            }
-        }
-        if (opN) {
-            /* rows paired: halves of a float2 are rows 2u and 2u+1 */
-            float2 sh2[RW / 2], sl2[RW / 2];
-#pragma unroll
-            for (int u = 0; u < RW / 2; u++) {
-                sh2[u] = sl2[u] = make_float2(0.f, 0.f);
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const float2 a = make_float2(ahi[2 * u][c], ahi[2 * u + 1][c]);
-                    if (FMT == FMT_F32) {
-                        pk_cacc1(sh2[u], sl2[u], a, xv[c]);
-                    } else {
-                        pk_cacc2(sh2[u], sl2[u], a, make_float2(alo[2 * u][c], alo[2 * u + 1][c]), xv[c]);
-                    }
+            for (int j = 0; j < CPW; j++) {
+                const int cc = cg * CPW + j;
+                const float4 q = *reinterpret_cast<const float4 *>(rowp + 16 * (cc ^ lane));
+                if (FMT == FMT_F32) {
+                    const float4 xh = *reinterpret_cast<const float4 *>(sx0h + 4 * cc);
+                    const float4 xn = *reinterpret_cast<const float4 *>(sx0n + 4 * cc);
+                    const float4 xl = *reinterpret_cast<const float4 *>(sx0l + 4 * cc);
+                    XIn x01, x23;
+                    x01.h = make_float2(xh.x, xh.y); x01.nh = make_float2(xn.x, xn.y); x01.l = make_float2(xl.x, xl.y);
+                    x23.h = make_float2(xh.z, xh.w); x23.nh = make_float2(xn.z, xn.w); x23.l = make_float2(xl.z, xl.w);
+                    pk_cacc1(sh, sl, make_float2(q.x, q.y), x01);
+                    pk_cacc1(sh, sl, make_float2(q.z, q.w), x23);
+                } else {
+                    XIn x;
+                    x.h = *reinterpret_cast<const float2 *>(sx0h + 2 * cc);
+                    x.nh = *reinterpret_cast<const float2 *>(sx0n + 2 * cc);
+                    x.l = *reinterpret_cast<const float2 *>(sx0l + 2 * cc);
+                    pk_cacc2(sh, sl, make_float2(q.x, q.y), make_float2(q.z, q.w), x);
                 }
             }
-            float sh[RW], sl[RW];
-#pragma unroll
-            for (int u = 0; u < RW / 2; u++) {
-                sh[2 * u] = sh2[u].x; sh[2 * u + 1] = sh2[u].y;
-                sl[2 * u] = sl2[u].x; sl[2 * u + 1] = sl2[u].y;
-            }
-            float vh, vl;
-            reduceR_df<RW>(sh, sl, lane, vh, vl);
-            const int row = r0 + halving_row_R<RW>(lane);
-            if (halving_owner<RW>(lane) && row < nr) atomic_add_pair(out0 + row, vh, vl);
+            dfadd(sh.x, sl.x, sh.y, sl.y);
+            npart[k & 1][cg * SR + rr] = make_float2(sh.x, sl.x);
         }
-        if (opT) {
+
+        const int r0 = k * SR + warp * RW;
+        if (opT && r0 < nr) {
 #pragma unroll
             for (int i = 0; i < RW; i++) {
+                const int rr = warp * RW + i;
+                const unsigned char *row = buf + (size_t)rr * RB;
                 const int r = min(r0 + i, kChunkRows - 1);
                 const XIn x1 = xin(sx1h[r], sx1l[r]);
                 if (FMT == FMT_F32) {
-                    pk_cacc1(ch[0], cl[0], make_float2(ahi[i][0], ahi[i][1]), x1);
-                    pk_cacc1(ch[1], cl[1], make_float2(ahi[i][2], ahi[i][3]), x1);
+                    const float4 q = *reinterpret_cast<const float4 *>(row + 16 * (lane ^ (rr & 31)));
+                    pk_cacc1(ch[0], cl[0], make_float2(q.x, q.y), x1);
+                    pk_cacc1(ch[1], cl[1], make_float2(q.z, q.w), x1);
                 } else {
-                    pk_cacc2(ch[0], cl[0], make_float2(ahi[i][0], ahi[i][1]), make_float2(alo[i][0], alo[i][1]), x1);
-                    pk_cacc2(ch[1], cl[1], make_float2(ahi[i][2], ahi[i][3]), make_float2(alo[i][2], alo[i][3]), x1);
+                    const float4 qa = *reinterpret_cast<const float4 *>(row + 16 * (lane ^ (rr & 31)));
+                    const float4 qb = *reinterpret_cast<const float4 *>(row + 16 * (32 + (lane ^ (rr & 31))));
+                    pk_cacc2(ch[0], cl[0], make_float2(qa.x, qa.y), make_float2(qa.z, qa.w), x1);
+                    pk_cacc2(ch[1], cl[1], make_float2(qb.x, qb.y), make_float2(qb.z, qb.w), x1);
                 }
             }
         }
     }
+    __syncthreads();
+    if (opN) merge_rows(nstage - 1);
     if (opT) {
-        float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw);
-        float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(red_raw + 8 * kTileCols * 4);
+        /* reduce over the warps through the last stage's slot (no copy is pending into it) */
+        unsigned char *rb = stage_raw + ((nstage - 1) % kStages) * kStageBytes;
+        float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(rb);
+        float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(rb + 8 * kTileCols * 4);
         rh[warp][lane_col<FMT>(lane, 0)] = ch[0].x;
         rh[warp][lane_col<FMT>(lane, 1)] = ch[0].y;
         rh[warp][lane_col<FMT>(lane, 2)] = ch[1].x;
@@ -942,8 +972,14 @@ static int pack_mixed(DevRep *d)
                 if (it.fmt == FMT_F32) {
                     h32[pos] = (float)src[c];
                 } else {
+                    /* float pairs: each 16-byte chunk (elements 2m, 2m+1 of a
+                     * row) holds hi0, hi1, lo0, lo1, so the hi and lo parts of
+                     * two neighbours are adjacent for packed arithmetic */
                     const float hi = (float)src[c];
-                    h32x2[pos] = make_float2(hi, (float)(src[c] - (double)hi));
+                    float *f = reinterpret_cast<float *>(h32x2.data());
+                    const size_t e = pos & ~size_t(1), k = pos & 1;
+                    f[2 * e + k] = hi;
+                    f[2 * e + 2 + k] = (float)(src[c] - (double)hi);
                 }
             }
         }
