@@ -436,6 +436,26 @@ def run_gpu(args):
     e2e_s = time.perf_counter() - t0
     barrier()
 
+    # 16 densities per launch (alpha/beta or stacked SCF trials): one
+    # H2ERI_build_Coulomb_device call builds all 16 J in the best mode
+    n16 = 16
+    D16 = np.stack([molecules.seeded_density(nbf, WORKLOAD["n_occ"], 3000 + i) for i in range(n16)])
+    dD16 = torch.tensor(D16, device="cuda")
+    dJ16 = torch.empty_like(dD16)
+    for _ in range(args.warmup):
+        if L.H2ERI_build_Coulomb_device(h.handle, n16, dD16.data_ptr(), dJ16.data_ptr(), sp) != 0:
+            raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+    torch.cuda.synchronize()
+    steps16 = max(2, args.steps // 10)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps16):
+        L.H2ERI_build_Coulomb_device(h.handle, n16, dD16.data_ptr(), dJ16.data_ptr(), sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms16 = e0.elapsed_time(e1) / steps16
+    J16 = dJ16.cpu().numpy()
+
     def max_over_ranks(x):
         if dist is None:
             return x
@@ -459,6 +479,11 @@ def run_gpu(args):
         cpu_v, cpu_n, cpu_dt, J_ref = cpu_baseline(orc, h, D)
     def rel(J):
         return float(np.linalg.norm(J - J_ref) / np.linalg.norm(J_ref))
+
+    def rel16(J, Dk):
+        Jo = np.zeros_like(Dk)
+        orc.oracle_build_Coulomb(h.handle, np.ascontiguousarray(Dk).ctypes.data, Jo.ctypes.data)
+        return float(np.linalg.norm(J - Jo) / np.linalg.norm(Jo))
 
     step_s = ms_best / 1e3 / args.steps
     value = ws * args.steps / (ms_best / 1e3)
@@ -492,6 +517,10 @@ def run_gpu(args):
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
         "gpu_launches": launches_per_J * args.steps,
         "phase_ms_last_host_call": {k: h.report()[k] for k in ("ms_fwd", "ms_mid", "ms_bwd", "ms_den", "ms_total")},
+        "multi_density": {"n_den": n16, "value": n16 / (ms16 / 1e3), "unit": "J builds/s",
+                          "ms_per_launch": ms16, "precision": best,
+                          "relerr_vs_fp64_oracle_max_sampled": max(rel16(J16[i], D16[i]) for i in (0, n16 - 1)),
+                          "sample": "densities 0 and 15 checked against the CPU oracle"},
         "setup_s": setup_s, "upload_s": upload_s,
     }
     print(json.dumps(out), flush=True)

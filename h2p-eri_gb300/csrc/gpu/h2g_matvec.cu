@@ -216,7 +216,7 @@ __device__ __forceinline__ void reduceR_df(float *h, float *l, int lane, float &
     dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 1), __shfl_xor_sync(0xffffffffu, vl, 1));
 }
 
-/* One CTA per (tile, vector). A tile is a chunk of up to kChunkRows rows and
+/* One CTA per (vector, tile). A tile is a chunk of up to kChunkRows rows and
  * kTileCols columns. The chunk streams through a kStages-deep ring of 32 KB
  * shared-memory stages filled with cp.async (16-byte copies, any leading
  * dimension, zero fill past the tile edge), so the next stages are in flight
@@ -249,8 +249,10 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     /* N-side row partials of the FP32 formats, [stage parity][column group * SR + row] */
     __shared__ __align__(16) float2 npart[2][256];
 
-    const Tile t = tiles[blockIdx.x];
-    const int v = blockIdx.y;
+    /* the vector index runs fastest: the CTAs of one tile for several
+     * densities run back to back and share the tile through L2 */
+    const Tile t = tiles[blockIdx.y];
+    const int v = blockIdx.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
     const int nr = t.nr, nc = t.nc;
@@ -947,14 +949,17 @@ static int ensure_work(DevRep *d, int nvec)
  * near-field diagonal blocks) and the single-float kernel otherwise. */
 static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s)
 {
-    if (r.count == 0) return;
-    dim3 grid(r.count, nvec);
-    if (d->precision == H2ERI_GPU_FP64)
-        k_tile<FMT_F64><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena, va);
-    else if (r.pair)
-        k_tile<FMT_F32X2><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena32x2, va);
-    else
-        k_tile<FMT_F32><<<grid, kTileThreads, kTileSmem, s>>>(d->tiles + r.first, d->arena32, va);
+    constexpr int kMaxGridY = 65535;
+    for (int f = 0; f < r.count; f += kMaxGridY) {
+        dim3 grid(nvec, std::min(kMaxGridY, r.count - f));
+        const Tile *t = d->tiles + r.first + f;
+        if (d->precision == H2ERI_GPU_FP64)
+            k_tile<FMT_F64><<<grid, kTileThreads, kTileSmem, s>>>(t, d->arena, va);
+        else if (r.pair)
+            k_tile<FMT_F32X2><<<grid, kTileThreads, kTileSmem, s>>>(t, d->arena32x2, va);
+        else
+            k_tile<FMT_F32><<<grid, kTileThreads, kTileSmem, s>>>(t, d->arena32, va);
+    }
 }
 
 /* Fill the mixed arenas from the host blocks (first use of mixed mode). */
