@@ -48,6 +48,11 @@ WORKLOADS = {
             "inputs_vs_L2": "H2 representation ~0.28 GB read per step > 129 MB L2",
             "k_cpu_stride": 2, "k_check_full": True},
 }
+# uneven batch: alkanes with lengths drawn from C8..C60 (seeded), two densities
+# each; BATCH_SIZE molecules (the set-up of each runs on the host first)
+WORKLOADS["batch"] = {"workload": "J builds for a batch of alkanes C8..C60 (seeded lengths), cc-pVDZ cartesian, "
+                                  "QR tol 1e-8, 2 densities each", "qr_tol": 1e-8, "seed": 4242,
+                      "inputs_vs_L2": "sum of the representations > 129 MB L2"}
 WORKLOAD = dict(WORKLOADS["c30"])
 METRIC = "J builds/s C30H62 (mixed vs FP64) at relerr<=1e-8"
 # DRAM bytes (read + write) of all tile-kernel launches of one mixed C30H62 J
@@ -353,9 +358,94 @@ def run_gpu_exchange(args):
     h.destroy()
 
 
+def run_gpu_batch(args):
+    """Uneven batch: every molecule's J builds (two densities) in one
+    H2ERI_build_Coulomb_batch call, against the same builds one molecule
+    after another on one stream."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    import h2eri_gb300 as hg
+    from h2eri_gb300 import build as hb, molecules
+    hb.build()
+    L = hg.lib()
+    lengths = [int(n) for n in np.random.default_rng(WORKLOAD["seed"]).integers(8, 61, size=args.batch_size)]
+    hs, t0 = [], time.perf_counter()
+    os.makedirs(CACHE_DIR, exist_ok=True)
+    for n in lengths:
+        mol = os.path.join(CACHE_DIR, f"alk{n}.mol")
+        molecules.write_alkane(mol, n)
+        hs.append(hg.H2ERI.from_mol(mol, qr_tol=WORKLOAD["qr_tol"]))
+    setup_s = time.perf_counter() - t0
+    log(f"set-up of {len(hs)} molecules (host, not timed): {setup_s:.1f} s")
+    best = "mixed" if args.precision in ("auto", "mixed") else "fp64"
+    dDs, dJs, Ds = [], [], []
+    for k, h in enumerate(hs):
+        L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if best == "mixed" else hg.FP64)
+        n_occ = (8 * lengths[k] + 2) // 2   # electrons of C_nH_2n+2 / 2
+        D = np.stack([molecules.seeded_density(h.num_bf, n_occ, 4000 + 10 * k + i) for i in range(2)])
+        Ds.append(D)
+        dDs.append(torch.tensor(D, device="cuda"))
+        dJs.append(torch.empty_like(dDs[-1]))
+    n = len(hs)
+    harr = (ctypes.c_void_p * n)(*[h.handle.value for h in hs])
+    narr = (ctypes.c_int * n)(*([2] * n))
+    darr = (ctypes.c_void_p * n)(*[t.data_ptr() for t in dDs])
+    jarr = (ctypes.c_void_p * n)(*[t.data_ptr() for t in dJs])
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def batched():
+        if L.H2ERI_build_Coulomb_batch(n, harr, narr, darr, jarr, sp) != 0:
+            raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+
+    def one_by_one():
+        for k in range(n):
+            L.H2ERI_build_Coulomb_device(hs[k].handle, 2, dDs[k].data_ptr(), dJs[k].data_ptr(), sp)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps, clk.summary()
+
+    ms_seq, _ = timed(one_by_one)
+    ms, c = timed(batched)
+    orc = load_oracle()
+    errs = []
+    for k in (0, n - 1):
+        Jo = np.zeros_like(Ds[k][0])
+        orc.oracle_build_Coulomb(hs[k].handle, np.ascontiguousarray(Ds[k][0]).ctypes.data, Jo.ctypes.data)
+        errs.append(float(np.linalg.norm(dJs[k][0].cpu().numpy() - Jo) / np.linalg.norm(Jo)))
+    builds = 2 * n
+    out = {"metric": "J builds/s, uneven batch of alkanes (one batched call)", "value": builds / (ms / 1e3),
+           "unit": "J builds/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32x2+f64" if best == "mixed" else "f64",
+           "data": "synthetic (generated alkane geometries, seeded densities)",
+           "config": dict(WORKLOAD, molecules=[f"C{m}H{2 * m + 2}" for m in lengths], precision=best,
+                          sample=f"{n} molecules (lengths from U{{8..60}}, seed 4242); 2 densities each"),
+           "one_by_one_ms_per_step": ms_seq, "batch_speedup": ms_seq / ms,
+           "relerr_vs_fp64_oracle_sampled": max(errs),
+           "clocks": {"sm_mhz": c["sm_mhz"], "sm_max_mhz": c["sm_max_mhz"], "reasons": c["reasons"]},
+           "setup_s": setup_s}
+    print(json.dumps(out), flush=True)
+    for h in hs:
+        h.destroy()
+
+
 def run_gpu(args):
     if args.path == "exchange":
         return run_gpu_exchange(args)
+    if args.workload == "batch":
+        return run_gpu_batch(args)
     import torch
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -539,6 +629,7 @@ def main():
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--workload", default="c30", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg (profiler runs)")
+    ap.add_argument("--batch-size", type=int, default=8, help="molecules of the uneven batch workload")
     ap.add_argument("--path", default="coulomb", choices=["coulomb", "exchange"],
                     help="coulomb: J builds (the headline); exchange: K builds (H2ERI_build_exchange)")
     args = ap.parse_args()

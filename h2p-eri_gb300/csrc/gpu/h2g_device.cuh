@@ -111,6 +111,7 @@ struct DevRep {
     int nden_cap = 0;
     cudaStream_t s_main = nullptr, s_aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_zero = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_bfork = nullptr, ev_bjoin = nullptr;   /* batched builds: fork from / join to the caller */
     cudaEvent_t ev_t[8] = {nullptr};
     float last_ms[5] = {0, 0, 0, 0, 0};   /* fwd, mid, bwd, den, total */
     int precision = 0;

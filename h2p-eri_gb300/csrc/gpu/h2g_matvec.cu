@@ -660,6 +660,8 @@ static void free_rep(DevRep *d)
     if (d->ev_join) cudaEventDestroy(d->ev_join);
     if (d->ev_zero) cudaEventDestroy(d->ev_zero);
     if (d->ev_done) cudaEventDestroy(d->ev_done);
+    if (d->ev_bfork) cudaEventDestroy(d->ev_bfork);
+    if (d->ev_bjoin) cudaEventDestroy(d->ev_bjoin);
     for (auto &e : d->ev_t)
         if (e) cudaEventDestroy(e);
     free_exchange_state(d);
@@ -886,6 +888,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_zero, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_done, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&d->ev_bfork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&d->ev_bjoin, cudaEventDisableTiming));
     for (auto &e : d->ev_t) CUDA_TRY(cudaEventCreate(&e));
 
     d->krnl = krnl;
@@ -1187,6 +1191,43 @@ extern "C" int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double
     if (n_den < 1) { set_error("n_den < 1"); return 3; }
     cudaStream_t s = stream ? (cudaStream_t)stream : d->s_main;
     return enqueue_coulomb(d, n_den, d_den, d_J, s, false);
+}
+
+/* J for several structures at once. Every structure's build runs on its
+ * own pair of streams, forked from `stream` and joined back to it, so the
+ * builds of small and large molecules overlap on the GPU. All device
+ * buffers are set up before anything is enqueued. */
+extern "C" int H2ERI_build_Coulomb_batch(int n, H2ERI_p *h2eris, const int *n_den, const double *const *d_dens,
+                                         double *const *d_Js, void *stream)
+{
+    if (n < 0 || (n > 0 && (h2eris == nullptr || n_den == nullptr || d_dens == nullptr || d_Js == nullptr))) {
+        set_error("H2ERI_build_Coulomb_batch: bad arguments");
+        return 3;
+    }
+    std::vector<DevRep *> reps(n, nullptr);
+    for (int i = 0; i < n; i++) {
+        if (n_den[i] < 1) { set_error("H2ERI_build_Coulomb_batch: n_den < 1"); return 3; }
+        for (int j = 0; j < i; j++)
+            if (h2eris[j] == h2eris[i]) {
+                set_error("H2ERI_build_Coulomb_batch: a structure appears twice (its builds share buffers)");
+                return 3;
+            }
+        int rc = get_rep(h2eris[i], &reps[i]);
+        if (rc) return rc;
+        rc = ensure_work(reps[i], n_den[i]);
+        if (rc) return rc;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int i = 0; i < n; i++) {
+        DevRep *d = reps[i];
+        CUDA_TRY(cudaEventRecord(d->ev_bfork, s));
+        CUDA_TRY(cudaStreamWaitEvent(d->s_main, d->ev_bfork, 0));
+        int rc = enqueue_coulomb(d, n_den[i], d_dens[i], d_Js[i], d->s_main, false);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(d->ev_bjoin, d->s_main));
+    }
+    for (int i = 0; i < n; i++) CUDA_TRY(cudaStreamWaitEvent(s, reps[i]->ev_bjoin, 0));
+    return 0;
 }
 
 extern "C" int H2ERI_build_Coulomb_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *J_mats)

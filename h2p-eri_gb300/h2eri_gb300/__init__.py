@@ -88,6 +88,7 @@ SIGNATURES = {
     "H2ERI_matvec_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     "H2ERI_build_Coulomb_multi": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
     "H2ERI_build_Coulomb_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
+    "H2ERI_build_Coulomb_batch": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
     "H2ERI_build_exchange_multi": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
     "H2ERI_build_exchange_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "H2ERI_gpu_exchange_report": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),

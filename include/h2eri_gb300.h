@@ -90,6 +90,14 @@ int H2ERI_matvec_device(H2ERI_p h2eri, int nvec, const double *d_x, double *d_y,
 int H2ERI_build_Coulomb_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *J_mats);
 /* Same on device arrays, enqueued on a stream. */
 int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double *d_den, double *d_J, void *stream);
+/* J for n structures (molecules of any size) in one call, device arrays:
+ * d_dens[i] / d_Js[i] hold n_den[i] densities / J matrices of h2eris[i]
+ * ([n_den][num_bf][num_bf]). The builds are forked from `stream` onto each
+ * structure's own streams, run concurrently and are joined back to `stream`.
+ * A structure may appear once per call. No counterpart in the reference
+ * (its callers loop over H2ERI_build_Coulomb). Returns 0 on success. */
+int H2ERI_build_Coulomb_batch(int n, H2ERI_p *h2eris, const int *n_den, const double *const *d_dens,
+                              double *const *d_Js, void *stream);
 /* K for n_den densities stored back to back ([n_den][num_bf][num_bf]) on the
  * host, one after the other. Returns 0 on success. */
 int H2ERI_build_exchange_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *K_mats);
