@@ -34,9 +34,10 @@ enum VecKind : uint8_t {
  * Offsets are element offsets (already shifted by r0 / c0) into the vector
  * space named by the kind byte. */
 struct Tile {
-    uint64_t a;            /* element offset of A[r0][c0] in the FP64 arena        */
-    uint64_t a2;           /* element offset in the mixed arena of the same matrix */
-    int32_t ld, ld2;       /* leading dimensions in the two arenas                 */
+    uint64_t a;            /* element offset of A[r0][c0] in the FP64 arena              */
+    uint64_t a2;           /* mixed formats: (c0 << 32) | r0, the tile's origin in the  */
+                           /* stored matrix (tensor-map coordinates)                    */
+    int32_t ld, ld2;       /* FP64 leading dimension; mixed formats: tensor map index   */
     int16_t nr, nc;
     int32_t in0, out0, in1, out1;
     uint8_t k_in0, k_out0, k_in1, k_out1;
@@ -85,6 +86,9 @@ struct DevRep {
     double *arena = nullptr;
     size_t arena_elems = 0;
     float *arena32 = nullptr;         /* B and D blocks, mixed mode */
+    void *tmaps = nullptr;            /* one 128-byte tensor map per mixed-arena matrix (TMA loads) */
+    unsigned *err_flag = nullptr;     /* mapped host word: nonzero after a kernel gave up a bounded wait */
+    unsigned *err_flag_dev = nullptr; /* its device address */
     float2 *arena32x2 = nullptr;      /* U bases as hi/lo pairs, mixed mode */
     size_t arena32_elems = 0, arena32x2_elems = 0;
     std::vector<PackItem> mixed_items;

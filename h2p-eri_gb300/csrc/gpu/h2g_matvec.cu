@@ -26,6 +26,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cuda.h>
+
 #include "h2eri_gb300.h"
 #include "h2g_device.cuh"
 #include "h2g_farith.cuh"
@@ -72,6 +74,7 @@ __device__ __forceinline__ int lane_col(int lane, int k)
 constexpr int kStageBytes = 32768;
 constexpr int kStages = 3;
 constexpr size_t kTileSmem = (size_t)kStageBytes * kStages;
+constexpr size_t kTileSmemLaunch = kTileSmem + 1024;   /* + slack to align the TMA destinations */
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes)
 {
@@ -80,6 +83,38 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+/* ---- TMA (tensor copies) and mbarriers, FP32 formats ---- */
+constexpr int kTmaBoxBytes = 128;              /* inner box extent: one 128-byte swizzle span */
+constexpr long long kWaitCycles = 2000000000LL; /* bound of every mbarrier wait (~1 s) */
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+/* Wait for phase `parity` of an mbarrier, giving up after kWaitCycles. */
+__device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    if (mbar_try(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
+}
+/* 2-D tensor copy of one box into shared memory, completing on bar. */
+__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map, int x, int y, unsigned bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                 ::"r"(dst), "l"(map), "r"(x), "r"(y), "r"(bar)
+                 : "memory");
+}
 
 template <int FMT> struct FmtInfo;
 template <> struct FmtInfo<FMT_F64> { static constexpr int ebytes = 8; };
@@ -237,13 +272,19 @@ __device__ __forceinline__ void reduceR_df(float *h, float *l, int lane, float &
  * output element is converted to FP64 once and added with an FP64 atomic. */
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
-k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va)
+k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va,
+       const CUtensorMap *__restrict__ maps, unsigned *err)
 {
     constexpr int EB = FmtInfo<FMT>::ebytes;
     constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage   */
     constexpr int RW = SR / 8;                            /* rows per warp    */
     constexpr int RB = kTileCols * EB;                    /* bytes per row    */
-    extern __shared__ __align__(128) unsigned char stage_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    /* the swizzled TMA boxes need 1024-byte aligned destinations */
+    unsigned char *stage_raw = (FMT == FMT_F64)
+        ? smem_raw
+        : reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ __align__(8) unsigned long long tbar[kStages];
     __shared__ __align__(16) float sx0h[kTileCols], sx0l[kTileCols], sx0n[kTileCols];
     __shared__ float sx1h[kChunkRows], sx1l[kChunkRows];
     /* N-side row partials of the FP32 formats, [stage parity][column group * SR + row] */
@@ -257,18 +298,17 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
     const int nr = t.nr, nc = t.nc;
     const int nstage = (nr + SR - 1) / SR;
-    const unsigned char *base = (FMT == FMT_F64)
-        ? reinterpret_cast<const unsigned char *>(reinterpret_cast<const double *>(arena_v) + t.a)
-        : (FMT == FMT_F32) ? reinterpret_cast<const unsigned char *>(reinterpret_cast<const float *>(arena_v) + t.a2)
-                           : reinterpret_cast<const unsigned char *>(reinterpret_cast<const float2 *>(arena_v) + t.a2);
-    const size_t ld_bytes = (size_t)((FMT == FMT_F64) ? t.ld : t.ld2) * EB;
+    const unsigned char *base = reinterpret_cast<const unsigned char *>(arena_v) + (size_t)t.a * EB;   /* FP64 */
+    const size_t ld_bytes = (size_t)t.ld * EB;
     const int nc_bytes16 = ((nc * EB) + 15) & ~15;
 
     /* prologue: first two stages in flight */
-    issue_stage<FMT>(stage_raw, base, ld_bytes, 0, nr, nc_bytes16, tid);
-    cp_async_commit();
-    if (nstage > 1) issue_stage<FMT>(stage_raw + kStageBytes, base, ld_bytes, SR, nr, nc_bytes16, tid);
-    cp_async_commit();
+    if (FMT == FMT_F64) {
+        issue_stage<FMT>(stage_raw, base, ld_bytes, 0, nr, nc_bytes16, tid);
+        cp_async_commit();
+        if (nstage > 1) issue_stage<FMT>(stage_raw + kStageBytes, base, ld_bytes, SR, nr, nc_bytes16, tid);
+        cp_async_commit();
+    }
 
     double *out0 = opN ? vec_ptr(va, t.k_out0, t.out0, v) : nullptr;
     bool ok[4];
@@ -342,7 +382,33 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
         return;
     }
 
-    /* ---- FP32 formats: split the tile's input slices once ---- */
+    /* ---- FP32 formats: stages arrive by TMA as NB swizzled boxes of
+     * SR rows x 128 bytes (16-byte chunk q of box row r at q ^ (r & 7)) ---- */
+    constexpr int NB = RB / kTmaBoxBytes;          /* boxes per stage: 4 (F32) or 8 (pairs) */
+    constexpr int BOXB = SR * kTmaBoxBytes;        /* bytes per box */
+    constexpr int BOXW = kTmaBoxBytes / EB;        /* elements per box row */
+    const CUtensorMap *map = maps + t.ld2;
+    const int tc0 = (int)(t.a2 >> 32), tr0 = (int)(t.a2 & 0xffffffffu);
+    if (tid == 0) {
+        for (int i = 0; i < kStages; i++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tbar[i])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+    }
+    __syncthreads();
+    auto tma_stage = [&](int k) {   /* thread 0 only */
+        const unsigned bar = smem_addr(&tbar[k % kStages]);
+        const unsigned dst = smem_addr(stage_raw + (k % kStages) * kStageBytes);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kStageBytes) : "memory");
+#pragma unroll
+        for (int bx = 0; bx < NB; bx++) tma_load_2d(dst + bx * BOXB, map, tc0 + bx * BOXW, tr0 + k * SR, bar);
+    };
+    if (tid == 0) {
+        tma_stage(0);
+        if (nstage > 1) tma_stage(1);
+    }
+
+    /* split the tile's input slices once */
     if (tid < kTileCols) {
         float h = 0.f, l = 0.f;
         if (opN && tid < nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
@@ -357,13 +423,14 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     __syncthreads();
 
     /* N side: lane-per-row. A stage's SR rows form NG groups of 32; the
-     * warps of a group split the row's 16-byte chunks (CPW each), every lane
-     * accumulates its row over its chunks as even/odd column pairs, and the
-     * NCG column-group partials of a row are merged once per stage. */
-    constexpr int RC = RB / 16;        /* chunks per row: 32 (F32) or 64 (pairs) */
-    constexpr int NG = SR / 32;        /* 32-row groups per stage               */
-    constexpr int NCG = 8 / NG;        /* column groups (warps) per row group   */
-    constexpr int CPW = RC / NCG;      /* chunks per warp: 8                    */
+     * NCG warps of a group take one box each (8 chunks, 32 or 16 columns);
+     * every lane accumulates its row over the box as even/odd column pairs,
+     * and the NCG box partials of a row are merged once per stage. Rows past
+     * the tile (a stage may hold rows of the next tile of the same matrix)
+     * are never merged. */
+    constexpr int NG = SR / 32;        /* 32-row groups per stage         */
+    constexpr int NCG = 8 / NG;        /* boxes (warps) per row group     */
+    static_assert(NCG == NB, "one box per N-side warp");
     const int ng = warp % NG, cg = warp / NG;
     auto merge_rows = [&](int k) {     /* partials of stage k -> out0 */
         if (tid < SR) {
@@ -382,24 +449,25 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
      * (lane_col); column pairs (slots 0,1 and 2,3) accumulate as float pairs */
     float2 ch[2], cl[2];
     ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
+    int lost = -1;   /* last stage whose wait gave up */
     for (int k = 0; k < nstage; k++) {
-        cp_async_wait1();
+        if (!mbar_wait(smem_addr(&tbar[k % kStages]), (unsigned)((k / kStages) & 1))) {
+            atomicOr(err, 1u);
+            lost = k;
+        }
         __syncthreads();
         if (opN && k > 0) merge_rows(k - 1);
-        if (k + 2 < nstage)
-            issue_stage<FMT>(stage_raw + ((k + 2) % kStages) * kStageBytes, base, ld_bytes, (k + 2) * SR, nr,
-                             nc_bytes16, tid);
-        cp_async_commit();
+        if (tid == 0 && k + 2 < nstage) tma_stage(k + 2);   /* its slot was freed by the barrier above */
         const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
 
         if (opN && k * SR + ng * 32 < nr) {
             const int rr = ng * 32 + lane;
-            const unsigned char *rowp = buf + (size_t)rr * RB;
+            const unsigned char *rowp = buf + cg * BOXB + rr * kTmaBoxBytes;
             float2 sh = make_float2(0.f, 0.f), sl = sh;
 #pragma unroll
-            for (int j = 0; j < CPW; j++) {
-                const int cc = cg * CPW + j;
-                const float4 q = *reinterpret_cast<const float4 *>(rowp + 16 * (cc ^ lane));
+            for (int j = 0; j < 8; j++) {
+                const int cc = cg * 8 + j;
+                const float4 q = *reinterpret_cast<const float4 *>(rowp + 16 * (j ^ (rr & 7)));
                 if (FMT == FMT_F32) {
                     const float4 xh = *reinterpret_cast<const float4 *>(sx0h + 4 * cc);
                     const float4 xn = *reinterpret_cast<const float4 *>(sx0n + 4 * cc);
@@ -423,25 +491,29 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
 
         const int r0 = k * SR + warp * RW;
         if (opT && r0 < nr) {
+            const int lb = (lane >> 3) * BOXB, lq = lane & 7;
 #pragma unroll
             for (int i = 0; i < RW; i++) {
                 const int rr = warp * RW + i;
-                const unsigned char *row = buf + (size_t)rr * RB;
+                const unsigned char *row = buf + lb + rr * kTmaBoxBytes + 16 * (lq ^ (rr & 7));
                 const int r = min(r0 + i, kChunkRows - 1);
                 const XIn x1 = xin(sx1h[r], sx1l[r]);
                 if (FMT == FMT_F32) {
-                    const float4 q = *reinterpret_cast<const float4 *>(row + 16 * (lane ^ (rr & 31)));
+                    const float4 q = *reinterpret_cast<const float4 *>(row);
                     pk_cacc1(ch[0], cl[0], make_float2(q.x, q.y), x1);
                     pk_cacc1(ch[1], cl[1], make_float2(q.z, q.w), x1);
                 } else {
-                    const float4 qa = *reinterpret_cast<const float4 *>(row + 16 * (lane ^ (rr & 31)));
-                    const float4 qb = *reinterpret_cast<const float4 *>(row + 16 * (32 + (lane ^ (rr & 31))));
+                    const float4 qa = *reinterpret_cast<const float4 *>(row);
+                    const float4 qb = *reinterpret_cast<const float4 *>(row + 4 * BOXB);
                     pk_cacc2(ch[0], cl[0], make_float2(qa.x, qa.y), make_float2(qa.z, qa.w), x1);
                     pk_cacc2(ch[1], cl[1], make_float2(qb.x, qb.y), make_float2(qb.z, qb.w), x1);
                 }
             }
         }
     }
+    /* a load whose wait gave up may still land: one more bounded wait before
+     * the slot is reused or the CTA exits */
+    if (lost >= 0) (void)mbar_wait(smem_addr(&tbar[lost % kStages]), (unsigned)((lost / kStages) & 1));
     __syncthreads();
     if (opN) merge_rows(nstage - 1);
     if (opT) {
@@ -512,6 +584,7 @@ namespace {
 struct MatLoc {
     size_t a = 0, a2 = 0;
     int ld = 0, ld2 = 0;
+    int map = -1;          /* tensor map of the mixed-arena copy (index of its PackItem) */
 };
 
 /* Packs matrices into the FP64 arena now and records where each goes in the
@@ -547,6 +620,7 @@ struct Packer {
             m.a2 = (n32x2 + 3) & ~size_t(3);
             n32x2 = m.a2 + (size_t)sr * m.ld2;
         }
+        m.map = (int)items.size();
         items.push_back(PackItem{src, nrow, ncol, lds, trans ? 1 : 0, mixed_fmt, m.a2, m.ld2});
         return m;
     }
@@ -562,9 +636,10 @@ struct Planner {
                 Tile t;
                 std::memset(&t, 0, sizeof(t));
                 t.a = m.a + (size_t)r0 * m.ld + c0;
-                t.a2 = m.a2 + (size_t)r0 * m.ld2 + c0;
+                /* mixed formats: tensor-map coordinates of the tile (TMA loads) */
+                t.a2 = ((uint64_t)(uint32_t)c0 << 32) | (uint32_t)r0;
                 t.ld = m.ld;
-                t.ld2 = m.ld2;
+                t.ld2 = m.map;
                 t.nr = (int16_t)std::min(kChunkRows, nrow - r0);
                 t.nc = (int16_t)std::min(kTileCols, ncol - c0);
                 if (kout0 != VK_NONE) { t.k_in0 = kin0; t.in0 = in0 + c0; t.k_out0 = kout0; t.out0 = out0 + r0; }
@@ -646,6 +721,8 @@ static void free_rep(DevRep *d)
     cudaFree(d->arena);
     cudaFree(d->arena32);
     cudaFree(d->arena32x2);
+    cudaFree(d->tmaps);
+    if (d->err_flag) cudaFreeHost(d->err_flag);
     cudaFree(d->tiles);
     cudaFree(d->unc_map);
     cudaFree(d->con_map);
@@ -873,9 +950,12 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaMalloc(&d->con_map, std::max<size_t>(con.size(), 1) * sizeof(int)));
     CUDA_TRY(cudaMemcpy(d->con_map, con.data(), con.size() * sizeof(int), cudaMemcpyHostToDevice));
 
-    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
-    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
-    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
+    CUDA_TRY(cudaHostAlloc((void **)&d->err_flag, sizeof(unsigned), cudaHostAllocMapped));
+    *d->err_flag = 0;
+    CUDA_TRY(cudaHostGetDevicePointer((void **)&d->err_flag_dev, d->err_flag, 0));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
     /* The tree sweeps are a chain of dependent launches (the critical path);
      * the near field is one large independent batch. Giving the chain's
      * stream the higher priority lets near-field tiles fill only the SMs the
@@ -957,13 +1037,61 @@ static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int
     for (int f = 0; f < r.count; f += kMaxGridY) {
         dim3 grid(nvec, std::min(kMaxGridY, r.count - f));
         const Tile *t = d->tiles + r.first + f;
+        const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(d->tmaps);
         if (d->precision == H2ERI_GPU_FP64)
-            k_tile<FMT_F64><<<grid, kTileThreads, kTileSmem, s>>>(t, d->arena, va);
+            k_tile<FMT_F64><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena, va, maps, d->err_flag_dev);
         else if (r.pair)
-            k_tile<FMT_F32X2><<<grid, kTileThreads, kTileSmem, s>>>(t, d->arena32x2, va);
+            k_tile<FMT_F32X2><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena32x2, va, maps, d->err_flag_dev);
         else
-            k_tile<FMT_F32><<<grid, kTileThreads, kTileSmem, s>>>(t, d->arena32, va);
+            k_tile<FMT_F32><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena32, va, maps, d->err_flag_dev);
     }
+}
+
+/* cuTensorMapEncodeTiled, looked up through the runtime (no link-time
+ * dependency on the driver library). */
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+/* One tensor map per matrix of the mixed arenas: a 2-D view (leading
+ * dimension as the extent, so the zero padding of a row is in range; float
+ * pairs as 8-byte elements) with boxes of 128 bytes x one stage of rows and
+ * the 128-byte swizzle; rows and columns outside the matrix read as zero. */
+static int build_tensor_maps(DevRep *d)
+{
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (fn == nullptr || q != cudaDriverEntryPointSuccess) {
+        set_error("cuTensorMapEncodeTiled is not available");
+        return 10;
+    }
+    const EncodeTiledFn encode = reinterpret_cast<EncodeTiledFn>(fn);
+    std::vector<CUtensorMap> maps(std::max<size_t>(d->mixed_items.size(), 1));
+    for (size_t i = 0; i < d->mixed_items.size(); i++) {
+        const PackItem &it = d->mixed_items[i];
+        const bool pair = it.fmt == FMT_F32X2;
+        const int eb = pair ? 8 : 4;
+        const int srows = it.trans ? it.ncol : it.nrow;
+        unsigned char *base = pair ? reinterpret_cast<unsigned char *>(d->arena32x2) + it.off * 8
+                                   : reinterpret_cast<unsigned char *>(d->arena32) + it.off * 4;
+        const cuuint64_t dims[2] = {(cuuint64_t)it.ld, (cuuint64_t)std::max(srows, 1)};
+        const cuuint64_t strides[1] = {(cuuint64_t)it.ld * eb};
+        const cuuint32_t box[2] = {(cuuint32_t)(kTmaBoxBytes / eb), (cuuint32_t)(kStageBytes / (kTileCols * eb))};
+        const cuuint32_t estr[2] = {1, 1};
+        const CUresult r = encode(&maps[i], pair ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                  base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            set_error("cuTensorMapEncodeTiled failed for mixed matrix " + std::to_string(i) + " (code " +
+                      std::to_string((int)r) + ")");
+            return 10;
+        }
+    }
+    CUDA_TRY(cudaMalloc(&d->tmaps, maps.size() * sizeof(CUtensorMap)));
+    CUDA_TRY(cudaMemcpy(d->tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+    return 0;
 }
 
 /* Fill the mixed arenas from the host blocks (first use of mixed mode). */
@@ -997,7 +1125,7 @@ static int pack_mixed(DevRep *d)
     CUDA_TRY(cudaMemcpy(d->arena32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMalloc(&d->arena32x2, h32x2.size() * sizeof(float2)));
     CUDA_TRY(cudaMemcpy(d->arena32x2, h32x2.data(), h32x2.size() * sizeof(float2), cudaMemcpyHostToDevice));
-    return 0;
+    return build_tensor_maps(d);
 }
 
 int set_precision_mode(DevRep *d, H2ERI_p h, int mode)
@@ -1057,6 +1185,16 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     CUDA_TRY(cudaStreamWaitEvent(s, d->ev_done, 0));
     CUDA_TRY(cudaGetLastError());
     return 0;
+}
+
+/* After a synchronous call: a tile kernel that gave up a bounded wait for
+ * a TMA load leaves a nonzero error word (mapped host memory). */
+static int check_kernel_flag(DevRep *d)
+{
+    if (d->err_flag == nullptr || *d->err_flag == 0) return 0;
+    *d->err_flag = 0;
+    set_error("a tile kernel gave up waiting for a TMA load (bounded wait expired); results are invalid");
+    return 11;
 }
 
 /* After a timed enqueue has completed: fill the reference timers. */
@@ -1173,6 +1311,8 @@ extern "C" int H2ERI_matvec_multi(H2ERI_p h2eri, int nvec, const double *x, doub
     if (rc) return rc;
     CUDA_TRY(cudaMemcpyAsync(y, d->ybuf, bytes, cudaMemcpyDeviceToHost, d->s_main));
     CUDA_TRY(cudaStreamSynchronize(d->s_main));
+    rc = check_kernel_flag(d);
+    if (rc) return rc;
     collect_times(d, h2eri);
     h2eri->n_matvec += nvec;
     return 0;
@@ -1244,6 +1384,8 @@ extern "C" int H2ERI_build_Coulomb_multi(H2ERI_p h2eri, int n_den, const double 
     if (rc) return rc;
     CUDA_TRY(cudaMemcpyAsync(J_mats, d->jbuf, bytes, cudaMemcpyDeviceToHost, d->s_main));
     CUDA_TRY(cudaStreamSynchronize(d->s_main));
+    rc = check_kernel_flag(d);
+    if (rc) return rc;
     collect_times(d, h2eri);
     h2eri->n_matvec += n_den;
     return 0;
