@@ -540,6 +540,219 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     }
 }
 
+/* Mixed-mode tile kernel (FP32 formats), two tiles per CTA. Stages arrive
+ * by TMA as NB swizzled boxes of SR rows x 128 bytes (16-byte chunk q of box
+ * row r at q ^ (r & 7)) into a kStages-deep ring that runs across both
+ * tiles: the second tile's first stages load while the first tile's last
+ * stages are multiplied, and both tiles' input slices are split into float
+ * pairs up front (two buffers), so a CTA waits once for memory, not once per
+ * tile. CTA (v, y) of a launch with G CTAs per vector takes tiles y and
+ * y + G. Arithmetic as in k_tile: N side lane-per-row with per-stage merges
+ * of the box partials, T side lanes over columns with float-pair sums. */
+template <int FMT>
+__global__ void __launch_bounds__(kTileThreads, 2)
+k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ VecArgs va,
+          const CUtensorMap *__restrict__ maps, unsigned *err)
+{
+    constexpr int EB = FmtInfo<FMT>::ebytes;
+    constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage        */
+    constexpr int RW = SR / 8;                            /* T-side rows per warp  */
+    constexpr int RB = kTileCols * EB;                    /* bytes per stage row   */
+    constexpr int NB = RB / kTmaBoxBytes;                 /* boxes per stage       */
+    constexpr int BOXB = SR * kTmaBoxBytes;               /* bytes per box         */
+    constexpr int BOXW = kTmaBoxBytes / EB;               /* elements per box row  */
+    constexpr int NG = SR / 32;                           /* N-side 32-row groups  */
+    constexpr int NCG = 8 / NG;                           /* boxes (warps) per group */
+    static_assert(NCG == NB, "one box per N-side warp");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char *stage_raw =
+        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ __align__(8) unsigned long long tbar[kStages];
+    struct Inputs {
+        float x0h[kTileCols], x0l[kTileCols], x0n[kTileCols], x1h[kChunkRows], x1l[kChunkRows];
+    };
+    __shared__ __align__(16) Inputs sxb[2];
+    __shared__ __align__(16) float2 npart[2][256];
+
+    const int v = blockIdx.x, G = gridDim.y;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ti0 = blockIdx.y, ti1 = blockIdx.y + G;
+    const int ntl = ti1 < n_tiles ? 2 : 1;
+    const Tile tA = tiles[ti0];
+    const Tile tB = tiles[ntl == 2 ? ti1 : ti0];
+    const int nsA = (tA.nr + SR - 1) / SR, nsB = ntl == 2 ? (tB.nr + SR - 1) / SR : 0;
+    const int S = nsA + nsB;
+
+    if (tid == 0) {
+        for (int i = 0; i < kStages; i++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tbar[i])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + tA.ld2) : "memory");
+        if (ntl == 2)
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + tB.ld2) : "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int g) {   /* thread 0: stage g of the CTA's sequence */
+        const bool b = g >= nsA;
+        const Tile &t = b ? tB : tA;
+        const int k = b ? g - nsA : g;
+        const unsigned bar = smem_addr(&tbar[g % kStages]);
+        const unsigned dst = smem_addr(stage_raw + (g % kStages) * kStageBytes);
+        const CUtensorMap *map = maps + t.ld2;
+        const int tc0 = (int)(t.a2 >> 32), tr0 = (int)(t.a2 & 0xffffffffu);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kStageBytes) : "memory");
+#pragma unroll
+        for (int bx = 0; bx < NB; bx++) tma_load_2d(dst + bx * BOXB, map, tc0 + bx * BOXW, tr0 + k * SR, bar);
+    };
+    if (tid == 0) {
+        issue(0);
+        if (S > 1) issue(1);
+    }
+
+    /* split the input slices of both tiles */
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        if (i >= ntl) break;
+        const Tile &t = i ? tB : tA;
+        Inputs &X = sxb[i];
+        const bool n0 = t.k_out0 != VK_NONE, n1 = t.k_out1 != VK_NONE;
+        if (tid < kTileCols) {
+            float h = 0.f, l = 0.f;
+            if (n0 && tid < t.nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
+            X.x0h[tid] = h; X.x0l[tid] = l; X.x0n[tid] = -h;
+        }
+        if (n1)
+            for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
+                float h = 0.f, l = 0.f;
+                if (r < t.nr) split(vec_ptr(va, t.k_in1, t.in1, v)[r], h, l);
+                X.x1h[r] = h; X.x1l[r] = l;
+            }
+    }
+    __syncthreads();
+
+    const int ng = warp % NG, cg = warp / NG;
+    /* merge the N-side partials of CTA stage g (tile t, its stage k) into out0 */
+    auto merge_rows = [&](int g, const Tile &t, int k) {
+        if (tid < SR) {
+            const int grow = k * SR + tid;
+            if (grow < t.nr) {
+                const float2 *P = npart[g & 1];
+                float h = P[tid].x, l = P[tid].y;
+#pragma unroll
+                for (int q = 1; q < NCG; q++) dfadd(h, l, P[q * SR + tid].x, P[q * SR + tid].y);
+                atomic_add_pair(vec_ptr(va, t.k_out0, t.out0, v) + grow, h, l);
+            }
+        }
+    };
+
+    float2 ch[2], cl[2];
+    int lost = -1;
+    for (int g = 0; g < S; g++) {
+        const bool b = g >= nsA;
+        const Tile &t = b ? tB : tA;
+        const Inputs &X = sxb[b ? 1 : 0];
+        const int k = b ? g - nsA : g;
+        const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
+        if (!mbar_wait(smem_addr(&tbar[g % kStages]), (unsigned)((g / kStages) & 1))) {
+            atomicOr(err, 1u);
+            lost = g;
+        }
+        __syncthreads();
+        if (g > 0) {
+            const bool pb = g - 1 >= nsA;
+            const Tile &pt = pb ? tB : tA;
+            if (pt.k_out0 != VK_NONE) merge_rows(g - 1, pt, pb ? g - 1 - nsA : g - 1);
+        }
+        if (tid == 0 && g + 2 < S) issue(g + 2);   /* its slot was freed by the barrier above */
+        if (k == 0) ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
+        const unsigned char *buf = stage_raw + (g % kStages) * kStageBytes;
+        const int nr = t.nr;
+
+        if (opN && k * SR + ng * 32 < nr) {
+            const int rr = ng * 32 + lane;
+            const unsigned char *rowp = buf + cg * BOXB + rr * kTmaBoxBytes;
+            float2 sh = make_float2(0.f, 0.f), sl = sh;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int cc = cg * 8 + j;
+                const float4 q = *reinterpret_cast<const float4 *>(rowp + 16 * (j ^ (rr & 7)));
+                if (FMT == FMT_F32) {
+                    const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
+                    const float4 xn = *reinterpret_cast<const float4 *>(X.x0n + 4 * cc);
+                    const float4 xl = *reinterpret_cast<const float4 *>(X.x0l + 4 * cc);
+                    XIn x01, x23;
+                    x01.h = make_float2(xh.x, xh.y); x01.nh = make_float2(xn.x, xn.y); x01.l = make_float2(xl.x, xl.y);
+                    x23.h = make_float2(xh.z, xh.w); x23.nh = make_float2(xn.z, xn.w); x23.l = make_float2(xl.z, xl.w);
+                    pk_cacc1(sh, sl, make_float2(q.x, q.y), x01);
+                    pk_cacc1(sh, sl, make_float2(q.z, q.w), x23);
+                } else {
+                    XIn x;
+                    x.h = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
+                    x.nh = *reinterpret_cast<const float2 *>(X.x0n + 2 * cc);
+                    x.l = *reinterpret_cast<const float2 *>(X.x0l + 2 * cc);
+                    pk_cacc2(sh, sl, make_float2(q.x, q.y), make_float2(q.z, q.w), x);
+                }
+            }
+            dfadd(sh.x, sl.x, sh.y, sl.y);
+            npart[g & 1][cg * SR + rr] = make_float2(sh.x, sl.x);
+        }
+
+        const int r0 = k * SR + warp * RW;
+        if (opT && r0 < nr) {
+            const int lb = (lane >> 3) * BOXB, lq = lane & 7;
+#pragma unroll
+            for (int i = 0; i < RW; i++) {
+                const int rr = warp * RW + i;
+                const unsigned char *row = buf + lb + rr * kTmaBoxBytes + 16 * (lq ^ (rr & 7));
+                const int r = min(r0 + i, kChunkRows - 1);
+                const XIn x1 = xin(X.x1h[r], X.x1l[r]);
+                if (FMT == FMT_F32) {
+                    const float4 q = *reinterpret_cast<const float4 *>(row);
+                    pk_cacc1(ch[0], cl[0], make_float2(q.x, q.y), x1);
+                    pk_cacc1(ch[1], cl[1], make_float2(q.z, q.w), x1);
+                } else {
+                    const float4 qa = *reinterpret_cast<const float4 *>(row);
+                    const float4 qb = *reinterpret_cast<const float4 *>(row + 4 * BOXB);
+                    pk_cacc2(ch[0], cl[0], make_float2(qa.x, qa.y), make_float2(qa.z, qa.w), x1);
+                    pk_cacc2(ch[1], cl[1], make_float2(qb.x, qb.y), make_float2(qb.z, qb.w), x1);
+                }
+            }
+        }
+
+        if (opT && k == (b ? nsB : nsA) - 1) {
+            /* the tile's column sums: reduce over the warps through this
+             * stage's slot (its next load is issued after the next barrier) */
+            __syncthreads();
+            unsigned char *rb = stage_raw + (g % kStages) * kStageBytes;
+            float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(rb);
+            float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(rb + 8 * kTileCols * 4);
+            rh[warp][lane_col<FMT>(lane, 0)] = ch[0].x;
+            rh[warp][lane_col<FMT>(lane, 1)] = ch[0].y;
+            rh[warp][lane_col<FMT>(lane, 2)] = ch[1].x;
+            rh[warp][lane_col<FMT>(lane, 3)] = ch[1].y;
+            rl[warp][lane_col<FMT>(lane, 0)] = cl[0].x;
+            rl[warp][lane_col<FMT>(lane, 1)] = cl[0].y;
+            rl[warp][lane_col<FMT>(lane, 2)] = cl[1].x;
+            rl[warp][lane_col<FMT>(lane, 3)] = cl[1].y;
+            __syncthreads();
+            double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
+            for (int c = tid; c < t.nc; c += kTileThreads) {
+                float h = rh[0][c], l = rl[0][c];
+#pragma unroll
+                for (int w = 1; w < 8; w++) dfadd(h, l, rh[w][c], rl[w][c]);
+                atomic_add_pair(out1 + c, h, l);
+            }
+        }
+    }
+    if (lost >= 0) (void)mbar_wait(smem_addr(&tbar[lost % kStages]), (unsigned)((lost / kStages) & 1));
+    __syncthreads();
+    {
+        const bool pb = S - 1 >= nsA;
+        const Tile &pt = pb ? tB : tA;
+        if (pt.k_out0 != VK_NONE) merge_rows(S - 1, pt, pb ? S - 1 - nsA : S - 1);
+    }
+}
+
 /* x[v][i] = c_i * D[v][map_i >> 1], c_i = 2 for off-diagonal shell pairs
  * (src/H2ERI_build_Coulomb.c:26-62). */
 __global__ void k_uncontract(const int *__restrict__ map, int n, const double *__restrict__ den,
@@ -956,6 +1169,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
     /* The tree sweeps are a chain of dependent launches (the critical path);
      * the near field is one large independent batch. Giving the chain's
      * stream the higher priority lets near-field tiles fill only the SMs the
@@ -1040,10 +1255,15 @@ static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int
         const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(d->tmaps);
         if (d->precision == H2ERI_GPU_FP64)
             k_tile<FMT_F64><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena, va, maps, d->err_flag_dev);
-        else if (r.pair)
-            k_tile<FMT_F32X2><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena32x2, va, maps, d->err_flag_dev);
-        else
-            k_tile<FMT_F32><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena32, va, maps, d->err_flag_dev);
+        else {
+            /* two tiles per CTA: tiles y and y + half of this launch */
+            const int n = std::min(kMaxGridY, r.count - f);
+            dim3 g2(nvec, (n + 1) / 2);
+            if (r.pair)
+                k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kTileSmemLaunch, s>>>(t, n, va, maps, d->err_flag_dev);
+            else
+                k_tile_mx<FMT_F32><<<g2, kTileThreads, kTileSmemLaunch, s>>>(t, n, va, maps, d->err_flag_dev);
+        }
     }
 }
 
