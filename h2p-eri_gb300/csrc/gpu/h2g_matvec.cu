@@ -279,16 +279,8 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
     constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage   */
     constexpr int RW = SR / 8;                            /* rows per warp    */
     constexpr int RB = kTileCols * EB;                    /* bytes per row    */
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    /* the swizzled TMA boxes need 1024-byte aligned destinations */
-    unsigned char *stage_raw = (FMT == FMT_F64)
-        ? smem_raw
-        : reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ __align__(8) unsigned long long tbar[kStages];
-    __shared__ __align__(16) float sx0h[kTileCols], sx0l[kTileCols], sx0n[kTileCols];
-    __shared__ float sx1h[kChunkRows], sx1l[kChunkRows];
-    /* N-side row partials of the FP32 formats, [stage parity][column group * SR + row] */
-    __shared__ __align__(16) float2 npart[2][256];
+    static_assert(FMT == FMT_F64, "the mixed formats use k_tile_mx");
+    extern __shared__ __align__(128) unsigned char stage_raw[];
 
     /* the vector index runs fastest: the CTAs of one tile for several
      * densities run back to back and share the tile through L2 */
@@ -382,162 +374,6 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
         return;
     }
 
-    /* ---- FP32 formats: stages arrive by TMA as NB swizzled boxes of
-     * SR rows x 128 bytes (16-byte chunk q of box row r at q ^ (r & 7)) ---- */
-    constexpr int NB = RB / kTmaBoxBytes;          /* boxes per stage: 4 (F32) or 8 (pairs) */
-    constexpr int BOXB = SR * kTmaBoxBytes;        /* bytes per box */
-    constexpr int BOXW = kTmaBoxBytes / EB;        /* elements per box row */
-    const CUtensorMap *map = maps + t.ld2;
-    const int tc0 = (int)(t.a2 >> 32), tr0 = (int)(t.a2 & 0xffffffffu);
-    if (tid == 0) {
-        for (int i = 0; i < kStages; i++)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tbar[i])) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
-    }
-    __syncthreads();
-    auto tma_stage = [&](int k) {   /* thread 0 only */
-        const unsigned bar = smem_addr(&tbar[k % kStages]);
-        const unsigned dst = smem_addr(stage_raw + (k % kStages) * kStageBytes);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kStageBytes) : "memory");
-#pragma unroll
-        for (int bx = 0; bx < NB; bx++) tma_load_2d(dst + bx * BOXB, map, tc0 + bx * BOXW, tr0 + k * SR, bar);
-    };
-    if (tid == 0) {
-        tma_stage(0);
-        if (nstage > 1) tma_stage(1);
-    }
-
-    /* split the tile's input slices once */
-    if (tid < kTileCols) {
-        float h = 0.f, l = 0.f;
-        if (opN && tid < nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
-        sx0h[tid] = h; sx0l[tid] = l; sx0n[tid] = -h;
-    }
-    if (opT)
-        for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
-            float h = 0.f, l = 0.f;
-            if (r < nr) split(vec_ptr(va, t.k_in1, t.in1, v)[r], h, l);
-            sx1h[r] = h; sx1l[r] = l;
-        }
-    __syncthreads();
-
-    /* N side: lane-per-row. A stage's SR rows form NG groups of 32; the
-     * NCG warps of a group take one box each (8 chunks, 32 or 16 columns);
-     * every lane accumulates its row over the box as even/odd column pairs,
-     * and the NCG box partials of a row are merged once per stage. Rows past
-     * the tile (a stage may hold rows of the next tile of the same matrix)
-     * are never merged. */
-    constexpr int NG = SR / 32;        /* 32-row groups per stage         */
-    constexpr int NCG = 8 / NG;        /* boxes (warps) per row group     */
-    static_assert(NCG == NB, "one box per N-side warp");
-    const int ng = warp % NG, cg = warp / NG;
-    auto merge_rows = [&](int k) {     /* partials of stage k -> out0 */
-        if (tid < SR) {
-            const int grow = k * SR + tid;
-            if (grow < nr) {
-                const float2 *P = npart[k & 1];
-                float h = P[tid].x, l = P[tid].y;
-#pragma unroll
-                for (int g = 1; g < NCG; g++) dfadd(h, l, P[g * SR + tid].x, P[g * SR + tid].y);
-                atomic_add_pair(out0 + grow, h, l);
-            }
-        }
-    };
-
-    /* T side: warp w takes rows [w*RW, (w+1)*RW) of a stage, each lane 4 columns
-     * (lane_col); column pairs (slots 0,1 and 2,3) accumulate as float pairs */
-    float2 ch[2], cl[2];
-    ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
-    int lost = -1;   /* last stage whose wait gave up */
-    for (int k = 0; k < nstage; k++) {
-        if (!mbar_wait(smem_addr(&tbar[k % kStages]), (unsigned)((k / kStages) & 1))) {
-            atomicOr(err, 1u);
-            lost = k;
-        }
-        __syncthreads();
-        if (opN && k > 0) merge_rows(k - 1);
-        if (tid == 0 && k + 2 < nstage) tma_stage(k + 2);   /* its slot was freed by the barrier above */
-        const unsigned char *buf = stage_raw + (k % kStages) * kStageBytes;
-
-        if (opN && k * SR + ng * 32 < nr) {
-            const int rr = ng * 32 + lane;
-            const unsigned char *rowp = buf + cg * BOXB + rr * kTmaBoxBytes;
-            float2 sh = make_float2(0.f, 0.f), sl = sh;
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int cc = cg * 8 + j;
-                const float4 q = *reinterpret_cast<const float4 *>(rowp + 16 * (j ^ (rr & 7)));
-                if (FMT == FMT_F32) {
-                    const float4 xh = *reinterpret_cast<const float4 *>(sx0h + 4 * cc);
-                    const float4 xn = *reinterpret_cast<const float4 *>(sx0n + 4 * cc);
-                    const float4 xl = *reinterpret_cast<const float4 *>(sx0l + 4 * cc);
-                    XIn x01, x23;
-                    x01.h = make_float2(xh.x, xh.y); x01.nh = make_float2(xn.x, xn.y); x01.l = make_float2(xl.x, xl.y);
-                    x23.h = make_float2(xh.z, xh.w); x23.nh = make_float2(xn.z, xn.w); x23.l = make_float2(xl.z, xl.w);
-                    pk_cacc1(sh, sl, make_float2(q.x, q.y), x01);
-                    pk_cacc1(sh, sl, make_float2(q.z, q.w), x23);
-                } else {
-                    XIn x;
-                    x.h = *reinterpret_cast<const float2 *>(sx0h + 2 * cc);
-                    x.nh = *reinterpret_cast<const float2 *>(sx0n + 2 * cc);
-                    x.l = *reinterpret_cast<const float2 *>(sx0l + 2 * cc);
-                    pk_cacc2(sh, sl, make_float2(q.x, q.y), make_float2(q.z, q.w), x);
-                }
-            }
-            dfadd(sh.x, sl.x, sh.y, sl.y);
-            npart[k & 1][cg * SR + rr] = make_float2(sh.x, sl.x);
-        }
-
-        const int r0 = k * SR + warp * RW;
-        if (opT && r0 < nr) {
-            const int lb = (lane >> 3) * BOXB, lq = lane & 7;
-#pragma unroll
-            for (int i = 0; i < RW; i++) {
-                const int rr = warp * RW + i;
-                const unsigned char *row = buf + lb + rr * kTmaBoxBytes + 16 * (lq ^ (rr & 7));
-                const int r = min(r0 + i, kChunkRows - 1);
-                const XIn x1 = xin(sx1h[r], sx1l[r]);
-                if (FMT == FMT_F32) {
-                    const float4 q = *reinterpret_cast<const float4 *>(row);
-                    pk_cacc1(ch[0], cl[0], make_float2(q.x, q.y), x1);
-                    pk_cacc1(ch[1], cl[1], make_float2(q.z, q.w), x1);
-                } else {
-                    const float4 qa = *reinterpret_cast<const float4 *>(row);
-                    const float4 qb = *reinterpret_cast<const float4 *>(row + 4 * BOXB);
-                    pk_cacc2(ch[0], cl[0], make_float2(qa.x, qa.y), make_float2(qa.z, qa.w), x1);
-                    pk_cacc2(ch[1], cl[1], make_float2(qb.x, qb.y), make_float2(qb.z, qb.w), x1);
-                }
-            }
-        }
-    }
-    /* a load whose wait gave up may still land: one more bounded wait before
-     * the slot is reused or the CTA exits */
-    if (lost >= 0) (void)mbar_wait(smem_addr(&tbar[lost % kStages]), (unsigned)((lost / kStages) & 1));
-    __syncthreads();
-    if (opN) merge_rows(nstage - 1);
-    if (opT) {
-        /* reduce over the warps through the last stage's slot (no copy is pending into it) */
-        unsigned char *rb = stage_raw + ((nstage - 1) % kStages) * kStageBytes;
-        float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(rb);
-        float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(rb + 8 * kTileCols * 4);
-        rh[warp][lane_col<FMT>(lane, 0)] = ch[0].x;
-        rh[warp][lane_col<FMT>(lane, 1)] = ch[0].y;
-        rh[warp][lane_col<FMT>(lane, 2)] = ch[1].x;
-        rh[warp][lane_col<FMT>(lane, 3)] = ch[1].y;
-        rl[warp][lane_col<FMT>(lane, 0)] = cl[0].x;
-        rl[warp][lane_col<FMT>(lane, 1)] = cl[0].y;
-        rl[warp][lane_col<FMT>(lane, 2)] = cl[1].x;
-        rl[warp][lane_col<FMT>(lane, 3)] = cl[1].y;
-        __syncthreads();
-        double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
-        for (int c = tid; c < nc; c += kTileThreads) {
-            float h = rh[0][c], l = rl[0][c];
-#pragma unroll
-            for (int w = 1; w < 8; w++) dfadd(h, l, rh[w][c], rl[w][c]);
-            atomic_add_pair(out1 + c, h, l);
-        }
-    }
 }
 
 /* Mixed-mode tile kernel (FP32 formats), two tiles per CTA. Stages arrive
@@ -1167,8 +1003,6 @@ static int build_rep(H2ERI_p h, DevRep *d)
     *d->err_flag = 0;
     CUDA_TRY(cudaHostGetDevicePointer((void **)&d->err_flag_dev, d->err_flag, 0));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
-    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
-    CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
     CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
     CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
     /* The tree sweeps are a chain of dependent launches (the critical path);
