@@ -601,7 +601,7 @@ def run_gpu(args):
                      "kernel": "k_tile (all tile launches of one J build)",
                      "alg_bytes_per_step": alg_bytes, "peak_kind": peak_kind,
                      "note": "achieved and traffic are per J build (all tile launches); the mixed tile kernels "
-                             "are FP32-pipe bound (compensated products), see profiles/"},
+                             "are latency-bound (16 warps per SM, stage barriers), see profiles/"},
         "cpu_baseline": {"value": cpu_v, "unit": "J builds/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": f"{cpu_n} J builds of the workload in {cpu_dt:.1f} s (oracle, OpenMP)"},
         "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},

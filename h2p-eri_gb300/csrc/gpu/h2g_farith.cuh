@@ -3,16 +3,14 @@
  *
  * A value is carried as an unevaluated sum hi + lo of two floats. Products
  * of a stored matrix entry a (one float, or a float pair) with a vector
- * entry x = xh + xl are accumulated error-free on the FP32 pipe: the product
- * fl(a xh) and its exact rounding error (from an FMA) are separated, the
- * rounded product is added to the running hi part with an error-free
- * two-sum (Knuth), and every error term goes to the lo part. Only the
- * storage rounding of a remains (2^-24 relative for single floats, ~2^-48
- * for pairs).
+ * entry x = xh + xl are accumulated on the FP32 pipe to about 2^-44 of the
+ * sum of their magnitudes, by anchored accumulation (below); partial sums are
+ * then combined with error-free two-sums (Knuth). Only the storage rounding
+ * of a matters (2^-24 relative for single floats, ~2^-48 for pairs).
  *
  * Blackwell executes two FP32 operations per instruction on 64-bit register
- * pairs (add/sub/mul/fma .f32x2); the pk_* helpers use them, so the
- * compensated update of two independent sums costs one issue slot per step.
+ * pairs (add/sub/mul/fma .f32x2); the pk_* helpers use them, so the update
+ * of two independent sums costs one issue slot per step.
  * All helpers round to nearest explicitly, so the compiler cannot contract
  * the two-sum into FMAs.
  */
@@ -58,49 +56,52 @@ __device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c)
 }
 __device__ __forceinline__ float2 bcast(float v) { return make_float2(v, v); }
 
-/* Vector entry prepared for products: (xh, xl) and -xh, each broadcast to
- * both halves of a pair. */
-struct XIn {
-    float2 h, nh, l;
-};
-__device__ __forceinline__ XIn xin(float xh, float xl)
+__device__ __forceinline__ float2 pk_abs(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+
+/* ---- anchored accumulation ----
+ * A chain of products a_i * (xh_i + xl_i) whose high parts obey
+ * sum |a_i xh_i| <= B is accumulated onto an anchor s0 = 1.5 * 2^k with
+ * 2^k > 4B. The running value s then stays in [1.25, 1.75] * 2^k, a single
+ * binade, so after s' = fma(a, xh, s) the part of the product that s' kept is
+ * exactly s' - s, and the part it dropped, a xh - (s' - s) (at most half an
+ * ulp of s), comes from a second FMA with one rounding of its own. The
+ * dropped parts and the small products a * xl go to a plain float sum l; the
+ * chain's value is (s - s0) + l, with s - s0 exact. This is five FP32
+ * operations per product where the two-sum update (error-free product, Knuth
+ * two-sum) takes eleven. The error is of order n 2^-46 B for n products
+ * (n^2 2^-46 B at worst), so the anchor is only as good as the bound: B is
+ * the computed sum |a_i| |xh_i| of the chain itself (one FMA per product),
+ * which keeps the error within a few 1e-13 of sum |a_i x_i| even when the
+ * magnitudes of a and x spread over four decades (a max|a| max|x| bound
+ * loses three more digits there). */
+
+/* The anchor 1.5 * 2^k for a chain bound b: 2^k > 4b, 2^-63 <= 2^k <= 2^123. */
+__device__ __forceinline__ float anchor_of(float b)
 {
-    XIn r;
-    r.h = bcast(xh);
-    r.nh = bcast(-xh);
-    r.l = bcast(xl);
-    return r;
+    const unsigned e = (__float_as_uint(b) >> 23) & 0xffu;   /* b < 2^(e - 126) */
+    const unsigned ek = min(max(e + 3u, 64u), 250u);
+    return __uint_as_float((ek << 23) | 0x400000u);
+}
+__device__ __forceinline__ float2 anchor2(float2 b) { return make_float2(anchor_of(b.x), anchor_of(b.y)); }
+
+/* (s, l) += a * (xh + xl) for two independent anchored chains (one per
+ * half), a single floats: 5 packed operations. */
+__device__ __forceinline__ void pk_aacc1(float2 &s, float2 &l, float2 a, float2 xh, float2 xl)
+{
+    const float2 s1 = pk_fma(a, xh, s);
+    const float2 r = pk_fma(a, xh, pk_sub(s, s1));
+    l = pk_add(pk_fma(a, xl, l), r);
+    s = s1;
 }
 
-/* (sh, sl) += a * x for two independent sums (one per half), a single
- * floats. With np = fl(a * -xh) = -fl(a xh), e = fma(a, xh, np) is the exact
- * rounding error of the product; s = sh - np is the two-sum of sh and the
- * rounded product. 11 packed operations. */
-__device__ __forceinline__ void pk_cacc1(float2 &sh, float2 &sl, float2 a, const XIn &x)
+/* Same for float-pair entries a = ah + al: 6 packed operations (the al * xl
+ * term, below 2^-48 of the product, is left out). */
+__device__ __forceinline__ void pk_aacc2(float2 &s, float2 &l, float2 ah, float2 al, float2 xh, float2 xl)
 {
-    const float2 np = pk_mul(a, x.nh);
-    const float2 e = pk_fma(a, x.h, np);
-    const float2 c = pk_fma(a, x.l, e);
-    const float2 s = pk_sub(sh, np);
-    const float2 bp = pk_sub(s, sh);
-    const float2 t2 = pk_sub(sh, pk_sub(s, bp));
-    const float2 err = pk_sub(t2, pk_add(np, bp));
-    sh = s;
-    sl = pk_add(sl, pk_add(err, c));
-}
-
-/* Same for float-pair entries a = ah + al (12 packed operations). */
-__device__ __forceinline__ void pk_cacc2(float2 &sh, float2 &sl, float2 ah, float2 al, const XIn &x)
-{
-    const float2 np = pk_mul(ah, x.nh);
-    const float2 e = pk_fma(ah, x.h, np);
-    const float2 c = pk_fma(ah, x.l, pk_fma(al, x.h, e));
-    const float2 s = pk_sub(sh, np);
-    const float2 bp = pk_sub(s, sh);
-    const float2 t2 = pk_sub(sh, pk_sub(s, bp));
-    const float2 err = pk_sub(t2, pk_add(np, bp));
-    sh = s;
-    sl = pk_add(sl, pk_add(err, c));
+    const float2 s1 = pk_fma(ah, xh, s);
+    const float2 r = pk_fma(ah, xh, pk_sub(s, s1));
+    l = pk_add(pk_fma(al, xh, pk_fma(ah, xl, l)), r);
+    s = s1;
 }
 
 /* Float-pair addition (ah + al) += (bh + bl) with an error-free two-sum on

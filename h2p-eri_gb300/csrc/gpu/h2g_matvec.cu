@@ -209,48 +209,6 @@ __device__ __forceinline__ double reduceR_f64(double *s, int lane)
     }
 }
 
-template <int R>
-__device__ __forceinline__ void reduceR_df(float *h, float *l, int lane, float &vh, float &vl)
-{
-    const bool b16 = lane & 16, b8 = lane & 8;
-    if constexpr (R == 8) {
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            float sh = b16 ? h[k] : h[k + 4], sl = b16 ? l[k] : l[k + 4];
-            float kh = b16 ? h[k + 4] : h[k], kl = b16 ? l[k + 4] : l[k];
-            dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 16), __shfl_xor_sync(0xffffffffu, sl, 16));
-            h[k] = kh; l[k] = kl;
-        }
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            float sh = b8 ? h[k] : h[k + 2], sl = b8 ? l[k] : l[k + 2];
-            float kh = b8 ? h[k + 2] : h[k], kl = b8 ? l[k + 2] : l[k];
-            dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 8), __shfl_xor_sync(0xffffffffu, sl, 8));
-            h[k] = kh; l[k] = kl;
-        }
-        const bool b4 = lane & 4;
-        float sh = b4 ? h[0] : h[1], sl = b4 ? l[0] : l[1];
-        vh = b4 ? h[1] : h[0];
-        vl = b4 ? l[1] : l[0];
-        dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, sh, 4), __shfl_xor_sync(0xffffffffu, sl, 4));
-    } else {
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            float sh = b16 ? h[k] : h[k + 2], sl = b16 ? l[k] : l[k + 2];
-            float kh = b16 ? h[k + 2] : h[k], kl = b16 ? l[k + 2] : l[k];
-            dfadd(kh, kl, __shfl_xor_sync(0xffffffffu, sh, 16), __shfl_xor_sync(0xffffffffu, sl, 16));
-            h[k] = kh; l[k] = kl;
-        }
-        float sh = b8 ? h[0] : h[1], sl = b8 ? l[0] : l[1];
-        vh = b8 ? h[1] : h[0];
-        vl = b8 ? l[1] : l[0];
-        dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, sh, 8), __shfl_xor_sync(0xffffffffu, sl, 8));
-        dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 4), __shfl_xor_sync(0xffffffffu, vl, 4));
-    }
-    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 2), __shfl_xor_sync(0xffffffffu, vl, 2));
-    dfadd(vh, vl, __shfl_xor_sync(0xffffffffu, vh, 1), __shfl_xor_sync(0xffffffffu, vl, 1));
-}
-
 /* One CTA per (vector, tile). A tile is a chunk of up to kChunkRows rows and
  * kTileCols columns. The chunk streams through a kStages-deep ring of 32 KB
  * shared-memory stages filled with cp.async (16-byte copies, any leading
@@ -260,16 +218,8 @@ __device__ __forceinline__ void reduceR_df(float *h, float *l, int lane, float &
  * [w*SR/8, (w+1)*SR/8) and each lane owns 4 columns (lane_col).
  * N-side row sums are added per stage; T-side column sums stay in registers
  * over the whole chunk and are added once (few atomics per coefficient).
- *   FMT_F64   : FP64 FMAs, FP64 reductions.
- *   FMT_F32X2 : matrix stored as float pairs; products are error-free
- *               (cacc) and partial sums are float pairs, so the result keeps
- *               ~2^-48 relative accuracy while running on the FP32 pipe.
- *   FMT_F32   : matrix stored as single floats (2^-24 storage rounding),
- *               products and sums as for float pairs, so the storage
- *               rounding is the only error (plain FP32 FMA chains roughly
- *               double it, measured 1.2e-8 vs 5e-9 on C10H22).
- * Inputs are split into float pairs once per tile in shared memory; every
- * output element is converted to FP64 once and added with an FP64 atomic. */
+ * FP64 FMAs and FP64 reductions (FMT_F64 only; the FP32 formats of the
+ * mixed mode run k_tile_mx). */
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
 k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va,
@@ -383,8 +333,16 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
  * stages are multiplied, and both tiles' input slices are split into float
  * pairs up front (two buffers), so a CTA waits once for memory, not once per
  * tile. CTA (v, y) of a launch with G CTAs per vector takes tiles y and
- * y + G. Arithmetic as in k_tile: N side lane-per-row with per-stage merges
- * of the box partials, T side lanes over columns with float-pair sums. */
+ * y + G. N side lane-per-row (one box of a row per lane) with per-stage
+ * merges of the box partials; T side lanes over columns, with float-pair
+ * column sums over the tile. Products are accumulated in anchored chains
+ * (h2g_farith.cuh): per lane, one chain per box of a row (N) or per column
+ * over the warp's rows of a stage (T), each anchored on its own bound
+ * sum |a| |xh|, so the only error that matters is the storage rounding of the
+ * matrix (2^-24 relative for FMT_F32, ~2^-48 for FMT_F32X2; plain FP32 FMA
+ * chains roughly double it, measured 1.2e-8 vs 5e-9 on C10H22). Inputs are
+ * split into float pairs once per tile; every output element is converted to
+ * FP64 once and added with FP64 atomics. */
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
 k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ VecArgs va,
@@ -405,7 +363,7 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     __shared__ __align__(8) unsigned long long tbar[kStages];
     struct Inputs {
-        float x0h[kTileCols], x0l[kTileCols], x0n[kTileCols], x1h[kChunkRows], x1l[kChunkRows];
+        float x0h[kTileCols], x0l[kTileCols], x0a[kTileCols], x1h[kChunkRows], x1l[kChunkRows];
     };
     __shared__ __align__(16) Inputs sxb[2];
     __shared__ __align__(16) float2 npart[2][256];
@@ -455,7 +413,7 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
         if (tid < kTileCols) {
             float h = 0.f, l = 0.f;
             if (n0 && tid < t.nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
-            X.x0h[tid] = h; X.x0l[tid] = l; X.x0n[tid] = -h;
+            X.x0h[tid] = h; X.x0l[tid] = l; X.x0a[tid] = fabsf(h);
         }
         if (n1)
             for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
@@ -505,54 +463,86 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
         const int nr = t.nr;
 
         if (opN && k * SR + ng * 32 < nr) {
+            /* the lane's row over one box: two anchored chains (even and odd
+             * columns), bounded by their own sums |a| |xh| */
             const int rr = ng * 32 + lane;
             const unsigned char *rowp = buf + cg * BOXB + rr * kTmaBoxBytes;
-            float2 sh = make_float2(0.f, 0.f), sl = sh;
+            float4 q[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) q[j] = *reinterpret_cast<const float4 *>(rowp + 16 * (j ^ (rr & 7)));
+            float2 bnd = make_float2(0.f, 0.f);
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const int cc = cg * 8 + j;
-                const float4 q = *reinterpret_cast<const float4 *>(rowp + 16 * (j ^ (rr & 7)));
                 if (FMT == FMT_F32) {
-                    const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
-                    const float4 xn = *reinterpret_cast<const float4 *>(X.x0n + 4 * cc);
-                    const float4 xl = *reinterpret_cast<const float4 *>(X.x0l + 4 * cc);
-                    XIn x01, x23;
-                    x01.h = make_float2(xh.x, xh.y); x01.nh = make_float2(xn.x, xn.y); x01.l = make_float2(xl.x, xl.y);
-                    x23.h = make_float2(xh.z, xh.w); x23.nh = make_float2(xn.z, xn.w); x23.l = make_float2(xl.z, xl.w);
-                    pk_cacc1(sh, sl, make_float2(q.x, q.y), x01);
-                    pk_cacc1(sh, sl, make_float2(q.z, q.w), x23);
+                    const float4 xa = *reinterpret_cast<const float4 *>(X.x0a + 4 * cc);
+                    bnd = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), make_float2(xa.x, xa.y), bnd);
+                    bnd = pk_fma(pk_abs(make_float2(q[j].z, q[j].w)), make_float2(xa.z, xa.w), bnd);
                 } else {
-                    XIn x;
-                    x.h = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
-                    x.nh = *reinterpret_cast<const float2 *>(X.x0n + 2 * cc);
-                    x.l = *reinterpret_cast<const float2 *>(X.x0l + 2 * cc);
-                    pk_cacc2(sh, sl, make_float2(q.x, q.y), make_float2(q.z, q.w), x);
+                    const float2 xa = *reinterpret_cast<const float2 *>(X.x0a + 2 * cc);
+                    bnd = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), xa, bnd);
                 }
             }
-            dfadd(sh.x, sl.x, sh.y, sl.y);
-            npart[g & 1][cg * SR + rr] = make_float2(sh.x, sl.x);
+            const float2 s0 = anchor2(bnd);
+            float2 sa = s0, la = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int cc = cg * 8 + j;
+                if (FMT == FMT_F32) {
+                    const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
+                    const float4 xl = *reinterpret_cast<const float4 *>(X.x0l + 4 * cc);
+                    pk_aacc1(sa, la, make_float2(q[j].x, q[j].y), make_float2(xh.x, xh.y), make_float2(xl.x, xl.y));
+                    pk_aacc1(sa, la, make_float2(q[j].z, q[j].w), make_float2(xh.z, xh.w), make_float2(xl.z, xl.w));
+                } else {
+                    const float2 xh = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
+                    const float2 xl = *reinterpret_cast<const float2 *>(X.x0l + 2 * cc);
+                    pk_aacc2(sa, la, make_float2(q[j].x, q[j].y), make_float2(q[j].z, q[j].w), xh, xl);
+                }
+            }
+            const float2 hi = pk_sub(sa, s0);   /* exact */
+            float h = hi.x, l = la.x;
+            dfadd(h, l, hi.y, la.y);
+            npart[g & 1][cg * SR + rr] = make_float2(h, l);
         }
 
         const int r0 = k * SR + warp * RW;
         if (opT && r0 < nr) {
+            /* the lane's 4 columns over the warp's RW rows of this stage:
+             * anchored chains per column, folded into the tile's float-pair
+             * column sums once per stage */
             const int lb = (lane >> 3) * BOXB, lq = lane & 7;
+            float4 qa[RW], qb[RW];
 #pragma unroll
             for (int i = 0; i < RW; i++) {
                 const int rr = warp * RW + i;
                 const unsigned char *row = buf + lb + rr * kTmaBoxBytes + 16 * (lq ^ (rr & 7));
+                qa[i] = *reinterpret_cast<const float4 *>(row);
+                if (FMT == FMT_F32X2) qb[i] = *reinterpret_cast<const float4 *>(row + 4 * BOXB);
+            }
+            float2 b0 = make_float2(0.f, 0.f), b1 = b0;
+#pragma unroll
+            for (int i = 0; i < RW; i++) {
+                const float2 xa = bcast(fabsf(X.x1h[min(r0 + i, kChunkRows - 1)]));
+                b0 = pk_fma(pk_abs(make_float2(qa[i].x, qa[i].y)), xa, b0);
+                if (FMT == FMT_F32) b1 = pk_fma(pk_abs(make_float2(qa[i].z, qa[i].w)), xa, b1);
+                else b1 = pk_fma(pk_abs(make_float2(qb[i].x, qb[i].y)), xa, b1);
+            }
+            const float2 s0 = anchor2(b0), s1 = anchor2(b1);
+            float2 sa = s0, sb = s1, la = make_float2(0.f, 0.f), lb2 = la;
+#pragma unroll
+            for (int i = 0; i < RW; i++) {
                 const int r = min(r0 + i, kChunkRows - 1);
-                const XIn x1 = xin(X.x1h[r], X.x1l[r]);
+                const float2 xh = bcast(X.x1h[r]), xl = bcast(X.x1l[r]);
                 if (FMT == FMT_F32) {
-                    const float4 q = *reinterpret_cast<const float4 *>(row);
-                    pk_cacc1(ch[0], cl[0], make_float2(q.x, q.y), x1);
-                    pk_cacc1(ch[1], cl[1], make_float2(q.z, q.w), x1);
+                    pk_aacc1(sa, la, make_float2(qa[i].x, qa[i].y), xh, xl);
+                    pk_aacc1(sb, lb2, make_float2(qa[i].z, qa[i].w), xh, xl);
                 } else {
-                    const float4 qa = *reinterpret_cast<const float4 *>(row);
-                    const float4 qb = *reinterpret_cast<const float4 *>(row + 4 * BOXB);
-                    pk_cacc2(ch[0], cl[0], make_float2(qa.x, qa.y), make_float2(qa.z, qa.w), x1);
-                    pk_cacc2(ch[1], cl[1], make_float2(qb.x, qb.y), make_float2(qb.z, qb.w), x1);
+                    pk_aacc2(sa, la, make_float2(qa[i].x, qa[i].y), make_float2(qa[i].z, qa[i].w), xh, xl);
+                    pk_aacc2(sb, lb2, make_float2(qb[i].x, qb[i].y), make_float2(qb[i].z, qb[i].w), xh, xl);
                 }
             }
+            pk_dfadd(ch[0], cl[0], pk_sub(sa, s0), la);
+            pk_dfadd(ch[1], cl[1], pk_sub(sb, s1), lb2);
         }
 
         if (opT && k == (b ? nsB : nsA) - 1) {
