@@ -84,23 +84,26 @@ __device__ __forceinline__ float anchor_of(float b)
 }
 __device__ __forceinline__ float2 anchor2(float2 b) { return make_float2(anchor_of(b.x), anchor_of(b.y)); }
 
-/* (s, l) += a * (xh + xl) for two independent anchored chains (one per
- * half), a single floats: 5 packed operations. */
-__device__ __forceinline__ void pk_aacc1(float2 &s, float2 &l, float2 a, float2 xh, float2 xl)
+/* (s, l1 + l2) += a * (xh + xl) for two independent anchored chains (one
+ * per half), a single floats: 5 packed operations. The low part is kept as
+ * two sums (dropped parts, small products) so that every running sum takes
+ * one dependent operation per product. */
+__device__ __forceinline__ void pk_aacc1(float2 &s, float2 &l1, float2 &l2, float2 a, float2 xh, float2 xl)
 {
     const float2 s1 = pk_fma(a, xh, s);
-    const float2 r = pk_fma(a, xh, pk_sub(s, s1));
-    l = pk_add(pk_fma(a, xl, l), r);
+    l1 = pk_add(l1, pk_fma(a, xh, pk_sub(s, s1)));
+    l2 = pk_fma(a, xl, l2);
     s = s1;
 }
 
 /* Same for float-pair entries a = ah + al: 6 packed operations (the al * xl
  * term, below 2^-48 of the product, is left out). */
-__device__ __forceinline__ void pk_aacc2(float2 &s, float2 &l, float2 ah, float2 al, float2 xh, float2 xl)
+__device__ __forceinline__ void pk_aacc2(float2 &s, float2 &l1, float2 &l2, float2 ah, float2 al, float2 xh,
+                                         float2 xl)
 {
     const float2 s1 = pk_fma(ah, xh, s);
-    const float2 r = pk_fma(ah, xh, pk_sub(s, s1));
-    l = pk_add(pk_fma(al, xh, pk_fma(ah, xl, l)), r);
+    l1 = pk_add(l1, pk_fma(al, xh, pk_fma(ah, xh, pk_sub(s, s1))));
+    l2 = pk_fma(ah, xl, l2);
     s = s1;
 }
 

@@ -326,50 +326,79 @@ k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const _
 
 }
 
+/* Shared memory of k_tile_mx (dynamic, laid out here): the stage ring first
+ * (TMA destinations with the 128-byte swizzle must start on 1024-byte
+ * boundaries; the kernel checks and refuses otherwise), then the N-side box
+ * partials of the stages in flight, the split inputs of both tiles, the
+ * stage mbarriers and the slot and row-group counters. Two CTAs fit in one
+ * SM (2 x (112 KB + 1 KB reserved) of 228 KB). */
+struct MxInputs {
+    float x0h[kTileCols], x0l[kTileCols], x1h[kChunkRows], x1l[kChunkRows];
+};
+struct MxSmem {
+    unsigned char ring[kStages][kStageBytes];
+    float2 npart[kStages][256];
+    MxInputs sx[2];
+    unsigned long long full[kStages];
+    int slot_cnt[kStages];
+    int grp_cnt[kStages][2];
+    int dead;
+};
+constexpr size_t kMxSmem = (sizeof(MxSmem) + 127) & ~size_t(127);
+
 /* Mixed-mode tile kernel (FP32 formats), two tiles per CTA. Stages arrive
  * by TMA as NB swizzled boxes of SR rows x 128 bytes (16-byte chunk q of box
  * row r at q ^ (r & 7)) into a kStages-deep ring that runs across both
- * tiles: the second tile's first stages load while the first tile's last
- * stages are multiplied, and both tiles' input slices are split into float
- * pairs up front (two buffers), so a CTA waits once for memory, not once per
- * tile. CTA (v, y) of a launch with G CTAs per vector takes tiles y and
- * y + G. N side lane-per-row (one box of a row per lane) with per-stage
- * merges of the box partials; T side lanes over columns, with float-pair
- * column sums over the tile. Products are accumulated in anchored chains
- * (h2g_farith.cuh): per lane, one chain per box of a row (N) or per column
- * over the warp's rows of a stage (T), each anchored on its own bound
- * sum |a| |xh|, so the only error that matters is the storage rounding of the
- * matrix (2^-24 relative for FMT_F32, ~2^-48 for FMT_F32X2; plain FP32 FMA
- * chains roughly double it, measured 1.2e-8 vs 5e-9 on C10H22). Inputs are
- * split into float pairs once per tile; every output element is converted to
- * FP64 once and added with FP64 atomics. */
+ * tiles; both tiles' input slices are split into float pairs up front. CTA
+ * (v, y) of a launch with G CTAs per vector takes tiles y and y + G.
+ *
+ * The warps never wait for one another inside the loop, only for their
+ * data: the last warp to finish with a ring slot (a shared counter) reloads
+ * it with the stage kStages ahead, so up to kStages stages are in flight and
+ * a warp that is done with a short stage moves on to the next one.
+ *   N side: lane per row; warp (ng, cg) takes rows [32 ng, 32 ng + 32) of a
+ *     stage over box cg; the box partials of a row group are merged by the
+ *     last of its warps to finish (a second counter) and added to out0.
+ *   T side: warp w owns a strip of 16-byte chunks of every row (4 chunks of
+ *     box w / 2 for single floats, all 8 chunks of box w for pairs); its
+ *     lanes split the strip's chunks and the stage's rows, so the column
+ *     sums of a tile are reduced inside the warp (shuffles) and added once.
+ * Products are accumulated in anchored chains (h2g_farith.cuh): per lane, one
+ * chain per box of a row (N) or per column over the lane's rows of a stage
+ * (T), anchored on its own bound sum |a| |xh|, so the only error that
+ * matters is the storage rounding of the matrix (2^-24 relative for FMT_F32,
+ * ~2^-48 for FMT_F32X2; plain FP32 FMA chains roughly double it, measured
+ * 1.2e-8 vs 5e-9 on C10H22). Every output element is converted to FP64 once
+ * and added with FP64 atomics. */
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
 k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ VecArgs va,
           const CUtensorMap *__restrict__ maps, unsigned *err)
 {
     constexpr int EB = FmtInfo<FMT>::ebytes;
-    constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage        */
-    constexpr int RW = SR / 8;                            /* T-side rows per warp  */
-    constexpr int RB = kTileCols * EB;                    /* bytes per stage row   */
-    constexpr int NB = RB / kTmaBoxBytes;                 /* boxes per stage       */
-    constexpr int BOXB = SR * kTmaBoxBytes;               /* bytes per box         */
-    constexpr int BOXW = kTmaBoxBytes / EB;               /* elements per box row  */
-    constexpr int NG = SR / 32;                           /* N-side 32-row groups  */
-    constexpr int NCG = 8 / NG;                           /* boxes (warps) per group */
+    constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage: 64 or 32   */
+    constexpr int RB = kTileCols * EB;                    /* bytes per stage row        */
+    constexpr int NB = RB / kTmaBoxBytes;                 /* boxes per stage: 4 or 8    */
+    constexpr int BOXB = SR * kTmaBoxBytes;               /* bytes per box              */
+    constexpr int BOXW = kTmaBoxBytes / EB;               /* elements per box row       */
+    constexpr int NG = SR / 32;                           /* N-side 32-row groups       */
+    constexpr int NCG = 8 / NG;                           /* boxes (warps) per group    */
     static_assert(NCG == NB, "one box per N-side warp");
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    unsigned char *stage_raw =
-        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ __align__(8) unsigned long long tbar[kStages];
-    struct Inputs {
-        float x0h[kTileCols], x0l[kTileCols], x0a[kTileCols], x1h[kChunkRows], x1l[kChunkRows];
-    };
-    __shared__ __align__(16) Inputs sxb[2];
-    __shared__ __align__(16) float2 npart[2][256];
+    constexpr int NW = kTileThreads / 32;
+    constexpr int TC = (FMT == FMT_F32) ? 4 : 8;          /* T side: chunks per warp row */
+    constexpr int TL = 32 / TC;                           /* T side: row lanes          */
+    constexpr int TR = SR / TL;                           /* T side: rows per lane      */
+    static_assert(TR == 8, "T-side lane layout");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MxSmem &sm = *reinterpret_cast<MxSmem *>(smem_raw);
+    volatile int *dead = &sm.dead;
 
-    const int v = blockIdx.x, G = gridDim.y;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (smem_addr(sm.ring) & 1023u) {   /* the same for every thread: nothing has started */
+        if (tid == 0) atomicOr(err, 2u);
+        return;
+    }
+    const int v = blockIdx.x, G = gridDim.y;
     const int ti0 = blockIdx.y, ti1 = blockIdx.y + G;
     const int ntl = ti1 < n_tiles ? 2 : 1;
     const Tile tA = tiles[ti0];
@@ -377,21 +406,12 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
     const int nsA = (tA.nr + SR - 1) / SR, nsB = ntl == 2 ? (tB.nr + SR - 1) / SR : 0;
     const int S = nsA + nsB;
 
-    if (tid == 0) {
-        for (int i = 0; i < kStages; i++)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tbar[i])) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + tA.ld2) : "memory");
-        if (ntl == 2)
-            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + tB.ld2) : "memory");
-    }
-    __syncthreads();
-    auto issue = [&](int g) {   /* thread 0: stage g of the CTA's sequence */
+    auto issue = [&](int g) {   /* one thread: stage g of the CTA's sequence into slot g % kStages */
         const bool b = g >= nsA;
         const Tile &t = b ? tB : tA;
         const int k = b ? g - nsA : g;
-        const unsigned bar = smem_addr(&tbar[g % kStages]);
-        const unsigned dst = smem_addr(stage_raw + (g % kStages) * kStageBytes);
+        const unsigned bar = smem_addr(&sm.full[g % kStages]);
+        const unsigned dst = smem_addr(sm.ring[g % kStages]);
         const CUtensorMap *map = maps + t.ld2;
         const int tc0 = (int)(t.a2 >> 32), tr0 = (int)(t.a2 & 0xffffffffu);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kStageBytes) : "memory");
@@ -399,8 +419,17 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
         for (int bx = 0; bx < NB; bx++) tma_load_2d(dst + bx * BOXB, map, tc0 + bx * BOXW, tr0 + k * SR, bar);
     };
     if (tid == 0) {
-        issue(0);
-        if (S > 1) issue(1);
+        for (int i = 0; i < kStages; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&sm.full[i])) : "memory");
+            sm.slot_cnt[i] = 0;
+            sm.grp_cnt[i][0] = sm.grp_cnt[i][1] = 0;
+        }
+        sm.dead = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + tA.ld2) : "memory");
+        if (ntl == 2)
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + tB.ld2) : "memory");
+        for (int g = 0; g < kStages && g < S; g++) issue(g);
     }
 
     /* split the input slices of both tiles */
@@ -408,12 +437,12 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
     for (int i = 0; i < 2; i++) {
         if (i >= ntl) break;
         const Tile &t = i ? tB : tA;
-        Inputs &X = sxb[i];
+        MxInputs &X = sm.sx[i];
         const bool n0 = t.k_out0 != VK_NONE, n1 = t.k_out1 != VK_NONE;
         if (tid < kTileCols) {
             float h = 0.f, l = 0.f;
             if (n0 && tid < t.nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
-            X.x0h[tid] = h; X.x0l[tid] = l; X.x0a[tid] = fabsf(h);
+            X.x0h[tid] = h; X.x0l[tid] = l;
         }
         if (n1)
             for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
@@ -422,44 +451,32 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
                 X.x1h[r] = h; X.x1l[r] = l;
             }
     }
-    __syncthreads();
+    __syncthreads();   /* inputs, barriers and counters ready; the only CTA-wide barrier */
 
     const int ng = warp % NG, cg = warp / NG;
-    /* merge the N-side partials of CTA stage g (tile t, its stage k) into out0 */
-    auto merge_rows = [&](int g, const Tile &t, int k) {
-        if (tid < SR) {
-            const int grow = k * SR + tid;
-            if (grow < t.nr) {
-                const float2 *P = npart[g & 1];
-                float h = P[tid].x, l = P[tid].y;
-#pragma unroll
-                for (int q = 1; q < NCG; q++) dfadd(h, l, P[q * SR + tid].x, P[q * SR + tid].y);
-                atomic_add_pair(vec_ptr(va, t.k_out0, t.out0, v) + grow, h, l);
-            }
-        }
-    };
-
+    const int tb = (FMT == FMT_F32) ? warp >> 1 : warp;                 /* T side: box      */
+    /* T side: chunk and row lane. A 16-byte load is served per quarter warp
+     * (8 lanes), which must hit 8 different chunk positions: with 4 chunks
+     * per row lane (single floats) a quarter warp takes rows r and r + 4,
+     * whose swizzles map the 4 chunks to the two halves of the line. */
+    const int tq = ((FMT == FMT_F32) ? (warp & 1) * 4 : 0) + lane % TC;
+    const int trl = (FMT == FMT_F32) ? (lane >> 3) + 4 * ((lane >> 2) & 1) : lane / TC;
     float2 ch[2], cl[2];
     int lost = -1;
     for (int g = 0; g < S; g++) {
         const bool b = g >= nsA;
         const Tile &t = b ? tB : tA;
-        const Inputs &X = sxb[b ? 1 : 0];
+        const MxInputs &X = sm.sx[b ? 1 : 0];
         const int k = b ? g - nsA : g;
+        const int slot = g % kStages;
         const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
-        if (!mbar_wait(smem_addr(&tbar[g % kStages]), (unsigned)((g / kStages) & 1))) {
+        if (!*dead && !mbar_wait(smem_addr(&sm.full[slot]), (unsigned)((g / kStages) & 1))) {
             atomicOr(err, 1u);
+            *dead = 1;
             lost = g;
         }
-        __syncthreads();
-        if (g > 0) {
-            const bool pb = g - 1 >= nsA;
-            const Tile &pt = pb ? tB : tA;
-            if (pt.k_out0 != VK_NONE) merge_rows(g - 1, pt, pb ? g - 1 - nsA : g - 1);
-        }
-        if (tid == 0 && g + 2 < S) issue(g + 2);   /* its slot was freed by the barrier above */
         if (k == 0) ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
-        const unsigned char *buf = stage_raw + (g % kStages) * kStageBytes;
+        const unsigned char *buf = sm.ring[slot];
         const int nr = t.nr;
 
         if (opN && k * SR + ng * 32 < nr) {
@@ -470,113 +487,159 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
             float4 q[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) q[j] = *reinterpret_cast<const float4 *>(rowp + 16 * (j ^ (rr & 7)));
-            float2 bnd = make_float2(0.f, 0.f);
+            float2 b0 = make_float2(0.f, 0.f), b1 = b0;
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const int cc = cg * 8 + j;
                 if (FMT == FMT_F32) {
-                    const float4 xa = *reinterpret_cast<const float4 *>(X.x0a + 4 * cc);
-                    bnd = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), make_float2(xa.x, xa.y), bnd);
-                    bnd = pk_fma(pk_abs(make_float2(q[j].z, q[j].w)), make_float2(xa.z, xa.w), bnd);
+                    const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
+                    b0 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(make_float2(xh.x, xh.y)), b0);
+                    b1 = pk_fma(pk_abs(make_float2(q[j].z, q[j].w)), pk_abs(make_float2(xh.z, xh.w)), b1);
                 } else {
-                    const float2 xa = *reinterpret_cast<const float2 *>(X.x0a + 2 * cc);
-                    bnd = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), xa, bnd);
+                    const float2 xh = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
+                    if (j & 1) b1 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(xh), b1);
+                    else b0 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(xh), b0);
                 }
             }
-            const float2 s0 = anchor2(bnd);
-            float2 sa = s0, la = make_float2(0.f, 0.f);
+            /* two chains per half on one anchor (bounded by both): their high
+             * parts are multiples of one ulp below 2^(k-2) and add exactly */
+            const float2 s0 = anchor2(pk_add(b0, b1)), z = make_float2(0.f, 0.f);
+            float2 sa = s0, sb = s0, la1 = z, la2 = z, lb1 = z, lb2 = z;
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const int cc = cg * 8 + j;
                 if (FMT == FMT_F32) {
                     const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
                     const float4 xl = *reinterpret_cast<const float4 *>(X.x0l + 4 * cc);
-                    pk_aacc1(sa, la, make_float2(q[j].x, q[j].y), make_float2(xh.x, xh.y), make_float2(xl.x, xl.y));
-                    pk_aacc1(sa, la, make_float2(q[j].z, q[j].w), make_float2(xh.z, xh.w), make_float2(xl.z, xl.w));
+                    pk_aacc1(sa, la1, la2, make_float2(q[j].x, q[j].y), make_float2(xh.x, xh.y), make_float2(xl.x, xl.y));
+                    pk_aacc1(sb, lb1, lb2, make_float2(q[j].z, q[j].w), make_float2(xh.z, xh.w), make_float2(xl.z, xl.w));
                 } else {
                     const float2 xh = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
                     const float2 xl = *reinterpret_cast<const float2 *>(X.x0l + 2 * cc);
-                    pk_aacc2(sa, la, make_float2(q[j].x, q[j].y), make_float2(q[j].z, q[j].w), xh, xl);
+                    if (j & 1) pk_aacc2(sb, lb1, lb2, make_float2(q[j].x, q[j].y), make_float2(q[j].z, q[j].w), xh, xl);
+                    else pk_aacc2(sa, la1, la2, make_float2(q[j].x, q[j].y), make_float2(q[j].z, q[j].w), xh, xl);
                 }
             }
-            const float2 hi = pk_sub(sa, s0);   /* exact */
-            float h = hi.x, l = la.x;
-            dfadd(h, l, hi.y, la.y);
-            npart[g & 1][cg * SR + rr] = make_float2(h, l);
+            const float2 hi = pk_add(pk_sub(sa, s0), pk_sub(sb, s0));   /* exact */
+            const float2 lo = pk_add(pk_add(la1, la2), pk_add(lb1, lb2));
+            float h = hi.x, l = lo.x;
+            dfadd(h, l, hi.y, lo.y);
+            sm.npart[slot][cg * SR + rr] = make_float2(h, l);
         }
 
-        const int r0 = k * SR + warp * RW;
-        if (opT && r0 < nr) {
-            /* the lane's 4 columns over the warp's RW rows of this stage:
-             * anchored chains per column, folded into the tile's float-pair
-             * column sums once per stage */
-            const int lb = (lane >> 3) * BOXB, lq = lane & 7;
-            float4 qa[RW], qb[RW];
+        if (opT) {
+            /* the lane's chunk over rows trl + TL i of the stage: anchored
+             * chains per column, folded into the tile's float-pair column
+             * sums once per stage. Rows past the tile have zero inputs. */
+            float4 q[TR];
 #pragma unroll
-            for (int i = 0; i < RW; i++) {
-                const int rr = warp * RW + i;
-                const unsigned char *row = buf + lb + rr * kTmaBoxBytes + 16 * (lq ^ (rr & 7));
-                qa[i] = *reinterpret_cast<const float4 *>(row);
-                if (FMT == FMT_F32X2) qb[i] = *reinterpret_cast<const float4 *>(row + 4 * BOXB);
+            for (int i = 0; i < TR; i++) {
+                const int rr = trl + TL * i;
+                q[i] = *reinterpret_cast<const float4 *>(buf + tb * BOXB + rr * kTmaBoxBytes + 16 * (tq ^ (rr & 7)));
             }
+            const float *x1h = X.x1h + k * SR + trl, *x1l = X.x1l + k * SR + trl;
             float2 b0 = make_float2(0.f, 0.f), b1 = b0;
 #pragma unroll
-            for (int i = 0; i < RW; i++) {
-                const float2 xa = bcast(fabsf(X.x1h[min(r0 + i, kChunkRows - 1)]));
-                b0 = pk_fma(pk_abs(make_float2(qa[i].x, qa[i].y)), xa, b0);
-                if (FMT == FMT_F32) b1 = pk_fma(pk_abs(make_float2(qa[i].z, qa[i].w)), xa, b1);
-                else b1 = pk_fma(pk_abs(make_float2(qb[i].x, qb[i].y)), xa, b1);
-            }
-            const float2 s0 = anchor2(b0), s1 = anchor2(b1);
-            float2 sa = s0, sb = s1, la = make_float2(0.f, 0.f), lb2 = la;
-#pragma unroll
-            for (int i = 0; i < RW; i++) {
-                const int r = min(r0 + i, kChunkRows - 1);
-                const float2 xh = bcast(X.x1h[r]), xl = bcast(X.x1l[r]);
+            for (int i = 0; i < TR; i++) {
+                const float2 xa = bcast(fabsf(x1h[TL * i]));
                 if (FMT == FMT_F32) {
-                    pk_aacc1(sa, la, make_float2(qa[i].x, qa[i].y), xh, xl);
-                    pk_aacc1(sb, lb2, make_float2(qa[i].z, qa[i].w), xh, xl);
+                    b0 = pk_fma(pk_abs(make_float2(q[i].x, q[i].y)), xa, b0);
+                    b1 = pk_fma(pk_abs(make_float2(q[i].z, q[i].w)), xa, b1);
                 } else {
-                    pk_aacc2(sa, la, make_float2(qa[i].x, qa[i].y), make_float2(qa[i].z, qa[i].w), xh, xl);
-                    pk_aacc2(sb, lb2, make_float2(qb[i].x, qb[i].y), make_float2(qb[i].z, qb[i].w), xh, xl);
+                    b0 = pk_fma(pk_abs(make_float2(q[i].x, q[i].y)), xa, b0);
                 }
             }
-            pk_dfadd(ch[0], cl[0], pk_sub(sa, s0), la);
-            pk_dfadd(ch[1], cl[1], pk_sub(sb, s1), lb2);
+            if (FMT == FMT_F32) {
+                const float2 s0 = anchor2(b0), s1 = anchor2(b1), z = make_float2(0.f, 0.f);
+                float2 sa = s0, sb = s1, la1 = z, la2 = z, lb1 = z, lb2 = z;
+#pragma unroll
+                for (int i = 0; i < TR; i++) {
+                    const float2 xh = bcast(x1h[TL * i]), xl = bcast(x1l[TL * i]);
+                    pk_aacc1(sa, la1, la2, make_float2(q[i].x, q[i].y), xh, xl);
+                    pk_aacc1(sb, lb1, lb2, make_float2(q[i].z, q[i].w), xh, xl);
+                }
+                pk_dfadd(ch[0], cl[0], pk_sub(sa, s0), pk_add(la1, la2));
+                pk_dfadd(ch[1], cl[1], pk_sub(sb, s1), pk_add(lb1, lb2));
+            } else {
+                /* two chains over alternate rows on one anchor: their high
+                 * parts are multiples of one ulp below 2^(k-2), so they add
+                 * exactly */
+                const float2 s0 = anchor2(b0), z = make_float2(0.f, 0.f);
+                float2 sa = s0, sb = s0, la1 = z, la2 = z, lb1 = z, lb2 = z;
+#pragma unroll
+                for (int i = 0; i < TR; i += 2) {
+                    const float2 xh0 = bcast(x1h[TL * i]), xl0 = bcast(x1l[TL * i]);
+                    const float2 xh1 = bcast(x1h[TL * (i + 1)]), xl1 = bcast(x1l[TL * (i + 1)]);
+                    pk_aacc2(sa, la1, la2, make_float2(q[i].x, q[i].y), make_float2(q[i].z, q[i].w), xh0, xl0);
+                    pk_aacc2(sb, lb1, lb2, make_float2(q[i + 1].x, q[i + 1].y), make_float2(q[i + 1].z, q[i + 1].w), xh1,
+                             xl1);
+                }
+                pk_dfadd(ch[0], cl[0], pk_add(pk_sub(sa, s0), pk_sub(sb, s0)),
+                         pk_add(pk_add(la1, la2), pk_add(lb1, lb2)));
+            }
+            if (k == (b ? nsB : nsA) - 1) {
+                /* tile done: reduce the column sums over the row lanes */
+#pragma unroll
+                for (int off = TC; off < 32; off <<= 1)
+#pragma unroll
+                    for (int j = 0; j < (FMT == FMT_F32 ? 2 : 1); j++) {
+                        const float2 oh = make_float2(__shfl_xor_sync(0xffffffffu, ch[j].x, off),
+                                                      __shfl_xor_sync(0xffffffffu, ch[j].y, off));
+                        const float2 ol = make_float2(__shfl_xor_sync(0xffffffffu, cl[j].x, off),
+                                                      __shfl_xor_sync(0xffffffffu, cl[j].y, off));
+                        pk_dfadd(ch[j], cl[j], oh, ol);
+                    }
+                if (trl == 0) {
+                    double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
+                    if (FMT == FMT_F32) {
+                        const int c = tb * 32 + tq * 4;
+                        if (c < t.nc) atomic_add_pair(out1 + c, ch[0].x, cl[0].x);
+                        if (c + 1 < t.nc) atomic_add_pair(out1 + c + 1, ch[0].y, cl[0].y);
+                        if (c + 2 < t.nc) atomic_add_pair(out1 + c + 2, ch[1].x, cl[1].x);
+                        if (c + 3 < t.nc) atomic_add_pair(out1 + c + 3, ch[1].y, cl[1].y);
+                    } else {
+                        const int c = tb * 16 + tq * 2;
+                        if (c < t.nc) atomic_add_pair(out1 + c, ch[0].x, cl[0].x);
+                        if (c + 1 < t.nc) atomic_add_pair(out1 + c + 1, ch[0].y, cl[0].y);
+                    }
+                }
+            }
         }
 
-        if (opT && k == (b ? nsB : nsA) - 1) {
-            /* the tile's column sums: reduce over the warps through this
-             * stage's slot (its next load is issued after the next barrier) */
-            __syncthreads();
-            unsigned char *rb = stage_raw + (g % kStages) * kStageBytes;
-            float (*rh)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(rb);
-            float (*rl)[kTileCols] = reinterpret_cast<float (*)[kTileCols]>(rb + 8 * kTileCols * 4);
-            rh[warp][lane_col<FMT>(lane, 0)] = ch[0].x;
-            rh[warp][lane_col<FMT>(lane, 1)] = ch[0].y;
-            rh[warp][lane_col<FMT>(lane, 2)] = ch[1].x;
-            rh[warp][lane_col<FMT>(lane, 3)] = ch[1].y;
-            rl[warp][lane_col<FMT>(lane, 0)] = cl[0].x;
-            rl[warp][lane_col<FMT>(lane, 1)] = cl[0].y;
-            rl[warp][lane_col<FMT>(lane, 2)] = cl[1].x;
-            rl[warp][lane_col<FMT>(lane, 3)] = cl[1].y;
-            __syncthreads();
-            double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
-            for (int c = tid; c < t.nc; c += kTileThreads) {
-                float h = rh[0][c], l = rl[0][c];
+        __syncwarp();
+        if (opN) {
+            /* the last warp of the row group merges the group's box partials */
+            int last = 0;
+            if (lane == 0) {
+                __threadfence_block();
+                last = atomicAdd(&sm.grp_cnt[slot][ng], 1) == NCG - 1;
+            }
+            if (__shfl_sync(0xffffffffu, last, 0)) {
+                __threadfence_block();
+                const int rr = ng * 32 + lane, grow = k * SR + rr;
+                if (grow < nr) {
+                    const float2 *P = sm.npart[slot];
+                    float h = P[rr].x, l = P[rr].y;
 #pragma unroll
-                for (int w = 1; w < 8; w++) dfadd(h, l, rh[w][c], rl[w][c]);
-                atomic_add_pair(out1 + c, h, l);
+                    for (int q = 1; q < NCG; q++) dfadd(h, l, P[q * SR + rr].x, P[q * SR + rr].y);
+                    atomic_add_pair(vec_ptr(va, t.k_out0, t.out0, v) + grow, h, l);
+                }
+                if (lane == 0) sm.grp_cnt[slot][ng] = 0;
+            }
+            __syncwarp();
+        }
+        /* release the slot; the last warp out reloads it kStages stages ahead */
+        if (lane == 0) {
+            __threadfence_block();
+            if (atomicAdd(&sm.slot_cnt[slot], 1) == NW - 1) {
+                sm.slot_cnt[slot] = 0;
+                __threadfence_block();
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                if (g + kStages < S && !*dead) issue(g + kStages);
             }
         }
     }
-    if (lost >= 0) (void)mbar_wait(smem_addr(&tbar[lost % kStages]), (unsigned)((lost / kStages) & 1));
-    __syncthreads();
-    {
-        const bool pb = S - 1 >= nsA;
-        const Tile &pt = pb ? tB : tA;
-        if (pt.k_out0 != VK_NONE) merge_rows(S - 1, pt, pb ? S - 1 - nsA : S - 1);
-    }
+    if (lost >= 0) (void)mbar_wait(smem_addr(&sm.full[lost % kStages]), (unsigned)((lost / kStages) & 1));
 }
 
 /* x[v][i] = c_i * D[v][map_i >> 1], c_i = 2 for off-diagonal shell pairs
@@ -993,8 +1056,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
     *d->err_flag = 0;
     CUDA_TRY(cudaHostGetDevicePointer((void **)&d->err_flag_dev, d->err_flag, 0));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
-    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
-    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
     /* The tree sweeps are a chain of dependent launches (the critical path);
      * the near field is one large independent batch. Giving the chain's
      * stream the higher priority lets near-field tiles fill only the SMs the
@@ -1084,9 +1147,9 @@ static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int
             const int n = std::min(kMaxGridY, r.count - f);
             dim3 g2(nvec, (n + 1) / 2);
             if (r.pair)
-                k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kTileSmemLaunch, s>>>(t, n, va, maps, d->err_flag_dev);
+                k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev);
             else
-                k_tile_mx<FMT_F32><<<g2, kTileThreads, kTileSmemLaunch, s>>>(t, n, va, maps, d->err_flag_dev);
+                k_tile_mx<FMT_F32><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev);
         }
     }
 }
@@ -1236,8 +1299,13 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
 static int check_kernel_flag(DevRep *d)
 {
     if (d->err_flag == nullptr || *d->err_flag == 0) return 0;
+    const unsigned f = *d->err_flag;
     *d->err_flag = 0;
-    set_error("a tile kernel gave up waiting for a TMA load (bounded wait expired); results are invalid");
+    if (f & 2u)
+        set_error("a tile kernel found its shared memory off the 1024-byte alignment that swizzled TMA copies "
+                  "need and did nothing; results are invalid");
+    else
+        set_error("a tile kernel gave up waiting for a TMA load (bounded wait expired); results are invalid");
     return 11;
 }
 
