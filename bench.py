@@ -6,8 +6,9 @@ Default (GPU) arm: the representation is built on the host (set-up, not
 timed), uploaded once, then each step is one J build
 (uncontract -> H2 matvec -> contract) with the density already in HBM. The
 e2e figure times the reference-signature host API (density H2D, build,
-J D2H) per step. Precision: mixed (far-field FP32 / FP32 pairs, near field
-compensated FP32 pairs) when available, else FP64; the FP64 figure is
+J D2H) per step. Precision: mixed (bases and leaf self blocks stored as FP32
+pairs, other blocks as FP32, anchored FP32 accumulation, FP64 output sums)
+when available, else FP64; the FP64 figure is
 always reported beside it, together with the relative error of each against
 the FP64 CPU oracle.
 
