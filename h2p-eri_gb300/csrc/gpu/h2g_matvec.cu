@@ -108,11 +108,16 @@ __device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity)
         if (clock64() - t0 > kWaitCycles) return false;
     return true;
 }
-/* 2-D tensor copy of one box into shared memory, completing on bar. */
+/* 2-D tensor copy of one box into shared memory, completing on bar. The
+ * stored matrices stream through L2 once per matvec, so the copies are marked
+ * evict-first: they then do not push out the small vectors that the FP64
+ * output atomics work on (measured 0.438 -> 0.418 ms per C30H62 J build). */
 __device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map, int x, int y, unsigned bar)
 {
-    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-                 ::"r"(dst), "l"(map), "r"(x), "r"(y), "r"(bar)
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, %3}], [%4], %5;"
+                 ::"r"(dst), "l"(map), "r"(x), "r"(y), "r"(bar), "l"(pol)
                  : "memory");
 }
 
