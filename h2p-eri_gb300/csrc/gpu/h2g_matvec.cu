@@ -799,7 +799,12 @@ double stored_elems(const BlockLoc &b)
  *   1. t = V in0                    (N on V)
  *   2. s = U^T in1, out0 += U t     (one pass over Ut: N and T)
  *   3. out1 += V^T s                (T on V)
- * so U is read once and V twice (once when only the N side is wanted). */
+ * so U is read once and V twice (each once when only one side is wanted).
+ * When U is the smaller factor (nrow < ncol) of a two-sided block, the roles
+ * swap and U is the one read twice:
+ *   1. s = U^T in1                  (N on Ut)
+ *   2. t = V in0, out1 += V^T s     (one pass over V: N and T)
+ *   3. out0 += U t                  (T on Ut) */
 void plan_block(Planner *st, const BlockLoc &b, uint8_t kin0, int in0, uint8_t kout0, int out0, uint8_t kin1,
                 int in1, uint8_t kout1, int out1)
 {
@@ -811,6 +816,12 @@ void plan_block(Planner *st, const BlockLoc &b, uint8_t kin0, int in0, uint8_t k
     const int r = b.rank;
     if (r == 0) return;
     const bool wantN = kout0 != VK_NONE, wantT = kout1 != VK_NONE;
+    if (wantN && wantT && b.nrow < b.ncol) {
+        st[0].add(b.ut, r, b.nrow, kin1, in1, VK_T, b.s_off, VK_NONE, 0, VK_NONE, 0);
+        st[1].add(b.v, r, b.ncol, kin0, in0, VK_T, b.t_off, VK_T, b.s_off, kout1, out1);
+        st[2].add(b.ut, r, b.nrow, VK_NONE, 0, VK_NONE, 0, VK_T, b.t_off, kout0, out0);
+        return;
+    }
     if (wantN) st[0].add(b.v, r, b.ncol, kin0, in0, VK_T, b.t_off, VK_NONE, 0, VK_NONE, 0);
     st[1].add(b.ut, r, b.nrow, wantT ? kin1 : VK_NONE, in1, wantT ? VK_T : VK_NONE, b.s_off,
               wantN ? VK_T : VK_NONE, b.t_off, wantN ? kout0 : VK_NONE, out0);
