@@ -14,7 +14,8 @@ void set_error(const std::string &msg);
 int get_rep(H2ERI_p h, DevRep **out);
 /* y = A x on device vectors, enqueued on s */
 int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t s, bool timed);
-int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStream_t s, bool timed);
+int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStream_t s, bool timed,
+                    bool den_in_host = false);   /* den_in_host: page-locked host memory, read in place */
 /* exchange state attached to a representation */
 void free_exchange_state(DevRep *d);
 /* precision switch (mixed far-field arenas) */

@@ -17,6 +17,7 @@
  * a second stream concurrently with the tree sweeps.
  */
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -657,6 +658,23 @@ __global__ void k_uncontract(const int *__restrict__ map, int n, const double *_
         int m = map[i];
         double d = den[v * den_stride + (m >> 1)];
         x[v * x_stride + i] = (m & 1) ? 2.0 * d : d;
+    }
+}
+
+/* The same as k_uncontract driven by the inverse map (con: D index ->
+ * (x index << 1) | diagonal flag, or -1), so the density is read in order:
+ * used when it is read in place from host memory, where scattered reads
+ * would each cross the host link. Every x entry has exactly one D index. */
+__global__ void k_uncontract_scatter(const int *__restrict__ con, long long n2, const double *__restrict__ den,
+                                     long long den_stride, double *__restrict__ x, long long x_stride)
+{
+    const int v = blockIdx.y;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x) {
+        const int m = con[i];
+        if (m >= 0) {
+            const double dv = den[v * den_stride + i];
+            x[v * x_stride + (m >> 1)] = (m & 1) ? dv : 2.0 * dv;
+        }
     }
 }
 
@@ -1355,13 +1373,19 @@ static int ensure_den(DevRep *d, int n_den)
     return 0;
 }
 
-int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStream_t s, bool timed)
+int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStream_t s, bool timed,
+                    bool den_in_host)
 {
     int rc = ensure_work(d, n_den);
     if (rc) return rc;
     const long long n2 = (long long)d->num_bf * d->num_bf;
-    dim3 g1((d->krnl + 255) / 256 < 4096 ? (d->krnl + 255) / 256 : 4096, n_den);
-    k_uncontract<<<g1, 256, 0, s>>>(d->unc_map, d->krnl, den, n2, d->xbuf, d->krnl);
+    if (den_in_host) {
+        dim3 g0((unsigned)std::min<long long>((n2 + 255) / 256, 8192), n_den);
+        k_uncontract_scatter<<<g0, 256, 0, s>>>(d->con_map, n2, den, n2, d->xbuf, d->krnl);
+    } else {
+        dim3 g1((d->krnl + 255) / 256 < 4096 ? (d->krnl + 255) / 256 : 4096, n_den);
+        k_uncontract<<<g1, 256, 0, s>>>(d->unc_map, d->krnl, den, n2, d->xbuf, d->krnl);
+    }
     rc = enqueue_matvec(d, n_den, d->xbuf, d->ybuf, s, timed);
     if (rc) return rc;
     long long nb = (n2 + 255) / 256;
@@ -1498,19 +1522,49 @@ extern "C" int H2ERI_build_Coulomb_batch(int n, H2ERI_p *h2eris, const int *n_de
     return 0;
 }
 
+/* Device address of a page-locked host buffer [p, p + bytes), or nullptr when
+ * any part of it is pageable. Both ends must resolve to the same contiguous
+ * device mapping, so kernels never reach host memory that is not mapped. */
+static void *pinned_device_view(const void *p, size_t bytes)
+{
+    if (p == nullptr || bytes == 0) return nullptr;
+    cudaPointerAttributes a0, a1;
+    const char *last = static_cast<const char *>(p) + bytes - 1;
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || a0.devicePointer == nullptr ||
+        a1.devicePointer == nullptr)
+        return nullptr;
+    if (static_cast<char *>(a1.devicePointer) - static_cast<char *>(a0.devicePointer) != (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a0.devicePointer;
+}
+
 extern "C" int H2ERI_build_Coulomb_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *J_mats)
 {
     DevRep *d;
     int rc = get_rep(h2eri, &d);
     if (rc) return rc;
     if (n_den < 1) { set_error("n_den < 1"); return 3; }
-    rc = ensure_den(d, n_den);
-    if (rc) return rc;
     size_t bytes = (size_t)d->num_bf * d->num_bf * n_den * sizeof(double);
-    CUDA_TRY(cudaMemcpyAsync(d->dbuf, den_mats, bytes, cudaMemcpyHostToDevice, d->s_main));
-    rc = enqueue_coulomb(d, n_den, d->dbuf, d->jbuf, d->s_main, true);
+    /* page-locked caller buffers are read and written in place over the
+     * host link by the uncontract / contract kernels; pageable ones go
+     * through device staging copies */
+    const double *dsrc = static_cast<const double *>(pinned_device_view(den_mats, bytes));
+    double *jdst = static_cast<double *>(pinned_device_view(J_mats, bytes));
+    if (dsrc == nullptr || jdst == nullptr) {
+        rc = ensure_den(d, n_den);
+        if (rc) return rc;
+    }
+    if (dsrc == nullptr) {
+        CUDA_TRY(cudaMemcpyAsync(d->dbuf, den_mats, bytes, cudaMemcpyHostToDevice, d->s_main));
+        dsrc = d->dbuf;
+    }
+    rc = enqueue_coulomb(d, n_den, dsrc, jdst ? jdst : d->jbuf, d->s_main, true, dsrc != d->dbuf);
     if (rc) return rc;
-    CUDA_TRY(cudaMemcpyAsync(J_mats, d->jbuf, bytes, cudaMemcpyDeviceToHost, d->s_main));
+    if (jdst == nullptr) CUDA_TRY(cudaMemcpyAsync(J_mats, d->jbuf, bytes, cudaMemcpyDeviceToHost, d->s_main));
     CUDA_TRY(cudaStreamSynchronize(d->s_main));
     rc = check_kernel_flag(d);
     if (rc) return rc;
