@@ -58,7 +58,7 @@ WORKLOAD = dict(WORKLOADS["c30"])
 METRIC = "J builds/s C30H62 (mixed vs FP64) at relerr<=1e-8"
 # DRAM bytes (read + write) of all tile-kernel launches of one mixed C30H62 J
 # build, from one ncu capture (profiles/k_tile_C30H62_mixed_launches_traffic.md)
-TRAFFIC_J_MIXED_C30 = 1749.9e6
+TRAFFIC_J_MIXED_C30 = 1707.5e6
 METRIC_K = "K builds/s (H2ERI_build_exchange path)"
 CACHE_DIR = os.path.join(tempfile.gettempdir(), "h2eri_gb300_cache")
 
