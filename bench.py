@@ -5,8 +5,8 @@ functions), QR tolerance 1e-8, one seeded density (n_occ = 121).
 Default (GPU) arm: the representation is built on the host (set-up, not
 timed), uploaded once, then each step is one J build
 (uncontract -> H2 matvec -> contract) with the density already in HBM. The
-e2e figure times the reference-signature host API (density H2D, build,
-J D2H) per step. Precision: mixed (bases and leaf self blocks stored as FP32
+e2e figure times the reference-signature host API (density from host memory,
+build, J to host memory) per step. Precision: mixed (bases and leaf self blocks stored as FP32
 pairs, other blocks as FP32, anchored FP32 accumulation, FP64 output sums)
 when available, else FP64; the FP64 figure is
 always reported beside it, together with the relative error of each against
