@@ -100,13 +100,13 @@ __device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity)
                  : "memory");
     return ok != 0;
 }
-/* Wait for phase `parity` of an mbarrier, giving up after kWaitCycles. */
-__device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity)
+/* Wait for phase `parity` of an mbarrier, giving up after `limit` cycles. */
+__device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity, long long limit = kWaitCycles)
 {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 /* 2-D tensor copy of one box into shared memory, completing on bar. The
@@ -646,6 +646,23 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
         }
     }
     if (lost >= 0) (void)mbar_wait(smem_addr(&sm.full[lost % kStages]), (unsigned)((lost / kStages) & 1));
+}
+
+/* Self-test of the bounded wait: one CTA waits on an mbarrier (arrival count
+ * 1) that nothing arrives at; the wait gives up after `limit` cycles and the
+ * error word is set, as in the tile kernels. No copy is in flight, so the CTA
+ * exits cleanly. */
+__global__ void k_wait_probe(unsigned *err, long long limit)
+{
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (!mbar_wait(smem_addr(&bar), 0u, limit) && threadIdx.x == 0) atomicOr(err, 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(&bar)) : "memory");
 }
 
 /* x[v][i] = c_i * D[v][map_i >> 1], c_i = 2 for off-diagonal shell pairs
@@ -1411,6 +1428,28 @@ using namespace h2g;
 }
 
 extern "C" const char *H2ERI_gpu_last_error(void) { return t_last_error.c_str(); }
+
+extern "C" int H2ERI_gpu_selftest_wait_timeout(long long cycles)
+{
+    if (cycles < 0) { set_error("cycles < 0"); return -1; }
+    unsigned *flag = nullptr, *flag_dev = nullptr;
+    if (cudaHostAlloc((void **)&flag, sizeof(unsigned), cudaHostAllocMapped) != cudaSuccess) {
+        set_error(std::string("cudaHostAlloc: ") + cudaGetErrorString(cudaGetLastError()));
+        return -1;
+    }
+    *flag = 0;
+    int rc = -1;
+    if (cudaHostGetDevicePointer((void **)&flag_dev, flag, 0) == cudaSuccess) {
+        k_wait_probe<<<1, 32>>>(flag_dev, cycles);
+        const cudaError_t e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) rc = *flag ? 1 : 0;
+        else set_error(std::string("bounded-wait probe: ") + cudaGetErrorString(e));
+    } else {
+        set_error("cudaHostGetDevicePointer failed");
+    }
+    cudaFreeHost(flag);
+    return rc;
+}
 
 extern "C" int H2ERI_gpu_upload(H2ERI_p h2eri)
 {

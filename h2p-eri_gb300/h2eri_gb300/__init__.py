@@ -84,6 +84,7 @@ SIGNATURES = {
     "H2ERI_gpu_release": (None, [_vp]),
     "H2ERI_gpu_set_precision": (ctypes.c_int, [_vp, ctypes.c_int]),
     "H2ERI_gpu_last_error": (ctypes.c_char_p, []),
+    "H2ERI_gpu_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_longlong]),
     "H2ERI_matvec_multi": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
     "H2ERI_matvec_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     "H2ERI_build_Coulomb_multi": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),

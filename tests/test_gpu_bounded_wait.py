@@ -1,0 +1,31 @@
+"""Failure detection on the GPU without a fault: every wait of the tile
+kernels on an mbarrier is bounded and reports its expiry through an error
+word in mapped host memory. The self-test kernel waits on a barrier that
+nothing arrives at, with a short limit, and must give up, report it and leave
+the device usable for the next hot-path call."""
+import numpy as np
+import pytest
+
+import h2eri_gb300 as hg
+from conftest import relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def test_expired_wait_is_reported(library):
+    for cycles in (0, 100_000, 2_000_000):   # up to ~1 ms of SM clock
+        assert library.H2ERI_gpu_selftest_wait_timeout(cycles) == 1
+
+
+def test_negative_limit_is_rejected(library):
+    assert library.H2ERI_gpu_selftest_wait_timeout(-1) == -1
+    assert b"cycles" in library.H2ERI_gpu_last_error()
+
+
+def test_device_usable_after_expired_waits(library, alk26, oracle_lib):
+    assert library.H2ERI_gpu_selftest_wait_timeout(500_000) == 1
+    D = hg.molecules.seeded_density(alk26.num_bf, 20, 4321)
+    J = alk26.build_coulomb(D)
+    Jo = np.zeros_like(D)
+    oracle_lib.oracle_build_Coulomb(alk26.handle, D.ctypes.data, Jo.ctypes.data)
+    assert relerr(J, Jo) < 1e-12
