@@ -43,6 +43,11 @@ WORKLOADS = {
             "molecule": "C30H62", "n_carbon": 30, "qr_tol": 1e-8, "n_occ": 121, "seed": 2000,
             "inputs_vs_L2": "H2 representation ~1.8 GB read per step > 129 MB L2 (no flush needed)",
             "k_cpu_stride": 16},
+    # the larger molecule of the mixed-precision configuration
+    "c100": {"workload": "J build C100H202 cc-pVDZ (2510 bf, cartesian), QR tol 1e-8, 1 density n_occ=401",
+             "molecule": "C100H202", "n_carbon": 100, "qr_tol": 1e-8, "n_occ": 401, "seed": 3000,
+             "inputs_vs_L2": "H2 representation ~6.7 GB read per step > 129 MB L2 (no flush needed)",
+             "k_cpu_stride": 64},
     # small case for profiler captures (the reference's CPU-runnable size)
     "c10": {"workload": "J build C10H22 cc-pVDZ (260 bf, cartesian), QR tol 1e-6, 1 density n_occ=41",
             "molecule": "C10H22", "n_carbon": 10, "qr_tol": 1e-6, "n_occ": 41, "seed": 1000,
