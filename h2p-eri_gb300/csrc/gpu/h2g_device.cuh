@@ -61,7 +61,6 @@ struct PackItem {
     int ld;               /* leading dimension of the stored matrix */
 };
 
-constexpr int kTileRows = 64;      /* rows per sub-tile (8 warps x 8 rows)    */
 constexpr int kChunkRows = 512;    /* rows per tile (CTA), a multiple of 64   */
 constexpr int kTileCols = 128;
 constexpr int kTileThreads = 256;

@@ -38,14 +38,6 @@ __device__ __forceinline__ float2 pk_sub(float2 a, float2 b)
         : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
     return d;
 }
-__device__ __forceinline__ float2 pk_mul(float2 a, float2 b)
-{
-    float2 d;
-    asm("{.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return d;
-}
 __device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c)
 {
     float2 d;

@@ -215,21 +215,19 @@ __device__ __forceinline__ double reduceR_f64(double *s, int lane)
     }
 }
 
-/* One CTA per (vector, tile). A tile is a chunk of up to kChunkRows rows and
- * kTileCols columns. The chunk streams through a kStages-deep ring of 32 KB
- * shared-memory stages filled with cp.async (16-byte copies, any leading
- * dimension, zero fill past the tile edge), so the next stages are in flight
- * while the current one is multiplied. A stage holds SR = 64 rows of single
- * floats or 32 rows of 8-byte elements; warp w multiplies rows
- * [w*SR/8, (w+1)*SR/8) and each lane owns 4 columns (lane_col).
- * N-side row sums are added per stage; T-side column sums stay in registers
- * over the whole chunk and are added once (few atomics per coefficient).
- * FP64 FMAs and FP64 reductions (FMT_F64 only; the FP32 formats of the
- * mixed mode run k_tile_mx). */
+/* FP64 tile kernel. One CTA per (vector, tile). A tile is a chunk of up to
+ * kChunkRows rows and kTileCols columns. The chunk streams through a
+ * kStages-deep ring of 32 KB shared-memory stages filled with cp.async
+ * (16-byte copies, any leading dimension, zero fill past the tile edge), so
+ * the next stages are in flight while the current one is multiplied. A stage
+ * holds SR = 32 rows of doubles; warp w multiplies rows [w*SR/8, (w+1)*SR/8)
+ * and each lane owns 4 columns (lane_col). N-side row sums are added per
+ * stage; T-side column sums stay in registers over the whole chunk and are
+ * added once (few atomics per coefficient). FP64 FMAs and FP64 reductions
+ * (FMT_F64 only; the FP32 formats of the mixed mode run k_tile_mx). */
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
-k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va,
-       const CUtensorMap *__restrict__ maps, unsigned *err)
+k_tile(const Tile *__restrict__ tiles, const void *__restrict__ arena_v, const __grid_constant__ VecArgs va)
 {
     constexpr int EB = FmtInfo<FMT>::ebytes;
     constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage   */
@@ -1192,7 +1190,7 @@ static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int
         const Tile *t = d->tiles + r.first + f;
         const CUtensorMap *maps = reinterpret_cast<const CUtensorMap *>(d->tmaps);
         if (d->precision == H2ERI_GPU_FP64)
-            k_tile<FMT_F64><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena, va, maps, d->err_flag_dev);
+            k_tile<FMT_F64><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena, va);
         else {
             /* two tiles per CTA: tiles y and y + half of this launch */
             const int n = std::min(kMaxGridY, r.count - f);
