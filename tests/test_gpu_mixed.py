@@ -1,7 +1,9 @@
-"""Mixed-precision far field / near field on the GPU: U bases as FP32 pairs,
-B and D blocks as FP32, compensated FP32 products, FP64 reductions. Checked
-against the FP64 oracle on the same representation; tolerance 1e-8 relative
-(the target accuracy of the mixed mode)."""
+"""Mixed precision on the GPU: U bases and leaf self-interaction D blocks as
+FP32 pairs, other B and D blocks as FP32, products accumulated in anchored
+FP32 chains, FP64 output sums. Checked against the FP64 oracle on the same
+representation through every entry point; tolerance 1e-8 relative (the
+target accuracy of the mixed mode)."""
+import ctypes
 import os
 
 import numpy as np
@@ -68,3 +70,82 @@ def test_mixed_small_molecules(small_mols, oracle_lib, name):
     finally:
         h.set_precision(hg.FP64)
     assert relerr(J, oracle_J(oracle_lib, h, D)) < TOL_MIXED
+
+
+def test_mixed_device_multi_density_and_linearity(alk26, oracle_lib, library):
+    """Several densities per launch on device arrays: each J within 1e-8 of
+    the oracle, and the build stays linear in the density to that level."""
+    torch = pytest.importorskip("torch")
+    n = alk26.num_bf
+    D1 = hg.molecules.seeded_density(n, 33, 3101)
+    D2 = hg.molecules.seeded_density(n, 33, 3102)
+    Ds = np.stack([D1, D2, 0.5 * D1 - 2.0 * D2])
+    dD = torch.tensor(Ds, device="cuda")
+    dJ = torch.zeros_like(dD)
+    alk26.set_precision(hg.MIXED)
+    try:
+        s = torch.cuda.current_stream()
+        rc = library.H2ERI_build_Coulomb_device(alk26.handle, 3, dD.data_ptr(), dJ.data_ptr(),
+                                                ctypes.c_void_p(s.cuda_stream))
+        assert rc == 0, library.H2ERI_gpu_last_error()
+        torch.cuda.synchronize()
+    finally:
+        alk26.set_precision(hg.FP64)
+    J = dJ.cpu().numpy()
+    for i in range(3):
+        assert relerr(J[i], oracle_J(oracle_lib, alk26, Ds[i])) < TOL_MIXED, i
+    assert relerr(J[2], 0.5 * J[0] - 2.0 * J[1]) < TOL_MIXED
+
+
+def test_mixed_noalloc_matches_device_entry_point(alk26, library):
+    """The allocation-free matvec runs the same mixed kernels."""
+    torch = pytest.importorskip("torch")
+    alk26.set_precision(hg.MIXED)
+    try:
+        s = torch.cuda.Stream()
+        sp = ctypes.c_void_p(s.cuda_stream)
+        x = torch.tensor(np.random.default_rng(77).standard_normal(alk26.krnl_mat_size), device="cuda")
+        y_ref = torch.empty_like(x)
+        y = torch.full_like(x, float("nan"))
+        torch.cuda.synchronize()
+        assert library.H2ERI_matvec_device(alk26.handle, 1, x.data_ptr(), y_ref.data_ptr(), sp) == 0
+        rc = library.H2ERI_matvec_device_noalloc(alk26.handle, x.data_ptr(), y.data_ptr(), sp)
+        assert rc == 0, library.H2ERI_gpu_last_error()
+        s.synchronize()
+    finally:
+        alk26.set_precision(hg.FP64)
+    # same kernels; only the order of the FP64 atomic additions differs
+    assert relerr(y.cpu().numpy(), y_ref.cpu().numpy()) < 1e-12
+
+
+def test_mixed_batch_and_page_locked_buffers(small_mols, alk32, oracle_lib, library):
+    """The batched call and the page-locked host path in mixed mode."""
+    torch = pytest.importorskip("torch")
+    hs = [small_mols["C4H10"], alk32]
+    dens = [np.stack([hg.molecules.seeded_density(h.num_bf, 4 + k, 700 + 10 * k + i) for i in range(2)])
+            for k, h in enumerate(hs)]
+    for h in hs:
+        h.set_precision(hg.MIXED)
+    try:
+        dDs = [torch.tensor(D, device="cuda") for D in dens]
+        dJs = [torch.zeros_like(t) for t in dDs]
+        harr = (ctypes.c_void_p * 2)(*[h.handle.value for h in hs])
+        narr = (ctypes.c_int * 2)(2, 2)
+        darr = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in dDs])
+        jarr = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in dJs])
+        s = torch.cuda.current_stream()
+        rc = library.H2ERI_build_Coulomb_batch(2, harr, narr, darr, jarr, ctypes.c_void_p(s.cuda_stream))
+        assert rc == 0, library.H2ERI_gpu_last_error()
+        torch.cuda.synchronize()
+        pD = torch.from_numpy(dens[1].copy()).pin_memory()
+        pJ = torch.zeros(pD.shape, dtype=torch.float64, pin_memory=True)
+        assert library.H2ERI_build_Coulomb_multi(alk32.handle, 2, pD.data_ptr(), pJ.data_ptr()) == 0
+    finally:
+        for h in hs:
+            h.set_precision(hg.FP64)
+    for h, D, dJ in zip(hs, dens, dJs):
+        J = dJ.cpu().numpy()
+        for i in range(2):
+            assert relerr(J[i], oracle_J(oracle_lib, h, D[i])) < TOL_MIXED
+    for i in range(2):
+        assert relerr(pJ[i].numpy(), oracle_J(oracle_lib, alk32, dens[1][i])) < TOL_MIXED
