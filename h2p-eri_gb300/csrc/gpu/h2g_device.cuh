@@ -112,8 +112,8 @@ struct DevRep {
     double *xbuf = nullptr, *ybuf = nullptr;   /* matvec staging, nvec_cap vectors */
     double *dbuf = nullptr, *jbuf = nullptr;   /* density / J staging, nden_cap matrices */
     int nden_cap = 0;
-    cudaStream_t s_main = nullptr, s_aux = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_zero = nullptr, ev_done = nullptr;
+    cudaStream_t s_main = nullptr, s_aux = nullptr, s_aux2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr, ev_zero = nullptr, ev_done = nullptr;
     cudaEvent_t ev_bfork = nullptr, ev_bjoin = nullptr;   /* batched builds: fork from / join to the caller */
     cudaEvent_t ev_t[8] = {nullptr};
     float last_ms[5] = {0, 0, 0, 0, 0};   /* fwd, mid, bwd, den, total */

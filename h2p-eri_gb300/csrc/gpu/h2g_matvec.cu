@@ -884,6 +884,8 @@ static void free_rep(DevRep *d)
     cudaFree(d->jbuf);
     if (d->s_main) cudaStreamDestroy(d->s_main);
     if (d->s_aux) cudaStreamDestroy(d->s_aux);
+    if (d->s_aux2) cudaStreamDestroy(d->s_aux2);
+    if (d->ev_join2) cudaEventDestroy(d->ev_join2);
     if (d->ev_fork) cudaEventDestroy(d->ev_fork);
     if (d->ev_join) cudaEventDestroy(d->ev_join);
     if (d->ev_zero) cudaEventDestroy(d->ev_zero);
@@ -1115,6 +1117,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
     CUDA_TRY(cudaStreamCreateWithPriority(&d->s_main, cudaStreamNonBlocking, prio_hi));
     CUDA_TRY(cudaStreamCreateWithPriority(&d->s_aux, cudaStreamNonBlocking, prio_lo));
+    CUDA_TRY(cudaStreamCreateWithPriority(&d->s_aux2, cudaStreamNonBlocking, prio_lo));
+    CUDA_TRY(cudaEventCreateWithFlags(&d->ev_join2, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_zero, cudaEventDisableTiming));
@@ -1324,8 +1328,15 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     CUDA_TRY(cudaMemsetAsync(y, 0, (size_t)d->krnl * nvec * sizeof(double), sm));
     CUDA_TRY(cudaEventRecord(d->ev_zero, sm));
     CUDA_TRY(cudaStreamWaitEvent(sa, d->ev_zero, 0));
+    /* the near field's float-pair blocks (leaf self-interaction) and its
+     * single-float blocks form two independent stage chains: each gets its
+     * own low-priority stream, so the few long CTAs of one do not leave the
+     * other waiting at a launch boundary */
+    CUDA_TRY(cudaStreamWaitEvent(d->s_aux2, d->ev_zero, 0));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], sa));
-    for (const Range &r : d->den) launch_range(d, r, va, nvec, sa);
+    for (const Range &r : d->den) launch_range(d, r, va, nvec, r.pair ? d->s_aux2 : sa);
+    CUDA_TRY(cudaEventRecord(d->ev_join2, d->s_aux2));
+    CUDA_TRY(cudaStreamWaitEvent(sa, d->ev_join2, 0));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[7], sa));
     CUDA_TRY(cudaEventRecord(d->ev_join, sa));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], sm));
