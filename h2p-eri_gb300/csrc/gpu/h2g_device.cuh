@@ -73,7 +73,9 @@ struct VecArgs {
 struct Range {
     int first = 0, count = 0;
     bool pair = false;     /* mixed mode: matrices of this range are float pairs */
+    int lane = 0;          /* near field: the stream (independent stage chain) it runs on */
 };
+constexpr int kNfLanes = 2;   /* near-field lanes: float-pair blocks, then groups of single-float blocks */
 
 /* Device copy of one H2 representation plus the launch plan. */
 struct DevRep {
@@ -112,8 +114,10 @@ struct DevRep {
     double *xbuf = nullptr, *ybuf = nullptr;   /* matvec staging, nvec_cap vectors */
     double *dbuf = nullptr, *jbuf = nullptr;   /* density / J staging, nden_cap matrices */
     int nden_cap = 0;
-    cudaStream_t s_main = nullptr, s_aux = nullptr, s_aux2 = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr, ev_zero = nullptr, ev_done = nullptr;
+    cudaStream_t s_main = nullptr, s_aux = nullptr;   /* s_aux: near-field lane 0 */
+    cudaStream_t s_nf[kNfLanes] = {nullptr};          /* near-field lanes 1.. (s_nf[0] unused) */
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_zero = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_nf[kNfLanes] = {nullptr};
     cudaEvent_t ev_bfork = nullptr, ev_bjoin = nullptr;   /* batched builds: fork from / join to the caller */
     cudaEvent_t ev_t[8] = {nullptr};
     float last_ms[5] = {0, 0, 0, 0, 0};   /* fwd, mid, bwd, den, total */

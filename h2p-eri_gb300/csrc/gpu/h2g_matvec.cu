@@ -884,8 +884,10 @@ static void free_rep(DevRep *d)
     cudaFree(d->jbuf);
     if (d->s_main) cudaStreamDestroy(d->s_main);
     if (d->s_aux) cudaStreamDestroy(d->s_aux);
-    if (d->s_aux2) cudaStreamDestroy(d->s_aux2);
-    if (d->ev_join2) cudaEventDestroy(d->ev_join2);
+    for (int i = 1; i < kNfLanes; i++) {
+        if (d->s_nf[i]) cudaStreamDestroy(d->s_nf[i]);
+        if (d->ev_nf[i]) cudaEventDestroy(d->ev_nf[i]);
+    }
     if (d->ev_fork) cudaEventDestroy(d->ev_fork);
     if (d->ev_join) cudaEventDestroy(d->ev_join);
     if (d->ev_zero) cudaEventDestroy(d->ev_zero);
@@ -944,7 +946,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
             need_down[node] = wrote_y1[node] || (pin && need_down[p] && rank[p] > 0);
         }
 
-    Planner midst[3], dend[3], deno[3];
+    Planner midst[3], dend[3], deno[kNfLanes][3];
+    double lane_load[kNfLanes] = {0.0};
     std::vector<Tile> all;
     double mat_bytes = 0.0, mat_bytes_mixed = 0.0, vec_bytes = 0.0, flops = 0.0;
     d->fwd.clear();
@@ -1052,7 +1055,12 @@ static int build_rep(H2ERI_p h, DevRep *d)
             int k = i - h->n_leaf_node;
             int n0 = h->r_inadm_pairs[2 * k], n1 = h->r_inadm_pairs[2 * k + 1];
             int o0 = h->mat_cluster[2 * n0], o1 = h->mat_cluster[2 * n1];
-            plan_block(deno, b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
+            /* single-float blocks: the least-loaded lane (stored elements) */
+            int ln = 1;
+            for (int q = 2; q < kNfLanes; q++)
+                if (lane_load[q] < lane_load[ln]) ln = q;
+            lane_load[ln] += el;
+            plan_block(deno[ln], b, VK_X, o1, VK_Y, o0, VK_X, o0, VK_Y, o1);
             vec_bytes += 8.0 * 2 * (b.nrow + b.ncol);
             flops += 4.0 * el;
         }
@@ -1060,11 +1068,14 @@ static int build_rep(H2ERI_p h, DevRep *d)
         mat_bytes_mixed += (diag ? 8.0 : 4.0) * el;
     }
     d->bytes_D = (pk.host.size() - d_start) * sizeof(double);
+    /* near-field lanes: lane 0 the float-pair blocks, lanes 1.. groups of
+     * single-float blocks; each lane's three stages form an independent
+     * chain on its own stream */
     d->den.clear();
-    for (int k = 0; k < 3; k++)
-        for (int pair = 1; pair >= 0; pair--) {
-            Planner &p = pair ? dend[k] : deno[k];
-            d->den.push_back(Range{(int)all.size(), (int)p.tiles.size(), pair == 1});
+    for (int ln = 0; ln < kNfLanes; ln++)
+        for (int k = 0; k < 3; k++) {
+            Planner &p = ln == 0 ? dend[k] : deno[ln][k];
+            d->den.push_back(Range{(int)all.size(), (int)p.tiles.size(), ln == 0, ln});
             all.insert(all.end(), p.tiles.begin(), p.tiles.end());
         }
 
@@ -1117,8 +1128,10 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
     CUDA_TRY(cudaStreamCreateWithPriority(&d->s_main, cudaStreamNonBlocking, prio_hi));
     CUDA_TRY(cudaStreamCreateWithPriority(&d->s_aux, cudaStreamNonBlocking, prio_lo));
-    CUDA_TRY(cudaStreamCreateWithPriority(&d->s_aux2, cudaStreamNonBlocking, prio_lo));
-    CUDA_TRY(cudaEventCreateWithFlags(&d->ev_join2, cudaEventDisableTiming));
+    for (int i = 1; i < kNfLanes; i++) {
+        CUDA_TRY(cudaStreamCreateWithPriority(&d->s_nf[i], cudaStreamNonBlocking, prio_lo));
+        CUDA_TRY(cudaEventCreateWithFlags(&d->ev_nf[i], cudaEventDisableTiming));
+    }
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_zero, cudaEventDisableTiming));
@@ -1299,6 +1312,25 @@ int set_precision_mode(DevRep *d, H2ERI_p h, int mode)
     return 0;
 }
 
+/* The near field on its lanes: each lane (the float-pair blocks; groups of
+ * single-float blocks) is an independent chain of three stages on its own
+ * low-priority stream, so the few long CTAs at the end of one stage do not
+ * leave the others waiting at a launch boundary. All lanes start after
+ * ev_zero and are joined into s_aux, which records ev_join. */
+static int launch_near_field(DevRep *d, const VecArgs &va, int nvec, bool timed = false)
+{
+    for (int ln = 1; ln < kNfLanes; ln++) CUDA_TRY(cudaStreamWaitEvent(d->s_nf[ln], d->ev_zero, 0));
+    CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_zero, 0));
+    for (const Range &r : d->den) launch_range(d, r, va, nvec, r.lane == 0 ? d->s_aux : d->s_nf[r.lane]);
+    for (int ln = 1; ln < kNfLanes; ln++) {
+        CUDA_TRY(cudaEventRecord(d->ev_nf[ln], d->s_nf[ln]));
+        CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_nf[ln], 0));
+    }
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[7], d->s_aux));
+    CUDA_TRY(cudaEventRecord(d->ev_join, d->s_aux));
+    return 0;
+}
+
 /* Enqueue y = A x for nvec vectors (device pointers) on stream s. If timed,
  * per-phase events are recorded (fwd, mid, bwd on the main chain, dense on
  * the auxiliary stream). */
@@ -1321,24 +1353,15 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     va.stride[VK_T] = d->lr_total;
     /* fork from the caller's stream onto the library's streams: the tree
      * chain on the high-priority stream, the near field on the other */
-    cudaStream_t sm = d->s_main, sa = d->s_aux;
+    cudaStream_t sm = d->s_main;
     CUDA_TRY(cudaEventRecord(d->ev_fork, s));
     CUDA_TRY(cudaStreamWaitEvent(sm, d->ev_fork, 0));
     CUDA_TRY(cudaMemsetAsync(d->work, 0, (2 * per_r + per_t) * sizeof(double), sm));
     CUDA_TRY(cudaMemsetAsync(y, 0, (size_t)d->krnl * nvec * sizeof(double), sm));
     CUDA_TRY(cudaEventRecord(d->ev_zero, sm));
-    CUDA_TRY(cudaStreamWaitEvent(sa, d->ev_zero, 0));
-    /* the near field's float-pair blocks (leaf self-interaction) and its
-     * single-float blocks form two independent stage chains: each gets its
-     * own low-priority stream, so the few long CTAs of one do not leave the
-     * other waiting at a launch boundary */
-    CUDA_TRY(cudaStreamWaitEvent(d->s_aux2, d->ev_zero, 0));
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], sa));
-    for (const Range &r : d->den) launch_range(d, r, va, nvec, r.pair ? d->s_aux2 : sa);
-    CUDA_TRY(cudaEventRecord(d->ev_join2, d->s_aux2));
-    CUDA_TRY(cudaStreamWaitEvent(sa, d->ev_join2, 0));
-    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[7], sa));
-    CUDA_TRY(cudaEventRecord(d->ev_join, sa));
+    if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], sm));
+    rc = launch_near_field(d, va, nvec, timed);
+    if (rc) return rc;
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], sm));
     for (const Range &r : d->fwd) launch_range(d, r, va, nvec, sm);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[1], sm));
@@ -1762,15 +1785,14 @@ extern "C" int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, dou
     va.base[VK_T] = work + 2 * per_r;
     va.stride[VK_T] = d->lr_total;
     cudaStream_t s = stream ? (cudaStream_t)stream : d->s_main;
-    cudaStream_t sm = d->s_main, sa = d->s_aux;
+    cudaStream_t sm = d->s_main;
     CUDA_TRY(cudaEventRecord(d->ev_fork, s));
     CUDA_TRY(cudaStreamWaitEvent(sm, d->ev_fork, 0));
     CUDA_TRY(cudaMemsetAsync(work, 0, need * sizeof(double), sm));      /* scratch keeps the last call's values */
     CUDA_TRY(cudaMemsetAsync(d_y, 0, (size_t)d->krnl * sizeof(double), sm));
     CUDA_TRY(cudaEventRecord(d->ev_zero, sm));
-    CUDA_TRY(cudaStreamWaitEvent(sa, d->ev_zero, 0));
-    for (const Range &r : d->den) launch_range(d, r, va, 1, sa);
-    CUDA_TRY(cudaEventRecord(d->ev_join, sa));
+    rc = launch_near_field(d, va, 1);
+    if (rc) return rc;
     for (const Range &r : d->fwd) launch_range(d, r, va, 1, sm);
     for (const Range &r : d->mid) launch_range(d, r, va, 1, sm);
     for (const Range &r : d->bwd) launch_range(d, r, va, 1, sm);
