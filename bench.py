@@ -157,6 +157,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x, dist, device):
+    """The largest value of x over the ranks (x itself with one process):
+    every rank times its own replicas, and the job is as slow as its slowest
+    rank."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ws, steps, ms_max):
+    """J builds per second of the whole job: each of the ws ranks ran `steps`
+    builds, and the slowest rank took ms_max milliseconds for its steps."""
+    return ws * steps / (ms_max / 1e3)
+
+
 def peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -552,16 +570,9 @@ def run_gpu(args):
     ms16 = e0.elapsed_time(e1) / steps16
     J16 = dJ16.cpu().numpy()
 
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    ms_best = max_over_ranks(results[best]["ms"])
-    ms_fp64 = max_over_ranks(results["fp64"]["ms"]) if "fp64" in results else float("nan")
-    e2e_s = max_over_ranks(e2e_s)
+    ms_best = max_over_ranks(results[best]["ms"], dist, "cuda")
+    ms_fp64 = max_over_ranks(results["fp64"]["ms"], dist, "cuda") if "fp64" in results else float("nan")
+    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     if rank != 0:
         barrier()
         return
@@ -582,7 +593,7 @@ def run_gpu(args):
         return float(np.linalg.norm(J - Jo) / np.linalg.norm(Jo))
 
     step_s = ms_best / 1e3 / args.steps
-    value = ws * args.steps / (ms_best / 1e3)
+    value = replica_value(ws, args.steps, ms_best)
     alg_bytes = rep["alg_matrix_bytes"] + rep["alg_vector_bytes"] + 2 * 8 * nbf * nbf
     if best == "mixed":
         rep_m = h.report()
