@@ -1099,6 +1099,7 @@ using namespace h2g;
 
 extern "C" int H2ERI_build_exchange_device(H2ERI_p h2eri, const double *d_den, double *d_K, void *stream)
 {
+    H2gRange nvtx_range("H2ERI_build_exchange_device");
     DevRep *d;
     KState *ks;
     int rc = get_kstate(h2eri, &d, &ks);
@@ -1110,6 +1111,7 @@ extern "C" int H2ERI_build_exchange_device(H2ERI_p h2eri, const double *d_den, d
 
 extern "C" int H2ERI_build_exchange_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *K_mats)
 {
+    H2gRange nvtx_range("H2ERI_build_exchange_multi");
     DevRep *d;
     KState *ks;
     int rc = get_kstate(h2eri, &d, &ks);

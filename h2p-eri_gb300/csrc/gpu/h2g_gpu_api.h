@@ -6,6 +6,16 @@
 #include <cuda_runtime.h>
 #include "h2eri_types.h"
 #include "h2g_device.cuh"
+#include <nvtx3/nvToolsExt.h>
+
+/* A named range for profilers (NVTX; header-only, inert unless a tool such
+ * as Nsight Systems is attached) around each hot-path entry point. */
+struct H2gRange {
+    explicit H2gRange(const char *name) { nvtxRangePushA(name); }
+    ~H2gRange() { nvtxRangePop(); }
+    H2gRange(const H2gRange &) = delete;
+    H2gRange &operator=(const H2gRange &) = delete;
+};
 
 namespace h2g {
 

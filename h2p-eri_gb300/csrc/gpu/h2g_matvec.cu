@@ -1177,6 +1177,18 @@ int get_rep(H2ERI_p h, DevRep **out)
     cudaGetDevice(&d->device);
     int rc = build_rep(h, d);
     if (rc != 0) { free_rep(d); return rc; }
+    /* H2G_PRECISION=mixed starts the structure in the mixed mode, for callers
+     * of the reference's entry points that do not call the extensions */
+    if (const char *pe = std::getenv("H2G_PRECISION")) {
+        if (std::strcmp(pe, "mixed") == 0) {
+            rc = set_precision_mode(d, h, H2ERI_GPU_MIXED);
+            if (rc != 0) { free_rep(d); return rc; }
+        } else if (pe[0] != '\0' && std::strcmp(pe, "fp64") != 0) {
+            set_error(std::string("H2G_PRECISION must be fp64 or mixed, not ") + pe);
+            free_rep(d);
+            return 3;
+        }
+    }
     g_reps[h] = d;
     *out = d;
     return 0;
@@ -1512,6 +1524,7 @@ extern "C" int H2ERI_gpu_set_precision(H2ERI_p h2eri, int mode)
 
 extern "C" int H2ERI_matvec_device(H2ERI_p h2eri, int nvec, const double *d_x, double *d_y, void *stream)
 {
+    H2gRange nvtx_range("H2ERI_matvec_device");
     DevRep *d;
     int rc = get_rep(h2eri, &d);
     if (rc) return rc;
@@ -1522,6 +1535,7 @@ extern "C" int H2ERI_matvec_device(H2ERI_p h2eri, int nvec, const double *d_x, d
 
 extern "C" int H2ERI_matvec_multi(H2ERI_p h2eri, int nvec, const double *x, double *y)
 {
+    H2gRange nvtx_range("H2ERI_matvec_multi");
     DevRep *d;
     int rc = get_rep(h2eri, &d);
     if (rc) return rc;
@@ -1548,6 +1562,7 @@ extern "C" void H2ERI_matvec(H2ERI_p h2eri, const double *x, double *y)
 
 extern "C" int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double *d_den, double *d_J, void *stream)
 {
+    H2gRange nvtx_range("H2ERI_build_Coulomb_device");
     DevRep *d;
     int rc = get_rep(h2eri, &d);
     if (rc) return rc;
@@ -1563,6 +1578,7 @@ extern "C" int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double
 extern "C" int H2ERI_build_Coulomb_batch(int n, H2ERI_p *h2eris, const int *n_den, const double *const *d_dens,
                                          double *const *d_Js, void *stream)
 {
+    H2gRange nvtx_range("H2ERI_build_Coulomb_batch");
     if (n < 0 || (n > 0 && (h2eris == nullptr || n_den == nullptr || d_dens == nullptr || d_Js == nullptr))) {
         set_error("H2ERI_build_Coulomb_batch: bad arguments");
         return 3;
@@ -1615,6 +1631,7 @@ static void *pinned_device_view(const void *p, size_t bytes)
 
 extern "C" int H2ERI_build_Coulomb_multi(H2ERI_p h2eri, int n_den, const double *den_mats, double *J_mats)
 {
+    H2gRange nvtx_range("H2ERI_build_Coulomb_multi");
     DevRep *d;
     int rc = get_rep(h2eri, &d);
     if (rc) return rc;
@@ -1739,6 +1756,7 @@ static int noalloc_scratch(int dev, double **out)
  * that first call before any stream capture. */
 extern "C" int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, void *stream)
 {
+    H2gRange nvtx_range("H2ERI_matvec_device_noalloc");
     if (h2eri == nullptr) { set_error("null H2ERI handle"); return 1; }
     DevRep *d = nullptr;
     {

@@ -149,3 +149,30 @@ def test_mixed_batch_and_page_locked_buffers(small_mols, alk32, oracle_lib, libr
             assert relerr(J[i], oracle_J(oracle_lib, h, D[i])) < TOL_MIXED
     for i in range(2):
         assert relerr(pJ[i].numpy(), oracle_J(oracle_lib, alk32, dens[1][i])) < TOL_MIXED
+
+
+def test_precision_from_environment(tmp_path, oracle_lib, library, monkeypatch):
+    """H2G_PRECISION=mixed starts a structure in the mixed mode, so callers of
+    the reference entry points alone get it; an unknown value is an error."""
+    p = str(tmp_path / "c4h10.mol")
+    hg.molecules.write_alkane(p, 4)
+    monkeypatch.setenv("H2G_PRECISION", "mixed")
+    h = hg.H2ERI.from_mol(p, qr_tol=1e-8)
+    try:
+        D = hg.molecules.seeded_density(h.num_bf, 4, 808)
+        J = np.zeros_like(D)
+        library.H2ERI_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)   # reference signature
+        assert h.report()["precision"] == hg.MIXED
+        e = relerr(J, oracle_J(oracle_lib, h, D))
+        assert 1e-14 < e < TOL_MIXED, e
+    finally:
+        h.destroy()
+    monkeypatch.setenv("H2G_PRECISION", "fp32")
+    h = hg.H2ERI.from_mol(p, qr_tol=1e-8)
+    try:
+        D = hg.molecules.seeded_density(h.num_bf, 4, 808)
+        J = np.zeros_like(D)
+        assert library.H2ERI_build_Coulomb_multi(h.handle, 1, D.ctypes.data, J.ctypes.data) != 0
+        assert b"H2G_PRECISION" in library.H2ERI_gpu_last_error()
+    finally:
+        h.destroy()
