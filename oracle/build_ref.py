@@ -19,6 +19,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 
 
+def available():
+    """True where the reference sources exist (the machine the repository is
+    developed on); elsewhere the reference build is skipped."""
+    return os.path.isdir(REF_SRC)
+
+
 def openblas_lib():
     import scipy
     libdir = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
