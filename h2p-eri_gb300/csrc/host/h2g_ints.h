@@ -3,8 +3,9 @@
  *
  * The reference delegates electron-repulsion integrals (ERI) and point-charge
  * potential integrals to the external SIMINT library
- * (H2P-ERI src/CMS.c:163-229, 268-482). SIMINT is not part of this build, so
- * this file provides an independent implementation of the same integrals:
+ * (H2P-ERI src/CMS.c:163-229, 268-482). SIMINT is an external dependency
+ * that this library does not take, so this file provides an independent
+ * implementation of the same integrals:
  *
  *   - Cartesian Gaussian shells, all Cartesian components of a shell share one
  *     contracted coefficient set (SIMINT convention, see h2g_normalize_shell);
