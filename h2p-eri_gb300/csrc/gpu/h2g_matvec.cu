@@ -901,6 +901,41 @@ static void free_rep(DevRep *d)
     delete d;
 }
 
+/* Host-side bounds check of the launch plan before anything reaches the
+ * device: every vector range a tile reads or adds to lies inside its vector,
+ * every tile lies inside the FP64 arena, and the tile shapes fit the
+ * kernels. A structure with damaged tree arrays (a corrupted file, a
+ * caller's mistake) is rejected here instead of faulting a kernel. */
+static bool plan_in_bounds(const std::vector<Tile> &tiles, size_t arena_elems, long long krnl, long long rank_total,
+                           long long lr_total, std::string &why)
+{
+    auto len = [&](uint8_t k) -> long long {
+        switch (k) {
+        case VK_X: case VK_Y: return krnl;
+        case VK_Y0: case VK_Y1: return rank_total;
+        case VK_T: return lr_total;
+        default: return -1;
+        }
+    };
+    auto range_ok = [&](uint8_t k, long long off, long long n) {
+        const long long L = len(k);
+        return L >= 0 && off >= 0 && off + n <= L;
+    };
+    for (size_t i = 0; i < tiles.size(); i++) {
+        const Tile &t = tiles[i];
+        const bool n_side = t.k_out0 != VK_NONE, t_side = t.k_out1 != VK_NONE;
+        bool ok = (n_side || t_side) && t.nr >= 1 && t.nr <= kChunkRows && t.nc >= 1 && t.nc <= kTileCols &&
+                  t.ld >= t.nc && t.a + (uint64_t)(t.nr - 1) * (uint64_t)t.ld + (uint64_t)((t.nc + 1) & ~1) <= arena_elems;
+        if (ok && n_side) ok = range_ok(t.k_in0, t.in0, t.nc) && range_ok(t.k_out0, t.out0, t.nr);
+        if (ok && t_side) ok = range_ok(t.k_in1, t.in1, t.nr) && range_ok(t.k_out1, t.out1, t.nc);
+        if (!ok) {
+            why = "launch plan out of bounds at tile " + std::to_string(i) + " (damaged tree arrays or blocks)";
+            return false;
+        }
+    }
+    return true;
+}
+
 static int build_rep(H2ERI_p h, DevRep *d)
 {
     if (h->U == nullptr || h->c_D_blks == nullptr || (h->n_B > 0 && h->c_B_blks == nullptr)) {
@@ -1088,6 +1123,13 @@ static int build_rep(H2ERI_p h, DevRep *d)
     d->alg_flops = flops;
     d->n_tiles = (int)all.size();
     d->arena_elems = pk.host.size();
+    {
+        std::string why;
+        if (!plan_in_bounds(all, d->arena_elems, krnl, d->rank_total, d->lr_total, why)) {
+            set_error(why);
+            return 3;
+        }
+    }
     CUDA_TRY(cudaMalloc(&d->arena, std::max<size_t>(d->arena_elems, 4) * sizeof(double)));
     CUDA_TRY(cudaMemcpy(d->arena, pk.host.data(), d->arena_elems * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMalloc(&d->tiles, std::max<size_t>(all.size(), 1) * sizeof(Tile)));
@@ -1105,6 +1147,10 @@ static int build_rep(H2ERI_p h, DevRep *d)
             for (int k = 0; k < nrow; k++) {
                 int xi = base + j * nrow + k;
                 int di = (scol + j) * nbf + srow + k;
+                if (xi < 0 || xi >= krnl || di < 0 || (long long)di >= (long long)nbf * nbf) {
+                    set_error("J maps out of bounds (damaged shell-pair arrays)");
+                    return 3;
+                }
                 unc[xi] = (di << 1) | (M != N ? 1 : 0);
                 con[di] = (xi << 1) | (M == N ? 1 : 0);
             }

@@ -29,3 +29,23 @@ def test_device_usable_after_expired_waits(library, alk26, oracle_lib):
     Jo = np.zeros_like(D)
     oracle_lib.oracle_build_Coulomb(alk26.handle, D.ctypes.data, Jo.ctypes.data)
     assert relerr(J, Jo) < 1e-12
+
+
+def test_damaged_structure_rejected_before_any_launch(library, tmp_path):
+    """Host-side validation: a structure whose tree arrays point outside the
+    vectors (here one leaf's row range moved past the end) is rejected when
+    it is uploaded, before any device memory is touched or kernel launched."""
+    p = str(tmp_path / "c4h10.mol")
+    hg.molecules.write_alkane(p, 4)
+    h = hg.H2ERI.from_mol(p, qr_tol=1e-6)
+    try:
+        leaf = h.s.height_nodes[0]
+        r0, r1 = h.s.mat_cluster[2 * leaf], h.s.mat_cluster[2 * leaf + 1]
+        shift = h.krnl_mat_size + 1000
+        h.s.mat_cluster[2 * leaf] = r0 + shift
+        h.s.mat_cluster[2 * leaf + 1] = r1 + shift
+        assert library.H2ERI_gpu_upload(h.handle) != 0
+        assert b"out of bounds" in library.H2ERI_gpu_last_error()
+        h.s.mat_cluster[2 * leaf], h.s.mat_cluster[2 * leaf + 1] = r0, r1
+    finally:
+        h.destroy()
