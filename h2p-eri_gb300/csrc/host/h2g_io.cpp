@@ -5,10 +5,12 @@
  * without breaking older readers.
  */
 #include <cstdint>
+#include <exception>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <string>
+#include <utility>
 #include <vector>
 #include <omp.h>
 
@@ -194,27 +196,101 @@ extern "C" int H2ERI_save_representation(H2ERI_p h, const char *path)
     return ok ? 0 : 3;
 }
 
+namespace {
+
+/* Every blob the loader indexes must exist with its element size and at
+ * least the count that the scalars imply, and every block header must match
+ * the block data; a damaged file is rejected before anything is built from
+ * it. */
+bool blobs_consistent(const std::map<std::string, std::vector<char>> &blobs,
+                      const std::map<std::string, uint32_t> &esz)
+{
+    auto has = [&](const std::string &n, uint32_t es, long long cnt) {
+        auto it = blobs.find(n);
+        auto ie = esz.find(n);
+        return cnt >= 0 && it != blobs.end() && ie != esz.end() && ie->second == es &&
+               it->second.size() >= (size_t)es * (size_t)cnt;
+    };
+    auto ival = [&](const std::string &n, size_t i) { return ((const int *)blobs.at(n).data())[i]; };
+    if (!has("scalars", 4, 21) || !has("dscalars", 8, 4)) return false;
+    const int *sc = (const int *)blobs.at("scalars").data();
+    const long long ns = sc[1], nsp = sc[5], nn = sc[9], root = sc[10], nleaf = sc[11], maxc = sc[12],
+                    maxl = sc[13], ninadm = sc[15], nadm = sc[16], nU = sc[17], nB = sc[18], nD = sc[19];
+    for (int i = 0; i < 21; i++)
+        if (sc[i] < 0 && i != 14) return false;   /* min_adm_level may be -1 */
+    if (ns < 1 || nsp < 1 || nn < 1 || root >= nn || nleaf < 1 || maxc < 1 || nU > nn) return false;
+    const long long nl = maxl + 1;
+    struct Need { const char *name; long long cnt; };
+    const Need fixed[] = {{"shell_bf_sidx", ns + 1}, {"sp_nbfp", nsp}, {"sp_bfp_sidx", nsp + 1},
+                          {"sp_shell_idx", 2 * nsp}, {"node_adm_pairs_sidx", nn + 1},
+                          {"node_inadm_pairs_sidx", nn + 1}, {"plist_sidx", ns + 1}, {"parent", nn},
+                          {"children", nn * maxc}, {"pt_cluster", 2 * nn}, {"mat_cluster", 2 * nn},
+                          {"n_child", nn}, {"node_level", nn}, {"node_height", nn}, {"level_n_node", nl},
+                          {"level_nodes", nl * nleaf}, {"height_n_node", nl}, {"height_nodes", nl * nleaf},
+                          {"r_inadm_pairs", 2 * ninadm}, {"r_adm_pairs", 2 * nadm}, {"node_n_r_adm", nn},
+                          {"B_p2i_rowptr", nn + 1}, {"D_p2i_rowptr", nn + 1}, {"B_nrow", nB}, {"B_ncol", nB},
+                          {"D_nrow", nD}, {"D_ncol", nD}};
+    for (const Need &q : fixed)
+        if (!has(q.name, 4, q.cnt)) return false;
+    const long long nadmp = ival("node_adm_pairs_sidx", nn), ninp = ival("node_inadm_pairs_sidx", nn),
+                    npl = ival("plist_sidx", ns), nbp = ival("B_p2i_rowptr", nn), ndp = ival("D_p2i_rowptr", nn);
+    if (!has("node_adm_pairs", 4, nadmp) || !has("node_inadm_pairs", 4, ninp) || !has("plist", 4, npl) ||
+        !has("plist_idx", 4, npl) || !has("B_p2i_colidx", 4, nbp) || !has("B_p2i_val", 4, nbp) ||
+        !has("D_p2i_colidx", 4, ndp) || !has("D_p2i_val", 4, ndp) || !has("mat_size", 8, 11) ||
+        !has("timers", 8, 4))
+        return false;
+    const std::pair<const char *, long long> mats[] = {{"U", nU}, {"B", nB}, {"D", nD}};
+    for (const auto &m : mats) {
+        const std::string hn = std::string(m.first) + "_hdr";
+        if (!has(hn, 4, 4 * m.second)) return false;
+        long long tot = 0;
+        for (long long i = 0; i < m.second; i++) {
+            const long long nr = ival(hn, 4 * i), nc = ival(hn, 4 * i + 1), ld = ival(hn, 4 * i + 2),
+                            cnt = ival(hn, 4 * i + 3);
+            if (nr < 0 || nc < 0 || cnt < 0) return false;
+            if (ld < 0 ? cnt != (nr + nc) * -ld : (cnt != nr * nc || (nc > 0 && ld < nc))) return false;
+            tot += cnt;
+        }
+        if (!has(m.first, 8, tot)) return false;
+    }
+    return true;
+}
+
+}  // namespace
+
 extern "C" int H2ERI_load_representation(const char *path, H2ERI_p *h2eri_)
 {
     FILE *f = std::fopen(path, "rb");
     if (f == nullptr) return 2;
+    std::fseek(f, 0, SEEK_END);
+    const long fsize = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
     char magic[8];
-    if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kMagic, 8) != 0) { std::fclose(f); return 4; }
+    if (fsize < 8 || std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kMagic, 8) != 0) { std::fclose(f); return 4; }
     std::map<std::string, std::vector<char>> blobs;
     std::map<std::string, uint32_t> esz;
-    while (true) {
-        char nm[32];
-        uint32_t es;
-        uint64_t cnt;
-        if (std::fread(nm, 1, 32, f) != 32) break;
-        if (std::fread(&es, 4, 1, f) != 1 || std::fread(&cnt, 8, 1, f) != 1) { std::fclose(f); return 5; }
-        std::vector<char> buf((size_t)es * cnt);
-        if (cnt > 0 && std::fread(buf.data(), es, cnt, f) != cnt) { std::fclose(f); return 5; }
-        nm[31] = 0;
-        blobs[nm] = std::move(buf);
-        esz[nm] = es;
+    try {
+        while (true) {
+            char nm[32];
+            uint32_t es;
+            uint64_t cnt;
+            if (std::fread(nm, 1, 32, f) != 32) break;
+            if (std::fread(&es, 4, 1, f) != 1 || std::fread(&cnt, 8, 1, f) != 1) { std::fclose(f); return 5; }
+            /* sizes bounded by what is left of the file: no allocation from garbage */
+            const long here = std::ftell(f);
+            if ((es != 1 && es != 4 && es != 8) || cnt > (uint64_t)(fsize - here) / es) { std::fclose(f); return 5; }
+            std::vector<char> buf((size_t)es * cnt);
+            if (cnt > 0 && std::fread(buf.data(), es, cnt, f) != cnt) { std::fclose(f); return 5; }
+            nm[31] = 0;
+            blobs[nm] = std::move(buf);
+            esz[nm] = es;
+        }
+    } catch (const std::exception &) {
+        std::fclose(f);
+        return 5;
     }
     std::fclose(f);
+    if (!blobs_consistent(blobs, esz)) return 6;
     auto get_i = [&](const char *n) -> int * {
         auto it = blobs.find(n);
         H2G_CHECK(it != blobs.end(), "representation file lacks %s\n", n);

@@ -100,6 +100,56 @@ def test_load_rejects_bad_file(library, tmp_path):
         hg.H2ERI.load(str(p))
 
 
+def _blobs(raw):
+    """(name, offset of element size, offset of data, element size, count) of
+    every blob of a representation file (8-byte magic, then blobs of a 32-byte
+    name, a 4-byte element size, an 8-byte count and the data)."""
+    import struct
+    out, pos = [], 8
+    while pos + 44 <= len(raw):
+        name = raw[pos:pos + 32].split(b"\0")[0].decode()
+        es, cnt = struct.unpack_from("<IQ", raw, pos + 32)
+        out.append((name, pos + 32, pos + 44, es, cnt))
+        pos += 44 + es * cnt
+    return out
+
+
+def test_load_rejects_damaged_representation(small_mols, tmp_path):
+    """Truncation, a block header that disagrees with its data, an inflated
+    node count and a blob size beyond the file are all rejected with an error
+    (nothing is read out of bounds); the undamaged file loads."""
+    import struct
+    good = tmp_path / "good.h2r"
+    small_mols["C4H10"].save(str(good))
+    raw = good.read_bytes()
+    blobs = {b[0]: b for b in _blobs(raw)}
+
+    def rejected(data, name):
+        p = tmp_path / f"{name}.h2r"
+        p.write_bytes(bytes(data))
+        with pytest.raises(hg.H2ERIError):
+            hg.H2ERI.load(str(p))
+
+    rejected(raw[:len(raw) - 1000], "truncated")
+    d = bytearray(raw)                       # first U block claims more elements than it has
+    _, _, off, _, _ = blobs["U_hdr"]
+    struct.pack_into("<i", d, off + 12, struct.unpack_from("<i", d, off + 12)[0] + 7)
+    rejected(d, "header")
+    d = bytearray(raw)                       # n_node far above the arrays' sizes
+    _, _, off, _, _ = blobs["scalars"]
+    struct.pack_into("<i", d, off + 9 * 4, 10 ** 6)
+    rejected(d, "scalars")
+    d = bytearray(raw)                       # a blob count beyond the end of the file
+    _, cpos, _, _, _ = blobs["mat_cluster"]
+    struct.pack_into("<Q", d, cpos + 4, 1 << 40)
+    rejected(d, "count")
+    h = hg.H2ERI.load(str(good))
+    try:
+        assert h.num_bf == small_mols["C4H10"].num_bf
+    finally:
+        h.destroy()
+
+
 def test_block_storage_formats(alk32):
     """Blocks are dense (ld >= ncol) or low-rank (ld = -rank, U then V^T), and
     the low-rank form is only kept when it saves at least 20% (src/H2ERI_build_H2.c:869)."""
