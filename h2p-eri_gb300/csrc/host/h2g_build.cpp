@@ -23,71 +23,214 @@ namespace h2g {
 /* Pivoted QR and interpolative decomposition                              */
 /* ---------------------------------------------------------------------- */
 
-/* Householder QR with column pivoting on a column-major m x n matrix R
- * (leading dimension ld), stopping when the largest remaining column norm
- * drops below rel_tol times the largest initial column norm
- * (H2P-ERI src/H2E_ID_compress.c:51-184). Returns the rank; p holds the
- * column permutation. */
-static int pivoted_qr(double *R, int m, int n, int ld, double rel_tol, int *p)
+/* Two-wide double vectors (GCC vector extension, no instruction-set header):
+ * element-wise IEEE arithmetic, so every host computes the same bits. */
+typedef double v2d __attribute__((vector_size(16)));
+
+static inline v2d ld2(const double *p) { v2d v; std::memcpy(&v, p, sizeof v); return v; }
+static inline void st2(double *p, v2d v) { std::memcpy(p, &v, sizeof v); }
+static inline v2d bc2(double x) { v2d v = {x, x}; return v; }
+static inline double hsum(v2d a, v2d b) { return (a[0] + b[0]) + (a[1] + b[1]); }
+
+/* a . b over n elements: four partial sums (elements i mod 4), combined in a
+ * fixed order, then the remainder */
+static double dot(const double *a, const double *b, int n)
 {
-    const int max_iter = std::min(m, n);
-    std::vector<double> cn(n);
-    double norm_p = 0.0;
-    int pivot = 0;
+    v2d s0 = bc2(0.0), s1 = bc2(0.0);
+    int i = 0;
+    for (; i + 4 <= n; i += 4) {
+        s0 += ld2(a + i) * ld2(b + i);
+        s1 += ld2(a + i + 2) * ld2(b + i + 2);
+    }
+    double r = hsum(s0, s1);
+    for (; i < n; i++) r += a[i] * b[i];
+    return r;
+}
+
+/* out[q] = dot(c + q * ld, x, n) for q = 0..3, the same sums as dot() */
+static void dot4(const double *c, int ld, const double *x, int n, double *out)
+{
+    const double *c1 = c + ld, *c2 = c1 + ld, *c3 = c2 + ld;
+    v2d a0 = bc2(0.0), b0 = a0, a1 = a0, b1 = a0, a2 = a0, b2 = a0, a3 = a0, b3 = a0;
+    int i = 0;
+    for (; i + 4 <= n; i += 4) {
+        const v2d xa = ld2(x + i), xb = ld2(x + i + 2);
+        a0 += ld2(c + i) * xa;  b0 += ld2(c + i + 2) * xb;
+        a1 += ld2(c1 + i) * xa; b1 += ld2(c1 + i + 2) * xb;
+        a2 += ld2(c2 + i) * xa; b2 += ld2(c2 + i + 2) * xb;
+        a3 += ld2(c3 + i) * xa; b3 += ld2(c3 + i + 2) * xb;
+    }
+    double r0 = hsum(a0, b0), r1 = hsum(a1, b1), r2 = hsum(a2, b2), r3 = hsum(a3, b3);
+    for (; i < n; i++) {
+        r0 += c[i] * x[i];
+        r1 += c1[i] * x[i];
+        r2 += c2[i] * x[i];
+        r3 += c3[i] * x[i];
+    }
+    out[0] = r0; out[1] = r1; out[2] = r2; out[3] = r3;
+}
+
+/* c[lo:m) -= sum_t v_t[lo:m) f[t], t = 0..k-1, with v_t = v + t * ld; every
+ * element subtracts its k products in the order of t. Two columns at once
+ * (c2/f2 non-null) share the loads of v. */
+static void apply_block(double *c, const double *f, double *c2, const double *f2,
+                        const double *v, int ld, int k, int lo, int m)
+{
+    int i = lo;
+    if (c2) {
+        for (; i + 4 <= m; i += 4) {
+            v2d a = ld2(c + i), b = ld2(c + i + 2), a2 = ld2(c2 + i), b2 = ld2(c2 + i + 2);
+            for (int t = 0; t < k; t++) {
+                const double *vt = v + (size_t)t * ld + i;
+                const v2d va = ld2(vt), vb = ld2(vt + 2), ft = bc2(f[t]), ft2 = bc2(f2[t]);
+                a -= va * ft;  b -= vb * ft;
+                a2 -= va * ft2; b2 -= vb * ft2;
+            }
+            st2(c + i, a); st2(c + i + 2, b);
+            st2(c2 + i, a2); st2(c2 + i + 2, b2);
+        }
+    } else {
+        for (; i + 4 <= m; i += 4) {
+            v2d a = ld2(c + i), b = ld2(c + i + 2);
+            for (int t = 0; t < k; t++) {
+                const double *vt = v + (size_t)t * ld + i;
+                const v2d ft = bc2(f[t]);
+                a -= ld2(vt) * ft;
+                b -= ld2(vt + 2) * ft;
+            }
+            st2(c + i, a); st2(c + i + 2, b);
+        }
+    }
+    for (; i < m; i++) {
+        double s = c[i], s2 = c2 ? c2[i] : 0.0;
+        for (int t = 0; t < k; t++) {
+            const double vt = v[(size_t)t * ld + i];
+            s -= vt * f[t];
+            if (c2) s2 -= vt * f2[t];
+        }
+        c[i] = s;
+        if (c2) c2[i] = s2;
+    }
+}
+
+/* Householder QR with column pivoting on a column-major m x n matrix A
+ * (leading dimension ld), stopping when the largest remaining column norm
+ * drops below rel_tol times the largest initial column norm, with the
+ * reference's pivot rule, reflectors and stopping test
+ * (H2P-ERI src/H2E_ID_compress.c:51-184). Returns the rank r; rows 0..r-1
+ * of A then hold R11 and R12 and p the column permutation.
+ *
+ * Blocked as in LAPACK's xLAQPS: within a block of up to kQrBlock
+ * reflectors only the pivot column and the pivot row are brought up to date,
+ * the other columns' pending updates are kept in F (current column j =
+ * stored column j - V F(j, :)^T), and the trailing matrix is updated once
+ * per block, so each step reads the trailing matrix once instead of reading
+ * and writing it. Partial column norms are downdated from the pivot row;
+ * where the downdate has lost its accuracy (LAPACK's test, in place of the
+ * reference's absolute threshold 1e-10 on the squared norm) the column is
+ * brought up to date and its norm taken again. */
+static int pivoted_qr(double *A, int m, int n, int ld, double rel_tol, int *p)
+{
+    constexpr int kQrBlock = 32;
+    const double kDowndateTol = 1.4901161193847656e-08;   /* sqrt(2^-52) */
+    const int kmax = std::min(m, n);
+    std::vector<double> vn1(n), vn2(n), F((size_t)n * kQrBlock, 0.0), aux(kQrBlock), d4(4);
+    double norm0 = 0.0;
     for (int j = 0; j < n; j++) {
         p[j] = j;
-        double s = 0.0;
-        const double *c = R + (size_t)j * ld;
-        for (int k = 0; k < m; k++) s += c[k] * c[k];
-        cn[j] = std::sqrt(s);
+        const double *c = A + (size_t)j * ld;
+        vn1[j] = vn2[j] = std::sqrt(dot(c, c, m));
+        norm0 = std::max(norm0, vn1[j]);
     }
-    for (int j = 0; j < n; j++)
-        if (cn[j] > norm_p) { norm_p = cn[j]; pivot = j; }
-    double stop_norm = std::max(std::sqrt((double)m) * 1e-15, rel_tol) * norm_p;
-    int rank = max_iter;
-    for (int i = 0; i < max_iter; i++) {
-        if (norm_p < stop_norm) { rank = i; break; }
-        if (i != pivot) {
-            std::swap(p[i], p[pivot]);
-            std::swap(cn[i], cn[pivot]);
-            double *a = R + (size_t)i * ld, *b = R + (size_t)pivot * ld;
-            for (int k = 0; k < m; k++) std::swap(a[k], b[k]);
-        }
-        const int hl = m - i;
-        double *h = R + (size_t)i * ld + i;
-        double sign = (h[0] > 0.0) ? 1.0 : -1.0;
-        double hn = 0.0;
-        for (int k = 0; k < hl; k++) hn += h[k] * h[k];
-        hn = std::sqrt(hn);
-        h[0] += sign * hn;
-        double hn2 = 0.0;
-        for (int k = 0; k < hl; k++) hn2 += h[k] * h[k];
-        double inv = 1.0 / std::sqrt(hn2);
-        for (int k = 0; k < hl; k++) h[k] *= inv;
-        for (int j = i + 1; j < n; j++) {
-            double *c = R + (size_t)j * ld + i;
-            double d = 0.0;
-            for (int k = 0; k < hl; k++) d += h[k] * c[k];
-            d *= 2.0;
-            for (int k = 0; k < hl; k++) c[k] -= d * h[k];
-            if (cn[j] < stop_norm) { cn[j] = 0.0; continue; }
-            double t = cn[j] * cn[j] - c[0] * c[0];
-            if (t <= 1e-10) {
+    const double stop = std::max(std::sqrt((double)m) * 1e-15, rel_tol) * norm0;
+    int off = 0;
+    while (off < kmax) {
+        const int nb = std::min(kQrBlock, kmax - off);
+        int k = 0;
+        for (; k < nb; k++) {
+            const int rk = off + k;
+            int pvt = rk;
+            for (int j = rk + 1; j < n; j++)
+                if (vn1[j] > vn1[pvt]) pvt = j;
+            if (vn1[pvt] < stop) break;
+            if (pvt != rk) {
+                double *a = A + (size_t)rk * ld, *b = A + (size_t)pvt * ld;
+                for (int i = 0; i < m; i++) std::swap(a[i], b[i]);
+                for (int t = 0; t < k; t++) std::swap(F[(size_t)rk * kQrBlock + t], F[(size_t)pvt * kQrBlock + t]);
+                std::swap(p[rk], p[pvt]);
+                std::swap(vn1[rk], vn1[pvt]);
+                std::swap(vn2[rk], vn2[pvt]);
+            }
+            double *x = A + (size_t)rk * ld;
+            const double *V = A + (size_t)off * ld;
+            /* the pivot column, up to date below its pivot row */
+            apply_block(x, &F[(size_t)rk * kQrBlock], nullptr, nullptr, V, ld, k, rk, m);
+            /* reflector I - tau v v^T with v = (1, x[rk+1:m) / (alpha - beta)) */
+            const double alpha = x[rk];
+            const double xn = dot(x + rk + 1, x + rk + 1, m - rk - 1);
+            double tau = 0.0, beta = alpha;
+            if (xn > 0.0) {
+                beta = -std::copysign(std::sqrt(alpha * alpha + xn), alpha);
+                tau = (beta - alpha) / beta;
+                const double sc = 1.0 / (alpha - beta);
+                for (int i = rk + 1; i < m; i++) x[i] *= sc;
+            }
+            x[rk] = 1.0;
+            /* F(j, k) = tau (A(rk:m, j)^T v) + F(j, 0:k) aux, aux = -tau V(rk:m, 0:k)^T v */
+            int j = rk + 1;
+            for (; j + 4 <= n; j += 4) {
+                dot4(A + (size_t)j * ld + rk, ld, x + rk, m - rk, d4.data());
+                for (int q = 0; q < 4; q++) F[(size_t)(j + q) * kQrBlock + k] = tau * d4[q];
+            }
+            for (; j < n; j++) F[(size_t)j * kQrBlock + k] = tau * dot(A + (size_t)j * ld + rk, x + rk, m - rk);
+            if (k > 0) {
+                for (int t = 0; t < k; t++) aux[t] = -tau * dot(V + (size_t)t * ld + rk, x + rk, m - rk);
+                for (j = rk + 1; j < n; j++) {
+                    double *f = &F[(size_t)j * kQrBlock];
+                    double s = 0.0;
+                    for (int t = 0; t < k; t++) s += f[t] * aux[t];
+                    f[k] += s;
+                }
+            }
+            /* the pivot row: A(rk, j) -= A(rk, off:rk+1) F(j, 0:k+1)^T */
+            for (j = rk + 1; j < n; j++) {
+                const double *f = &F[(size_t)j * kQrBlock];
                 double s = 0.0;
-                for (int k = 1; k < hl; k++) s += c[k] * c[k];
-                cn[j] = std::sqrt(s);
-            } else {
-                cn[j] = std::sqrt(t);
+                for (int t = 0; t <= k; t++) s += V[(size_t)t * ld + rk] * f[t];
+                A[(size_t)j * ld + rk] -= s;
+            }
+            x[rk] = beta;
+            /* downdate the remaining column norms */
+            for (j = rk + 1; j < n; j++) {
+                if (vn1[j] < stop) { vn1[j] = 0.0; continue; }
+                const double q = std::fabs(A[(size_t)j * ld + rk]) / vn1[j];
+                const double t = std::max(0.0, (1.0 + q) * (1.0 - q));
+                const double r = vn1[j] / vn2[j];
+                if (t * r * r > kDowndateTol) {
+                    vn1[j] *= std::sqrt(t);
+                    continue;
+                }
+                double *c = A + (size_t)j * ld;
+                double *f = &F[(size_t)j * kQrBlock];
+                apply_block(c, f, nullptr, nullptr, V, ld, k + 1, rk + 1, m);
+                std::fill(f, f + k + 1, 0.0);
+                vn1[j] = vn2[j] = std::sqrt(dot(c + rk + 1, c + rk + 1, m - rk - 1));
             }
         }
-        h[0] = -sign * hn;
-        for (int k = 1; k < hl; k++) h[k] = 0.0;
-        pivot = i + 1;
-        norm_p = 0.0;
-        for (int j = i + 1; j < n; j++)
-            if (cn[j] > norm_p) { norm_p = cn[j]; pivot = j; }
+        /* the trailing matrix: A(r0:m, r0:n) -= V(r0:m, 0:k) F(r0:n, 0:k)^T */
+        const int r0 = off + k;
+        if (k > 0) {
+            const double *V = A + (size_t)off * ld;
+            int j = r0;
+            for (; j + 2 <= n; j += 2)
+                apply_block(A + (size_t)j * ld, &F[(size_t)j * kQrBlock], A + (size_t)(j + 1) * ld,
+                            &F[(size_t)(j + 1) * kQrBlock], V, ld, k, r0, m);
+            if (j < n) apply_block(A + (size_t)j * ld, &F[(size_t)j * kQrBlock], nullptr, nullptr, V, ld, k, r0, m);
+        }
+        if (k < nb) return r0;
+        off = r0;
     }
-    return rank;
+    return kmax;
 }
 
 /* ID over the rows of a row-major nrow x ncol matrix A: A ~= U * A(J, :)
@@ -120,12 +263,28 @@ void id_compress(H2E_dense_mat_p A, double rel_tol, H2E_dense_mat_p *U_out, H2E_
     /* E = R11^{-1} R12, R11 r x r upper triangular, R12 r x (nrow - r); column-major with ld */
     const int ne = nrow - r;
     double *R = A->data;
-    for (int c = 0; c < ne; c++) {
-        double *x = R + (size_t)(r + c) * ld;
+    /* back substitution by columns of R11 (contiguous), two columns of E at once */
+    int ce = 0;
+    for (; ce + 2 <= ne; ce += 2) {
+        double *x = R + (size_t)(r + ce) * ld, *y = x + ld;
         for (int i = r - 1; i >= 0; i--) {
-            double s = x[i];
-            for (int k = i + 1; k < r; k++) s -= R[(size_t)k * ld + i] * x[k];
-            x[i] = s / R[(size_t)i * ld + i];
+            const double *ri = R + (size_t)i * ld;
+            const double xi = x[i] / ri[i], yi = y[i] / ri[i];
+            x[i] = xi;
+            y[i] = yi;
+            for (int k = 0; k < i; k++) {
+                x[k] -= ri[k] * xi;
+                y[k] -= ri[k] * yi;
+            }
+        }
+    }
+    for (; ce < ne; ce++) {
+        double *x = R + (size_t)(r + ce) * ld;
+        for (int i = r - 1; i >= 0; i--) {
+            const double *ri = R + (size_t)i * ld;
+            const double xi = x[i] / ri[i];
+            x[i] = xi;
+            for (int k = 0; k < i; k++) x[k] -= ri[k] * xi;
         }
     }
     H2E_dense_mat_p U = dmat_new(nrow, r);
