@@ -107,13 +107,17 @@ void h2g_boys(int mmax, double T, double *F)
         int k = (int)(T / BOYS_H + 0.5);
         double d = T - k * BOYS_H;                   /* |d| <= h/2 */
         const double *row = g_boys_tab[k];
+        /* F_m(T_k + d) = sum_j F_{m+j}(T_k) (-d)^j / j!, the factors shared by all m */
+        _Static_assert(BOYS_NTAY == 7, "one factor 1/j! per Taylor term");
+        static const double inv_fact[BOYS_NTAY] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720};
+        double f[BOYS_NTAY], pw = 1.0;
+        for (int j = 0; j < BOYS_NTAY; j++) {
+            f[j] = pw * inv_fact[j];
+            pw *= -d;
+        }
         for (int m = 0; m <= mmax; m++) {
-            /* F_m(T_k + d) = sum_j F_{m+j}(T_k) (-d)^j / j! */
-            double s = 0.0, f = 1.0;
-            for (int j = 0; j < BOYS_NTAY; j++) {
-                s += row[m + j] * f;
-                f *= -d / (double)(j + 1);
-            }
+            double s = 0.0;
+            for (int j = 0; j < BOYS_NTAY; j++) s += row[m + j] * f[j];
             F[m] = s;
         }
     } else {
@@ -236,20 +240,108 @@ static void hrr(int l1, int l2, const double AB[3], const double *src, int nrep,
 /* ERI                                                                      */
 /* ------------------------------------------------------------------------ */
 
+/* Primitive quartets are processed H2G_LANES at a time: every recurrence
+ * term is a GCC vector of one value per quartet (element-wise IEEE
+ * arithmetic, no instruction-set header), so the index bookkeeping of the
+ * recurrences is shared by the lanes. */
+#define H2G_LANES 4
+typedef double vlane __attribute__((vector_size(H2G_LANES * sizeof(double))));
+_Static_assert(H2G_LANES == 4, "the lane sums below add four lanes");
+
 typedef struct {
-    double vrr[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L) * (H2G_MAX_M + 1)];
+    vlane *vrr;       /* [(e nf + f) nm + m], grown to the largest class seen */
+    size_t vrr_cap;
     double acc[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L)];
     double t1[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L) * 8];
     double w1[2 * H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L) * 16];
+    double *kq;       /* per ket primitive pair: 1/q and K/q */
+    int kq_cap;
 } eri_ws;
 
 static __thread eri_ws *tls_ws = NULL;
 
 static eri_ws *get_ws(void)
 {
-    if (tls_ws == NULL) tls_ws = (eri_ws *)malloc(sizeof(eri_ws));
+    if (tls_ws == NULL) {
+        tls_ws = (eri_ws *)malloc(sizeof(eri_ws));
+        tls_ws->vrr = NULL;
+        tls_ws->vrr_cap = 0;
+        tls_ws->kq = NULL;
+        tls_ws->kq_cap = 0;
+    }
     return tls_ws;
 }
+
+static vlane *vrr_buf(eri_ws *ws, size_t n)
+{
+    if (ws->vrr_cap < n) {
+        free(ws->vrr);
+        ws->vrr = (vlane *)aligned_alloc(64, ((n * sizeof(vlane) + 63) / 64) * 64);
+        ws->vrr_cap = n;
+    }
+    return ws->vrr;
+}
+
+/* 1/q and K/q of every ket primitive pair, in ws->kq[2 j], ws->kq[2 j + 1] */
+static const double *ket_recip(eri_ws *ws, const h2g_pair *ket)
+{
+    if (ws->kq_cap < ket->nprim) {
+        free(ws->kq);
+        ws->kq_cap = ket->nprim < 64 ? 64 : ket->nprim;
+        ws->kq = (double *)malloc(sizeof(double) * 2 * (size_t)ws->kq_cap);
+    }
+    for (int j = 0; j < ket->nprim; j++) {
+        const double iq = 1.0 / ket->p[j];
+        ws->kq[2 * j] = iq;
+        ws->kq[2 * j + 1] = ket->K[j] * iq;
+    }
+    return ws->kq;
+}
+
+/* Obara-Saika vertical recurrences for one batch of primitive quartets, on
+ * values of type T (double, or vlane for H2G_LANES quartets at once):
+ * V[(e nf + f) nm + m] = [e|f]^(m), from [0|0]^(m) in V[0..M]. */
+#define VRR(T)                                                                                  \
+    do {                                                                                        \
+        /* bra side: [e|0]^(m) */                                                               \
+        for (int c = 1; c < ne; c++) {                                                          \
+            const int L = g_lxyz[c][0] + g_lxyz[c][1] + g_lxyz[c][2];                           \
+            const int d = g_dir[c], e = g_prev[c], e2 = g_prev2[c];                             \
+            T *vc = V + (size_t)c * nf * nm;                                                    \
+            const T *ve = V + (size_t)e * nf * nm;                                              \
+            if (e2 >= 0) {                                                                      \
+                const T *ve2 = V + (size_t)e2 * nf * nm;                                        \
+                const T ei2p = (double)(g_lxyz[c][d] - 1) * i2p;                                \
+                for (int m = 0; m <= M - L; m++)                                                \
+                    vc[m] = PA[d] * ve[m] + WP[d] * ve[m + 1] + ei2p * (ve2[m] - rp * ve2[m + 1]);\
+            } else {                                                                            \
+                for (int m = 0; m <= M - L; m++) vc[m] = PA[d] * ve[m] + WP[d] * ve[m + 1];     \
+            }                                                                                   \
+        }                                                                                       \
+        /* ket side: [e|f]^(m) */                                                               \
+        for (int c = 1; c < nf; c++) {                                                          \
+            const int Lf = g_lxyz[c][0] + g_lxyz[c][1] + g_lxyz[c][2];                          \
+            const int d = g_dir[c], f = g_prev[c], f2 = g_prev2[c];                             \
+            const T fi2q = (double)(g_lxyz[c][d] - 1) * i2q;                                    \
+            for (int e = 0; e < ne; e++) {                                                      \
+                const int Le = g_lxyz[e][0] + g_lxyz[e][1] + g_lxyz[e][2];                      \
+                const int mmax = M - Le - Lf;                                                   \
+                if (mmax < 0) continue;                                                         \
+                T *vc = V + ((size_t)e * nf + c) * nm;                                          \
+                const T *vf = V + ((size_t)e * nf + f) * nm;                                    \
+                const T *vf2 = (f2 >= 0) ? V + ((size_t)e * nf + f2) * nm : NULL;               \
+                const int em = g_minus[e][d];                                                   \
+                const T *vem = (em >= 0) ? V + ((size_t)em * nf + f) * nm : NULL;               \
+                const T ed2pq = (double)g_lxyz[e][d] * i2pq;                                    \
+                for (int m = 0; m <= mmax; m++) {                                               \
+                    T v = QC[d] * vf[m] + WQ[d] * vf[m + 1];                                    \
+                    if (vf2) v += fi2q * (vf2[m] - rq * vf2[m + 1]);                            \
+                    if (vem) v += ed2pq * vem[m + 1];                                           \
+                    vc[m] = v;                                                                  \
+                }                                                                               \
+            }                                                                                   \
+        }                                                                                       \
+    } while (0)
 
 void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
 {
@@ -261,16 +353,22 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
     double *acc = ws->acc;
     const double two_pi_52 = 2.0 * pow(M_PI, 2.5);
 
+    /* per primitive quartet: 1/(p+q) is the only division; with 1/p per bra
+     * and 1/q, K/q per ket primitive pair,
+     *   rho = p q / (p+q), W - P = q (Q - P) / (p+q), W - Q = p (P - Q) / (p+q),
+     *   prefactor 2 pi^(5/2) K_ab K_cd / (p q sqrt(p+q)) */
+    const double *kq = ket_recip(ws, ket);
     if (M == 0) {
         double s = 0.0, F[1];
         for (int i = 0; i < bra->nprim; i++) {
             const double p = bra->p[i], *P = bra->P + 3 * i;
+            const double kp = two_pi_52 * bra->K[i] / p;
             for (int j = 0; j < ket->nprim; j++) {
                 const double q = ket->p[j], *Q = ket->P + 3 * j;
-                double pq = p + q, rho = p * q / pq;
+                const double ipq = 1.0 / (p + q), rho = p * q * ipq;
                 double dx = P[0] - Q[0], dy = P[1] - Q[1], dz = P[2] - Q[2];
                 h2g_boys(0, rho * (dx * dx + dy * dy + dz * dz), F);
-                s += two_pi_52 / (p * q * sqrt(pq)) * bra->K[i] * ket->K[j] * F[0];
+                s += kp * kq[2 * j + 1] * sqrt(ipq) * F[0];
             }
         }
         out[0] = s;
@@ -278,71 +376,70 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
     }
 
     memset(acc, 0, sizeof(double) * (size_t)ne * nf);
-    double *V = ws->vrr;
-    /* V[(e * nf + f) * nm + m] */
-    for (int i = 0; i < bra->nprim; i++) {
+    vlane *Vv = vrr_buf(ws, (size_t)ne * nf * nm);
+    const int nk = ket->nprim, nq = bra->nprim * nk;
+    /* one or two primitive quartets: one at a time (lanes would be idle) */
+    for (int qi = 0; qi < (nq <= 2 ? nq : 0); qi++) {
+        double *V = (double *)Vv;
+        const int i = qi / nk, j = qi - i * nk;
         const double p = bra->p[i], *P = bra->P + 3 * i;
-        double PA[3] = {P[0] - bra->A[0], P[1] - bra->A[1], P[2] - bra->A[2]};
-        for (int j = 0; j < ket->nprim; j++) {
+        const double q = ket->p[j], *Q = ket->P + 3 * j;
+        const double ipq = 1.0 / (p + q), rho = p * q * ipq, ip = 1.0 / p;
+        double PA[3], WP[3], WQ[3], QC[3], PQ2 = 0.0;
+        for (int d = 0; d < 3; d++) {
+            const double pq_d = P[d] - Q[d];
+            PA[d] = P[d] - bra->A[d];
+            WP[d] = -(q * ipq) * pq_d;
+            WQ[d] = (p * ipq) * pq_d;
+            QC[d] = Q[d] - ket->A[d];
+            PQ2 += pq_d * pq_d;
+        }
+        const double i2p = 0.5 * ip, rp = q * ipq, i2q = 0.5 * kq[2 * j], rq = p * ipq, i2pq = 0.5 * ipq;
+        double F[H2G_MAX_M + 1];
+        h2g_boys(M, rho * PQ2, F);
+        const double pref = two_pi_52 * bra->K[i] * ip * kq[2 * j + 1] * sqrt(ipq);
+        for (int m = 0; m <= M; m++) V[m] = pref * F[m];
+        VRR(double);
+        for (int e = g_cum[la]; e < ne; e++)
+            for (int f = g_cum[lc]; f < nf; f++) acc[e * nf + f] += V[((size_t)e * nf + f) * nm];
+    }
+    for (int q0 = 0; q0 < (nq <= 2 ? 0 : nq); q0 += H2G_LANES) {
+        vlane *V = Vv;
+        /* lane l holds primitive quartet q0 + l = (i, j); lanes past the end
+         * carry a zero prefactor and finite geometry, so they add zeros */
+        vlane PA[3], WP[3], WQ[3], QC[3], i2p, rp, i2q, rq, i2pq;
+        double F[H2G_LANES][H2G_MAX_M + 1], pref[H2G_LANES];
+        for (int l = 0; l < H2G_LANES; l++) {
+            const int qi = (q0 + l < nq) ? q0 + l : q0;
+            const int i = qi / nk, j = qi - i * nk;
+            const double p = bra->p[i], *P = bra->P + 3 * i;
             const double q = ket->p[j], *Q = ket->P + 3 * j;
-            const double pq = p + q, rho = p * q / pq;
-            double W[3], WP[3], WQ[3], QC[3];
+            const double ipq = 1.0 / (p + q), rho = p * q * ipq, ip = 1.0 / p;
             double PQ2 = 0.0;
             for (int d = 0; d < 3; d++) {
-                W[d] = (p * P[d] + q * Q[d]) / pq;
-                WP[d] = W[d] - P[d];
-                WQ[d] = W[d] - Q[d];
-                QC[d] = Q[d] - ket->A[d];
-                PQ2 += (P[d] - Q[d]) * (P[d] - Q[d]);
+                const double pq_d = P[d] - Q[d];
+                PA[d][l] = P[d] - bra->A[d];
+                WP[d][l] = -(q * ipq) * pq_d;
+                WQ[d][l] = (p * ipq) * pq_d;
+                QC[d][l] = Q[d] - ket->A[d];
+                PQ2 += pq_d * pq_d;
             }
-            double F[H2G_MAX_M + 1];
-            h2g_boys(M, rho * PQ2, F);
-            const double pref = two_pi_52 / (p * q * sqrt(pq)) * bra->K[i] * ket->K[j];
-            for (int m = 0; m <= M; m++) V[m] = pref * F[m];
-            const double i2p = 0.5 / p, rp = rho / p, i2q = 0.5 / q, rq = rho / q, i2pq = 0.5 / pq;
-            /* bra side: [e|0]^(m) */
-            for (int c = 1; c < ne; c++) {
-                const int L = g_lxyz[c][0] + g_lxyz[c][1] + g_lxyz[c][2];
-                const int d = g_dir[c], e = g_prev[c], e2 = g_prev2[c];
-                const double ei = (double)(g_lxyz[c][d] - 1);
-                double *vc = V + (size_t)c * nf * nm;
-                const double *ve = V + (size_t)e * nf * nm;
-                for (int m = 0; m <= M - L; m++) {
-                    double v = PA[d] * ve[m] + WP[d] * ve[m + 1];
-                    if (e2 >= 0) {
-                        const double *ve2 = V + (size_t)e2 * nf * nm;
-                        v += ei * i2p * (ve2[m] - rp * ve2[m + 1]);
-                    }
-                    vc[m] = v;
-                }
-            }
-            /* ket side: [e|f]^(m) */
-            for (int c = 1; c < nf; c++) {
-                const int Lf = g_lxyz[c][0] + g_lxyz[c][1] + g_lxyz[c][2];
-                const int d = g_dir[c], f = g_prev[c], f2 = g_prev2[c];
-                const double fi = (double)(g_lxyz[c][d] - 1);
-                for (int e = 0; e < ne; e++) {
-                    const int Le = g_lxyz[e][0] + g_lxyz[e][1] + g_lxyz[e][2];
-                    const int mmax = M - Le - Lf;
-                    if (mmax < 0) continue;
-                    double *vc = V + ((size_t)e * nf + c) * nm;
-                    const double *vf = V + ((size_t)e * nf + f) * nm;
-                    const double *vf2 = (f2 >= 0) ? V + ((size_t)e * nf + f2) * nm : NULL;
-                    const int em = g_minus[e][d];
-                    const double ed = (double)g_lxyz[e][d];
-                    const double *vem = (em >= 0) ? V + ((size_t)em * nf + f) * nm : NULL;
-                    for (int m = 0; m <= mmax; m++) {
-                        double v = QC[d] * vf[m] + WQ[d] * vf[m + 1];
-                        if (vf2) v += fi * i2q * (vf2[m] - rq * vf2[m + 1]);
-                        if (vem) v += ed * i2pq * vem[m + 1];
-                        vc[m] = v;
-                    }
-                }
-            }
-            for (int e = g_cum[la]; e < ne; e++)
-                for (int f = g_cum[lc]; f < nf; f++)
-                    acc[e * nf + f] += V[((size_t)e * nf + f) * nm];
+            i2p[l] = 0.5 * ip;
+            rp[l] = q * ipq;
+            i2q[l] = 0.5 * kq[2 * j];
+            rq[l] = p * ipq;
+            i2pq[l] = 0.5 * ipq;
+            h2g_boys(M, rho * PQ2, F[l]);
+            pref[l] = (q0 + l < nq) ? two_pi_52 * bra->K[i] * ip * kq[2 * j + 1] * sqrt(ipq) : 0.0;
         }
+        for (int m = 0; m <= M; m++)
+            for (int l = 0; l < H2G_LANES; l++) V[m][l] = pref[l] * F[l][m];
+        VRR(vlane);
+        for (int e = g_cum[la]; e < ne; e++)
+            for (int f = g_cum[lc]; f < nf; f++) {
+                const vlane v = V[((size_t)e * nf + f) * nm];
+                acc[e * nf + f] += (v[0] + v[1]) + (v[2] + v[3]);   /* H2G_LANES == 4 */
+            }
     }
 
     /* HRR on the bra: acc[e][f] -> t1[(a b)][f], f kept as a trailing vector */
