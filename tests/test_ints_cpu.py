@@ -98,3 +98,23 @@ def test_ssss_closed_form(L):
     F0 = 0.5 * sqrt(pi / T) * erf(sqrt(T))
     ref = 2 * pi ** 2.5 / (p * q * sqrt(p + q)) * F0
     assert abs(v - ref) < 1e-13 * ref
+
+
+def test_eri_contraction_is_sum_of_primitive_quartets(L):
+    """Linearity in the contraction: a contracted quartet (here 3 x 3 = 9
+    primitive quartets, computed four at a time with one padded batch) equals
+    the sum of its single-primitive quartets (computed one at a time)."""
+    keep = []
+    rng = np.random.default_rng(7)
+    cen = [rng.uniform(-1.5, 1.5, 3) for _ in range(4)]
+    aA, cA = [4.1, 1.2, 0.35], [0.3, -0.5, 0.8]
+    aC, cC = [2.2, 0.9, 0.27], [0.6, 0.4, -0.2]
+    B = make_shell(2, cen[1], [0.8], [1.1], keep)
+    D = make_shell(0, cen[3], [0.5], [0.9], keep)
+    full = quartet(L, make_shell(1, cen[0], aA, cA, keep), B, make_shell(1, cen[2], aC, cC, keep), D)
+    parts = np.zeros_like(full)
+    for i in range(3):
+        for k in range(3):
+            parts += quartet(L, make_shell(1, cen[0], [aA[i]], [cA[i]], keep), B,
+                             make_shell(1, cen[2], [aC[k]], [cC[k]], keep), D)
+    np.testing.assert_allclose(full, parts, rtol=1e-12, atol=1e-14 * np.abs(full).max())
