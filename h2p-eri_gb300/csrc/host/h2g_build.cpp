@@ -217,8 +217,10 @@ static int pivoted_qr(double *A, int m, int n, int ld, double rel_tol, int *p)
                 vn1[j] = vn2[j] = std::sqrt(dot(c + rk + 1, c + rk + 1, m - rk - 1));
             }
         }
-        /* the trailing matrix: A(r0:m, r0:n) -= V(r0:m, 0:k) F(r0:n, 0:k)^T */
+        /* stopped inside the block: rows 0..r0-1 (R11, R12) are final already */
         const int r0 = off + k;
+        if (k < nb) return r0;
+        /* the trailing matrix: A(r0:m, r0:n) -= V(r0:m, 0:k) F(r0:n, 0:k)^T */
         if (k > 0) {
             const double *V = A + (size_t)off * ld;
             int j = r0;
@@ -227,7 +229,6 @@ static int pivoted_qr(double *A, int m, int n, int ld, double rel_tol, int *p)
                             &F[(size_t)(j + 1) * kQrBlock], V, ld, k, r0, m);
             if (j < n) apply_block(A + (size_t)j * ld, &F[(size_t)j * kQrBlock], nullptr, nullptr, V, ld, k, r0, m);
         }
-        if (k < nb) return r0;
         off = r0;
     }
     return kmax;
