@@ -457,26 +457,39 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
 /* Point-charge potential integrals                                         */
 /* ------------------------------------------------------------------------ */
 
-void h2g_potential(const h2g_shell *A, const h2g_shell *B,
-                   double cx, double cy, double cz, double charge, double *out)
+void h2g_potential_points(const h2g_shell *A, const h2g_shell *B, int n_pt, const double *cx,
+                          const double *cy, const double *cz, double charge, double *out, int ldo)
 {
     h2g_ints_init();
     const int la = A->am, lb = B->am, L = la + lb;
-    const int ne = g_cum[L + 1], nm = L + 1;
+    const int ne = g_cum[L + 1], nm = L + 1, nab = h2g_ncart(la) * h2g_ncart(lb);
     double acc[H2G_NCUM(H2G_MAX_L)];
     double V[H2G_NCUM(H2G_MAX_L) * (H2G_MAX_L + 1)];
     double work[2 * H2G_NCUM(H2G_MAX_L) * 16];
-    memset(acc, 0, sizeof(double) * ne);
-    const double Av[3] = {A->x, A->y, A->z}, Bv[3] = {B->x, B->y, B->z}, C[3] = {cx, cy, cz};
+    double res[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L)];
+    const double Av[3] = {A->x, A->y, A->z}, Bv[3] = {B->x, B->y, B->z};
     double ab2 = 0.0;
     for (int d = 0; d < 3; d++) ab2 += (Av[d] - Bv[d]) * (Av[d] - Bv[d]);
+    /* primitive-pair data, shared by all points: p, K, P[3] */
+    const int npp = A->nprim * B->nprim;
+    double *pp = (double *)malloc(sizeof(double) * 5 * (size_t)(npp > 0 ? npp : 1));
     for (int i = 0; i < A->nprim; i++)
         for (int j = 0; j < B->nprim; j++) {
             const double a = A->alpha[i], b = B->alpha[j], p = a + b;
-            const double K = A->coef[i] * B->coef[j] * exp(-a * b / p * ab2);
-            double P[3], PA[3], PC[3], PC2 = 0.0;
+            double *q = pp + 5 * (i * B->nprim + j);
+            q[0] = p;
+            q[1] = A->coef[i] * B->coef[j] * exp(-a * b / p * ab2);
+            for (int d = 0; d < 3; d++) q[2 + d] = (a * Av[d] + b * Bv[d]) / p;
+        }
+    const double ABv[3] = {Av[0] - Bv[0], Av[1] - Bv[1], Av[2] - Bv[2]};
+    for (int pt = 0; pt < n_pt; pt++) {
+        const double C[3] = {cx[pt], cy[pt], cz[pt]};
+        memset(acc, 0, sizeof(double) * ne);
+        for (int k = 0; k < npp; k++) {
+            const double *q = pp + 5 * k;
+            const double p = q[0], K = q[1], *P = q + 2;
+            double PA[3], PC[3], PC2 = 0.0;
             for (int d = 0; d < 3; d++) {
-                P[d] = (a * Av[d] + b * Bv[d]) / p;
                 PA[d] = P[d] - Av[d];
                 PC[d] = P[d] - C[d];
                 PC2 += PC[d] * PC[d];
@@ -499,6 +512,14 @@ void h2g_potential(const h2g_shell *A, const h2g_shell *B,
             }
             for (int e = g_cum[la]; e < ne; e++) acc[e] += V[e * nm];
         }
-    double ABv[3] = {Av[0] - Bv[0], Av[1] - Bv[1], Av[2] - Bv[2]};
-    hrr(la, lb, ABv, acc, 1, out, work);
+        hrr(la, lb, ABv, acc, 1, res, work);
+        for (int r = 0; r < nab; r++) out[(size_t)r * ldo + pt] = res[r];
+    }
+    free(pp);
+}
+
+void h2g_potential(const h2g_shell *A, const h2g_shell *B,
+                   double cx, double cy, double cz, double charge, double *out)
+{
+    h2g_potential_points(A, B, 1, &cx, &cy, &cz, charge, out, 1);
 }

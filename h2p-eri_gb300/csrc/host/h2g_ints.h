@@ -69,6 +69,12 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out);
 void h2g_potential(const h2g_shell *A, const h2g_shell *B,
                    double cx, double cy, double cz, double charge, double *out);
 
+/* The same for n_pt charges at (cx[k], cy[k], cz[k]), the primitive-pair
+ * data formed once: out[ab * ldo + k] is component ab (row-major [a][b]) at
+ * point k. */
+void h2g_potential_points(const h2g_shell *A, const h2g_shell *B, int n_pt, const double *cx,
+                          const double *cy, const double *cz, double charge, double *out, int ldo);
+
 /* Boys function F_m(T) for m = 0..mmax (mmax <= 4*H2G_MAX_AM). */
 void h2g_boys(int mmax, double T, double *F);
 

@@ -196,19 +196,14 @@ void nai_pairs_to_mat(H2ERI_p h2eri, int n_bra, const int *bra, int n_pt,
                       const double *x, const double *y, const double *z, double *mat, int ldm)
 {
     int num_sp = h2eri->num_sp;
-    double buf[15 * 15];
     int row = 0;
     for (int i = 0; i < n_bra; i++) {
         const shell_t *Ms = h2eri->sp_shells + bra[i];
         const shell_t *Ns = h2eri->sp_shells + bra[i] + num_sp;
         h2g_shell M = {Ms->am, Ms->nprim, Ms->x, Ms->y, Ms->z, Ms->alpha, Ms->coef};
         h2g_shell N = {Ns->am, Ns->nprim, Ns->x, Ns->y, Ns->z, Ns->alpha, Ns->coef};
-        int nr = h2g_ncart(M.am) * h2g_ncart(N.am);
-        for (int p = 0; p < n_pt; p++) {
-            h2g_potential(&N, &M, x[p], y[p], z[p], 1.0, buf);
-            for (int r = 0; r < nr; r++) mat[(size_t)(row + r) * ldm + p] = buf[r];
-        }
-        row += nr;
+        h2g_potential_points(&N, &M, n_pt, x, y, z, 1.0, mat + (size_t)row * ldm, ldm);
+        row += h2g_ncart(M.am) * h2g_ncart(N.am);
     }
 }
 
