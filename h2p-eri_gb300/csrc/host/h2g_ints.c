@@ -403,15 +403,18 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
         for (int e = g_cum[la]; e < ne; e++)
             for (int f = g_cum[lc]; f < nf; f++) acc[e * nf + f] += V[((size_t)e * nf + f) * nm];
     }
+    int ci = 0, cj = 0;   /* (i, j) of primitive quartet q0 */
     for (int q0 = 0; q0 < (nq <= 2 ? 0 : nq); q0 += H2G_LANES) {
         vlane *V = Vv;
         /* lane l holds primitive quartet q0 + l = (i, j); lanes past the end
-         * carry a zero prefactor and finite geometry, so they add zeros */
+         * repeat quartet q0 with a zero prefactor, so they add zeros */
         vlane PA[3], WP[3], WQ[3], QC[3], i2p, rp, i2q, rq, i2pq;
         double F[H2G_LANES][H2G_MAX_M + 1], pref[H2G_LANES];
+        const int i0 = ci, j0 = cj;
         for (int l = 0; l < H2G_LANES; l++) {
-            const int qi = (q0 + l < nq) ? q0 + l : q0;
-            const int i = qi / nk, j = qi - i * nk;
+            const int live = q0 + l < nq;
+            const int i = live ? ci : i0, j = live ? cj : j0;
+            if (live && ++cj == nk) { cj = 0; ci++; }
             const double p = bra->p[i], *P = bra->P + 3 * i;
             const double q = ket->p[j], *Q = ket->P + 3 * j;
             const double ipq = 1.0 / (p + q), rho = p * q * ipq, ip = 1.0 / p;
@@ -430,7 +433,7 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
             rq[l] = p * ipq;
             i2pq[l] = 0.5 * ipq;
             h2g_boys(M, rho * PQ2, F[l]);
-            pref[l] = (q0 + l < nq) ? two_pi_52 * bra->K[i] * ip * kq[2 * j + 1] * sqrt(ipq) : 0.0;
+            pref[l] = live ? two_pi_52 * bra->K[i] * ip * kq[2 * j + 1] * sqrt(ipq) : 0.0;
         }
         for (int m = 0; m <= M; m++)
             for (int l = 0; l < H2G_LANES; l++) V[m][l] = pref[l] * F[l][m];
