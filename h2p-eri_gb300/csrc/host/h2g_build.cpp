@@ -142,6 +142,7 @@ static int pivoted_qr(double *A, int m, int n, int ld, double rel_tol, int *p)
         vn1[j] = vn2[j] = std::sqrt(dot(c, c, m));
         norm0 = std::max(norm0, vn1[j]);
     }
+    if (!(norm0 > 0.0)) return 0;   /* a zero matrix has rank 0 (no zero pivots) */
     const double stop = std::max(std::sqrt((double)m) * 1e-15, rel_tol) * norm0;
     int off = 0;
     while (off < kmax) {
