@@ -911,6 +911,23 @@ void build_h2(H2ERI_p h)
 
 }  // namespace h2g
 
+extern "C" int h2g_id_rows(int nrow, int ncol, const double *A, double rel_tol, int *J, double *U)
+{
+    using namespace h2g;
+    H2E_dense_mat_p M = dmat_new(nrow, ncol);
+    if ((size_t)nrow * ncol > 0) std::memcpy(M->data, A, sizeof(double) * (size_t)nrow * ncol);
+    H2E_int_vec_p Jv = ivec_new(std::max(nrow, 1));
+    H2E_dense_mat_p Um = nullptr;
+    id_compress(M, rel_tol, &Um, Jv);
+    const int r = Jv->length;
+    std::memcpy(J, Jv->data, sizeof(int) * (size_t)r);
+    if (r > 0) std::memcpy(U, Um->data, sizeof(double) * (size_t)nrow * r);
+    dmat_free(&M);
+    dmat_free(&Um);
+    ivec_free(&Jv);
+    return r;
+}
+
 extern "C" void H2ERI_build_H2(H2ERI_p h2eri, const int BD_JIT)
 {
     H2G_CHECK(BD_JIT == 0,

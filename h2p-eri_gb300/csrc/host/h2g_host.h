@@ -66,4 +66,9 @@ void build_h2(H2ERI_p h2eri);
 
 }  // namespace h2g
 
+/* id_compress on a copy of a row-major nrow x ncol matrix, for tests through
+ * the shared library: returns the rank r, J[0..r) the sorted skeleton rows,
+ * U (nrow x r, row-major, room for nrow * min(nrow, ncol) values). */
+extern "C" int h2g_id_rows(int nrow, int ncol, const double *A, double rel_tol, int *J, double *U);
+
 #endif
