@@ -341,18 +341,19 @@ extern "C" void CMS_read_mol_file(const char *mol_fname, int *natom_, int *nshel
         return (int)(p - tbl);
     };
     int natom = 0;
-    H2G_CHECK(std::fscanf(f, "%d", &natom) == 1, "bad mol header\n");
+    H2G_CHECK(std::fscanf(f, "%d", &natom) == 1 && natom >= 0, "bad mol header\n");
     std::vector<shell_t> shells;
     for (int a = 0; a < natom; a++) {
         char sym[16];
         int nshell, nprimall, nallprimg;
         double x, y, z;
-        H2G_CHECK(std::fscanf(f, "%15s %d %d %d", sym, &nshell, &nprimall, &nallprimg) == 4, "bad atom header\n");
+        H2G_CHECK(std::fscanf(f, "%15s %d %d %d", sym, &nshell, &nprimall, &nallprimg) == 4 && nshell >= 0,
+                  "bad atom header\n");
         H2G_CHECK(std::fscanf(f, "%lf %lf %lf", &x, &y, &z) == 3, "bad coordinates\n");
         for (int s = 0; s < nshell; s++) {
             char type[16];
             int nprim, ngen;
-            H2G_CHECK(std::fscanf(f, "%15s %d %d", type, &nprim, &ngen) == 3, "bad shell header\n");
+            H2G_CHECK(std::fscanf(f, "%15s %d %d", type, &nprim, &ngen) == 3 && nprim >= 1, "bad shell header\n");
             H2G_CHECK(ngen >= 1 && ngen <= (int)std::strlen(type), "bad contraction count\n");
             size_t base = shells.size();
             for (int g = 0; g < ngen; g++) {

@@ -36,3 +36,4 @@ def test_seeded_density_is_projector():
     np.testing.assert_allclose(D, D.T, atol=1e-14)
     np.testing.assert_allclose(D @ D, D, atol=1e-12)
     assert abs(np.trace(D) - 7) < 1e-12
+
