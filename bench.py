@@ -280,6 +280,53 @@ def run_reference_exchange(args):
     h.destroy()
 
 
+def run_setup(args):
+    """--path setup: seconds per host set-up of the workload's molecule
+    (H2ERI_init, CMS_read_mol_file, H2ERI_process_shells, H2ERI_partition,
+    H2ERI_build_H2; OpenMP over the host cores). With --impl reference: the
+    reference's own set-up, compiled from its sources (the integral engine of
+    this package stands in for SIMINT), only where those sources exist."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import h2eri_gb300 as hg
+    from h2eri_gb300 import build as hb, molecules
+    hb.build()
+    mol = os.path.join(tempfile.mkdtemp(), f"alk{WORKLOAD['n_carbon']}.mol")
+    molecules.write_alkane(mol, WORKLOAD["n_carbon"])
+    qr = WORKLOAD["qr_tol"]
+    if args.impl == "reference":
+        from oracle import build_ref
+        if not build_ref.available():
+            print(json.dumps({"impl": "reference", "unavailable": "reference sources absent on this machine, "
+                              "so its set-up cannot be compiled here"}), flush=True)
+            return
+        R = ctypes.CDLL(build_ref.build(verbose=False))
+        R.oref_build.restype = ctypes.c_void_p
+        R.oref_build.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+
+        def one():
+            R.oref_build(mol.encode(), 1e-10, 1e-10, qr, 0)   # the reference struct is not freed
+    else:
+        def one():
+            hg.H2ERI.from_mol(mol, qr_tol=qr).destroy()
+    steps = max(1, min(args.steps, 3))
+    one()                                    # warm-up: library load, Boys table
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        one()
+        times.append(time.perf_counter() - t0)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    out = {"metric": f"host set-up seconds {WORKLOAD['molecule']} (H2ERI_build_H2 and the calls before it)",
+           "value": statistics.median(times), "unit": "s", "higher_is_better": False, "steps": steps,
+           "warmup": 1, "samples_s": [round(t, 3) for t in times], "cores": cores, "dtype": "f64",
+           "data": "synthetic (generated alkane geometry)", "config": dict(WORKLOAD)}
+    if args.impl == "reference":
+        out["impl"] = "reference"
+    print(json.dumps(out), flush=True)
+
+
 def run_gpu_exchange(args):
     """K builds/s: the exchange path (H2ERI_build_exchange) on one GPU."""
     import torch
@@ -647,14 +694,17 @@ def main():
     ap.add_argument("--workload", default="c30", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg (profiler runs)")
     ap.add_argument("--batch-size", type=int, default=8, help="molecules of the uneven batch workload")
-    ap.add_argument("--path", default="coulomb", choices=["coulomb", "exchange"],
-                    help="coulomb: J builds (the headline); exchange: K builds (H2ERI_build_exchange)")
+    ap.add_argument("--path", default="coulomb", choices=["coulomb", "exchange", "setup"],
+                    help="coulomb: J builds (the headline); exchange: K builds (H2ERI_build_exchange); "
+                         "setup: seconds per host set-up (CPU only)")
     args = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[args.workload])
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.path == "setup":
+        run_setup(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
