@@ -19,6 +19,10 @@ all host threads), same workload and metric.
 Multi-GPU (torchrun): one independent replica per GPU (the path does not
 shard: a J build has no exchange step); value = builds of all ranks / max
 time over ranks.
+
+--path exchange: K builds per second (H2ERI_build_exchange). --path setup:
+seconds per host set-up (CPU only; with --impl reference the reference's own
+set-up where its sources exist).
 """
 import argparse
 import ctypes
