@@ -376,10 +376,44 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
     }
 
     memset(acc, 0, sizeof(double) * (size_t)ne * nf);
+    if (M == 1) {
+        /* one p function in the quartet: [p|s] = PA [s|s]^(0) + WP [s|s]^(1)
+         * (or [s|p] = QC [s|s]^(0) + WQ [s|s]^(1)), summed directly */
+        const int bra_p = (La == 1);
+        const double *C0 = bra_p ? bra->A : ket->A;
+        double s0 = 0.0, s1[3] = {0.0, 0.0, 0.0};
+        for (int i = 0; i < bra->nprim; i++) {
+            const double p = bra->p[i], *P = bra->P + 3 * i;
+            const double ip = 1.0 / p;
+            for (int j = 0; j < ket->nprim; j++) {
+                const double q = ket->p[j], *Q = ket->P + 3 * j;
+                const double ipq = 1.0 / (p + q), rho = p * q * ipq;
+                double pq[3], PQ2 = 0.0;
+                for (int d = 0; d < 3; d++) {
+                    pq[d] = P[d] - Q[d];
+                    PQ2 += pq[d] * pq[d];
+                }
+                double F[2];
+                h2g_boys(1, rho * PQ2, F);
+                const double pref = two_pi_52 * bra->K[i] * ip * kq[2 * j + 1] * sqrt(ipq);
+                const double V0 = pref * F[0], V1 = pref * F[1];
+                s0 += V0;
+                if (bra_p) {
+                    const double rp = q * ipq;
+                    for (int d = 0; d < 3; d++) s1[d] += (P[d] - C0[d]) * V0 + (-rp * pq[d]) * V1;
+                } else {
+                    const double rq = p * ipq;
+                    for (int d = 0; d < 3; d++) s1[d] += (Q[d] - C0[d]) * V0 + (rq * pq[d]) * V1;
+                }
+            }
+        }
+        acc[0] = s0;                               /* [s|s]: ne = 4, nf = 1 or ne = 1, nf = 4 */
+        for (int d = 0; d < 3; d++) acc[1 + d] = s1[d];
+    }
     vlane *Vv = vrr_buf(ws, (size_t)ne * nf * nm);
     const int nk = ket->nprim, nq = bra->nprim * nk;
     /* one or two primitive quartets: one at a time (lanes would be idle) */
-    for (int qi = 0; qi < (nq <= 2 ? nq : 0); qi++) {
+    for (int qi = 0; qi < (M > 1 && nq <= 2 ? nq : 0); qi++) {
         double *V = (double *)Vv;
         const int i = qi / nk, j = qi - i * nk;
         const double p = bra->p[i], *P = bra->P + 3 * i;
@@ -404,7 +438,7 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
             for (int f = g_cum[lc]; f < nf; f++) acc[e * nf + f] += V[((size_t)e * nf + f) * nm];
     }
     int ci = 0, cj = 0;   /* (i, j) of primitive quartet q0 */
-    for (int q0 = 0; q0 < (nq <= 2 ? 0 : nq); q0 += H2G_LANES) {
+    for (int q0 = 0; q0 < (M > 1 && nq > 2 ? nq : 0); q0 += H2G_LANES) {
         vlane *V = Vv;
         /* lane l holds primitive quartet q0 + l = (i, j); lanes past the end
          * repeat quartet q0 with a zero prefactor, so they add zeros */
