@@ -118,3 +118,33 @@ def test_eri_contraction_is_sum_of_primitive_quartets(L):
             parts += quartet(L, make_shell(1, cen[0], [aA[i]], [cA[i]], keep), B,
                              make_shell(1, cen[2], [aC[k]], [cC[k]], keep), D)
     np.testing.assert_allclose(full, parts, rtol=1e-12, atol=1e-14 * np.abs(full).max())
+
+
+@pytest.mark.parametrize("side", ["bra", "ket"])
+def test_single_p_quartet_is_centre_derivative(L, side):
+    """(p s|s s) = d/dA (s' s|s s) with s' the s shell of coefficients
+    c_k / (2 a_k) (x - A_x) e^(-a r^2) = (1/2a) d/dA_x e^(-a r^2); likewise on
+    the ket. Central differences (step 1e-4) against the one-p path."""
+    keep = []
+    rng = np.random.default_rng(11)
+    cen = [rng.uniform(-1.2, 1.2, 3) for _ in range(4)]
+    a, c = [3.1, 0.9, 0.31], [0.5, -0.3, 0.7]
+    sp = [ci / (2 * ai) for ai, ci in zip(a, c)]
+    others = [make_shell(0, cen[k], [1.7, 0.45], [0.6, 0.8], keep) for k in range(3)]
+    h = 1e-4
+    for d in range(3):
+        if side == "bra":
+            p_val = quartet(L, make_shell(1, cen[0], a, c, keep), *others)[d, 0, 0, 0]
+        else:
+            p_val = quartet(L, others[0], others[1], make_shell(1, cen[0], a, c, keep), others[2])[0, 0, d, 0]
+        vals = []
+        for sgn in (1, -1):
+            A = np.array(cen[0], dtype=float)
+            A[d] += sgn * h
+            s_shell = make_shell(0, A, a, sp, keep)
+            if side == "bra":
+                vals.append(quartet(L, s_shell, *others)[0, 0, 0, 0])
+            else:
+                vals.append(quartet(L, others[0], others[1], s_shell, others[2])[0, 0, 0, 0])
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(p_val - fd) < 1e-7 * max(abs(p_val), 1e-3), (d, p_val, fd)
