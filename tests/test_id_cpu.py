@@ -74,3 +74,20 @@ def test_id_exact_low_rank_and_zero(L):
     assert np.linalg.norm(A - U @ A[J]) < 1e-12 * np.linalg.norm(A)
     r0, J0, _ = id_rows(L, np.zeros((10, 20)), 1e-8)     # a zero block has rank 0
     assert r0 == 0 and len(J0) == 0
+
+
+def test_id_rows_in_the_span_of_others(L):
+    """Exact rank with rows that are combinations of other rows (they fall
+    below the stop norm as the span fills and leave the per-step work) and
+    rows that are negligible from the start: the rank is the span's, and the
+    coefficients of every non-skeleton row reproduce it."""
+    rng = np.random.default_rng(21)
+    B = graded(rng, 40, 260, 40, 0.8)                     # 40 independent rows, graded
+    M = rng.standard_normal((70, 40)) * 0.3
+    tiny = 1e-14 * rng.standard_normal((20, 260))
+    A = np.vstack([B, M @ B, tiny])[rng.permutation(130)]
+    r, J, U = id_rows(L, A, 1e-10)
+    assert r == 40
+    assert np.linalg.norm(A - U @ A[J]) < 1e-9 * np.linalg.norm(A)
+    r_ref, P = lapack_rank_and_pivots(A, 1e-10)
+    assert r_ref == 40 and len(set(J) & set(P[:r_ref])) >= 38
