@@ -501,7 +501,6 @@ void h2g_potential_points(const h2g_shell *A, const h2g_shell *B, int n_pt, cons
     const int la = A->am, lb = B->am, L = la + lb;
     const int ne = g_cum[L + 1], nm = L + 1, nab = h2g_ncart(la) * h2g_ncart(lb);
     double acc[H2G_NCUM(H2G_MAX_L)];
-    double V[H2G_NCUM(H2G_MAX_L) * (H2G_MAX_L + 1)];
     double work[2 * H2G_NCUM(H2G_MAX_L) * 16];
     double res[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L)];
     const double Av[3] = {A->x, A->y, A->z}, Bv[3] = {B->x, B->y, B->z};
@@ -519,22 +518,33 @@ void h2g_potential_points(const h2g_shell *A, const h2g_shell *B, int n_pt, cons
             for (int d = 0; d < 3; d++) q[2 + d] = (a * Av[d] + b * Bv[d]) / p;
         }
     const double ABv[3] = {Av[0] - Bv[0], Av[1] - Bv[1], Av[2] - Bv[2]};
-    for (int pt = 0; pt < n_pt; pt++) {
-        const double C[3] = {cx[pt], cy[pt], cz[pt]};
-        memset(acc, 0, sizeof(double) * ne);
+    /* H2G_LANES points at a time (lanes past n_pt repeat the last point and
+     * are discarded) */
+    vlane Vl[H2G_NCUM(H2G_MAX_L) * (H2G_MAX_L + 1)], accl[H2G_NCUM(H2G_MAX_L)];
+    for (int pt0 = 0; pt0 < n_pt; pt0 += H2G_LANES) {
+        vlane C[3];
+        for (int l = 0; l < H2G_LANES; l++) {
+            const int pt = (pt0 + l < n_pt) ? pt0 + l : n_pt - 1;
+            C[0][l] = cx[pt];
+            C[1][l] = cy[pt];
+            C[2][l] = cz[pt];
+        }
+        for (int e = 0; e < ne; e++) accl[e] = (vlane){0.0, 0.0, 0.0, 0.0};
         for (int k = 0; k < npp; k++) {
             const double *q = pp + 5 * k;
             const double p = q[0], K = q[1], *P = q + 2;
-            double PA[3], PC[3], PC2 = 0.0;
+            double PA[3];
+            vlane PC[3], PC2 = {0.0, 0.0, 0.0, 0.0};
             for (int d = 0; d < 3; d++) {
                 PA[d] = P[d] - Av[d];
                 PC[d] = P[d] - C[d];
                 PC2 += PC[d] * PC[d];
             }
-            double F[H2G_MAX_L + 1];
-            h2g_boys(L, p * PC2, F);
+            double F[H2G_LANES][H2G_MAX_L + 1];
+            for (int l = 0; l < H2G_LANES; l++) h2g_boys(L, p * PC2[l], F[l]);
             const double pref = -charge * 2.0 * M_PI / p * K;
-            for (int m = 0; m <= L; m++) V[m] = pref * F[m];
+            for (int m = 0; m <= L; m++)
+                for (int l = 0; l < H2G_LANES; l++) Vl[m][l] = pref * F[l][m];
             const double i2p = 0.5 / p;
             /* [e+1_i]^(m) = PA_i [e]^(m) - PC_i [e]^(m+1) + e_i/(2p) ([e-1_i]^(m) - [e-1_i]^(m+1)) */
             for (int c = 1; c < ne; c++) {
@@ -542,15 +552,18 @@ void h2g_potential_points(const h2g_shell *A, const h2g_shell *B, int n_pt, cons
                 const int d = g_dir[c], e = g_prev[c], e2 = g_prev2[c];
                 const double ei = (double)(g_lxyz[c][d] - 1);
                 for (int m = 0; m <= L - Lc; m++) {
-                    double v = PA[d] * V[e * nm + m] - PC[d] * V[e * nm + m + 1];
-                    if (e2 >= 0) v += ei * i2p * (V[e2 * nm + m] - V[e2 * nm + m + 1]);
-                    V[c * nm + m] = v;
+                    vlane v = PA[d] * Vl[e * nm + m] - PC[d] * Vl[e * nm + m + 1];
+                    if (e2 >= 0) v += ei * i2p * (Vl[e2 * nm + m] - Vl[e2 * nm + m + 1]);
+                    Vl[c * nm + m] = v;
                 }
             }
-            for (int e = g_cum[la]; e < ne; e++) acc[e] += V[e * nm];
+            for (int e = g_cum[la]; e < ne; e++) accl[e] += Vl[e * nm];
         }
-        hrr(la, lb, ABv, acc, 1, res, work);
-        for (int r = 0; r < nab; r++) out[(size_t)r * ldo + pt] = res[r];
+        for (int l = 0; l < H2G_LANES && pt0 + l < n_pt; l++) {
+            for (int e = 0; e < ne; e++) acc[e] = accl[e][l];
+            hrr(la, lb, ABv, acc, 1, res, work);
+            for (int r = 0; r < nab; r++) out[(size_t)r * ldo + pt0 + l] = res[r];
+        }
     }
     free(pp);
 }
