@@ -932,7 +932,8 @@ extern "C" void H2ERI_partition(H2ERI_p h)
             *vals = (int *)std::malloc(sizeof(int) * std::max<size_t>(tot, 1));
             (*sidx)[0] = 0;
             for (int i = 0; i < n_node; i++) {
-                std::memcpy(*vals + (*sidx)[i], lists[i].data(), sizeof(int) * lists[i].size());
+                if (!lists[i].empty())
+                    std::memcpy(*vals + (*sidx)[i], lists[i].data(), sizeof(int) * lists[i].size());
                 (*sidx)[i + 1] = (*sidx)[i] + (int)lists[i].size();
             }
         };
