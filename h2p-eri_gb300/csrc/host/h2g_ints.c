@@ -165,7 +165,7 @@ void h2g_pair_init(h2g_pair *pr, const h2g_shell *A, const h2g_shell *B)
     pr->P = (double *)malloc(sizeof(double) * (size_t)np * 3);
     pr->p = (double *)malloc(sizeof(double) * (size_t)np);
     pr->K = (double *)malloc(sizeof(double) * (size_t)np);
-    pr->bexp = (double *)malloc(sizeof(double) * (size_t)np);
+    pr->ip = (double *)malloc(sizeof(double) * (size_t)np);
     double ab2 = 0.0;
     for (int d = 0; d < 3; d++) ab2 += (pr->A[d] - pr->B[d]) * (pr->A[d] - pr->B[d]);
     int n = 0;
@@ -176,7 +176,7 @@ void h2g_pair_init(h2g_pair *pr, const h2g_shell *A, const h2g_shell *B)
             if (fabs(K) < 1e-30) continue;
             pr->p[n] = p;
             pr->K[n] = K;
-            pr->bexp[n] = b;
+            pr->ip[n] = 1.0 / p;
             for (int d = 0; d < 3; d++) pr->P[3 * n + d] = (a * pr->A[d] + b * pr->B[d]) / p;
             n++;
         }
@@ -185,8 +185,8 @@ void h2g_pair_init(h2g_pair *pr, const h2g_shell *A, const h2g_shell *B)
 
 void h2g_pair_free(h2g_pair *pr)
 {
-    free(pr->P); free(pr->p); free(pr->K); free(pr->bexp);
-    pr->P = pr->p = pr->K = pr->bexp = NULL;
+    free(pr->P); free(pr->p); free(pr->K); free(pr->ip);
+    pr->P = pr->p = pr->K = pr->ip = NULL;
     pr->nprim = 0;
 }
 
@@ -254,8 +254,6 @@ typedef struct {
     double acc[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L)];
     double t1[H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L) * 8];
     double w1[2 * H2G_NCUM(H2G_MAX_L) * H2G_NCUM(H2G_MAX_L) * 16];
-    double *kq;       /* per ket primitive pair: 1/q and K/q */
-    int kq_cap;
 } eri_ws;
 
 static __thread eri_ws *tls_ws = NULL;
@@ -266,8 +264,6 @@ static eri_ws *get_ws(void)
         tls_ws = (eri_ws *)malloc(sizeof(eri_ws));
         tls_ws->vrr = NULL;
         tls_ws->vrr_cap = 0;
-        tls_ws->kq = NULL;
-        tls_ws->kq_cap = 0;
     }
     return tls_ws;
 }
@@ -280,22 +276,6 @@ static vlane *vrr_buf(eri_ws *ws, size_t n)
         ws->vrr_cap = n;
     }
     return ws->vrr;
-}
-
-/* 1/q and K/q of every ket primitive pair, in ws->kq[2 j], ws->kq[2 j + 1] */
-static const double *ket_recip(eri_ws *ws, const h2g_pair *ket)
-{
-    if (ws->kq_cap < ket->nprim) {
-        free(ws->kq);
-        ws->kq_cap = ket->nprim < 64 ? 64 : ket->nprim;
-        ws->kq = (double *)malloc(sizeof(double) * 2 * (size_t)ws->kq_cap);
-    }
-    for (int j = 0; j < ket->nprim; j++) {
-        const double iq = 1.0 / ket->p[j];
-        ws->kq[2 * j] = iq;
-        ws->kq[2 * j + 1] = ket->K[j] * iq;
-    }
-    return ws->kq;
 }
 
 /* Obara-Saika vertical recurrences for one batch of primitive quartets, on
@@ -353,11 +333,10 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
     double *acc = ws->acc;
     const double two_pi_52 = 2.0 * pow(M_PI, 2.5);
 
-    /* per primitive quartet: 1/(p+q) is the only division; with 1/p per bra
-     * and 1/q, K/q per ket primitive pair,
+    /* per primitive quartet: 1/(p+q) is the only division; with 1/p and 1/q
+     * stored with the primitive pairs,
      *   rho = p q / (p+q), W - P = q (Q - P) / (p+q), W - Q = p (P - Q) / (p+q),
      *   prefactor 2 pi^(5/2) K_ab K_cd / (p q sqrt(p+q)) */
-    const double *kq = ket_recip(ws, ket);
     if (M == 0) {
         double s = 0.0, F[1];
         for (int i = 0; i < bra->nprim; i++) {
@@ -368,7 +347,7 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
                 const double ipq = 1.0 / (p + q), rho = p * q * ipq;
                 double dx = P[0] - Q[0], dy = P[1] - Q[1], dz = P[2] - Q[2];
                 h2g_boys(0, rho * (dx * dx + dy * dy + dz * dz), F);
-                s += kp * kq[2 * j + 1] * sqrt(ipq) * F[0];
+                s += kp * (ket->K[j] * ket->ip[j]) * sqrt(ipq) * F[0];
             }
         }
         out[0] = s;
@@ -384,7 +363,7 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
         double s0 = 0.0, s1[3] = {0.0, 0.0, 0.0};
         for (int i = 0; i < bra->nprim; i++) {
             const double p = bra->p[i], *P = bra->P + 3 * i;
-            const double ip = 1.0 / p;
+            const double ip = bra->ip[i];
             for (int j = 0; j < ket->nprim; j++) {
                 const double q = ket->p[j], *Q = ket->P + 3 * j;
                 const double ipq = 1.0 / (p + q), rho = p * q * ipq;
@@ -395,7 +374,7 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
                 }
                 double F[2];
                 h2g_boys(1, rho * PQ2, F);
-                const double pref = two_pi_52 * bra->K[i] * ip * kq[2 * j + 1] * sqrt(ipq);
+                const double pref = two_pi_52 * bra->K[i] * ip * (ket->K[j] * ket->ip[j]) * sqrt(ipq);
                 const double V0 = pref * F[0], V1 = pref * F[1];
                 s0 += V0;
                 if (bra_p) {
@@ -418,7 +397,7 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
         const int i = qi / nk, j = qi - i * nk;
         const double p = bra->p[i], *P = bra->P + 3 * i;
         const double q = ket->p[j], *Q = ket->P + 3 * j;
-        const double ipq = 1.0 / (p + q), rho = p * q * ipq, ip = 1.0 / p;
+        const double ipq = 1.0 / (p + q), rho = p * q * ipq, ip = bra->ip[i];
         double PA[3], WP[3], WQ[3], QC[3], PQ2 = 0.0;
         for (int d = 0; d < 3; d++) {
             const double pq_d = P[d] - Q[d];
@@ -428,10 +407,10 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
             QC[d] = Q[d] - ket->A[d];
             PQ2 += pq_d * pq_d;
         }
-        const double i2p = 0.5 * ip, rp = q * ipq, i2q = 0.5 * kq[2 * j], rq = p * ipq, i2pq = 0.5 * ipq;
+        const double i2p = 0.5 * ip, rp = q * ipq, i2q = 0.5 * ket->ip[j], rq = p * ipq, i2pq = 0.5 * ipq;
         double F[H2G_MAX_M + 1];
         h2g_boys(M, rho * PQ2, F);
-        const double pref = two_pi_52 * bra->K[i] * ip * kq[2 * j + 1] * sqrt(ipq);
+        const double pref = two_pi_52 * bra->K[i] * ip * (ket->K[j] * ket->ip[j]) * sqrt(ipq);
         for (int m = 0; m <= M; m++) V[m] = pref * F[m];
         VRR(double);
         for (int e = g_cum[la]; e < ne; e++)
@@ -451,7 +430,7 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
             if (live && ++cj == nk) { cj = 0; ci++; }
             const double p = bra->p[i], *P = bra->P + 3 * i;
             const double q = ket->p[j], *Q = ket->P + 3 * j;
-            const double ipq = 1.0 / (p + q), rho = p * q * ipq, ip = 1.0 / p;
+            const double ipq = 1.0 / (p + q), rho = p * q * ipq, ip = bra->ip[i];
             double PQ2 = 0.0;
             for (int d = 0; d < 3; d++) {
                 const double pq_d = P[d] - Q[d];
@@ -463,11 +442,11 @@ void h2g_eri_quartet(const h2g_pair *bra, const h2g_pair *ket, double *out)
             }
             i2p[l] = 0.5 * ip;
             rp[l] = q * ipq;
-            i2q[l] = 0.5 * kq[2 * j];
+            i2q[l] = 0.5 * ket->ip[j];
             rq[l] = p * ipq;
             i2pq[l] = 0.5 * ipq;
             h2g_boys(M, rho * PQ2, F[l]);
-            pref[l] = live ? two_pi_52 * bra->K[i] * ip * kq[2 * j + 1] * sqrt(ipq) : 0.0;
+            pref[l] = live ? two_pi_52 * bra->K[i] * ip * (ket->K[j] * ket->ip[j]) * sqrt(ipq) : 0.0;
         }
         for (int m = 0; m <= M; m++)
             for (int l = 0; l < H2G_LANES; l++) V[m][l] = pref[l] * F[l][m];

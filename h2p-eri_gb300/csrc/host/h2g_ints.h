@@ -52,7 +52,7 @@ typedef struct h2g_pair_s {
     double *P;           /* [nprim][3] Gaussian product centres */
     double *p;           /* [nprim] exponent sums a + b */
     double *K;           /* [nprim] c_a c_b exp(-a b / p |AB|^2) */
-    double *bexp;        /* [nprim] exponent b (unused by the recurrences, kept for debugging) */
+    double *ip;          /* [nprim] 1 / p */
 } h2g_pair;
 
 /* Build primitive-pair data; primitive pairs whose prefactor magnitude falls

@@ -32,7 +32,7 @@ class ShellT(ctypes.Structure):
 class Pair(ctypes.Structure):
     _fields_ = [("am1", ctypes.c_int), ("am2", ctypes.c_int), ("nprim", ctypes.c_int),
                 ("A", ctypes.c_double * 3), ("B", ctypes.c_double * 3)] + \
-               [(n, ctypes.POINTER(ctypes.c_double)) for n in ("P", "p", "K", "bexp")]
+               [(n, ctypes.POINTER(ctypes.c_double)) for n in ("P", "p", "K", "ip")]
 
 
 def ncart(l):
