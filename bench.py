@@ -3,14 +3,16 @@ the ERI tensor, C30H62 (all-trans zigzag, cc-pVDZ Cartesian, 760 basis
 functions), QR tolerance 1e-8, one seeded density (n_occ = 121).
 
 Default (GPU) arm: the representation is built on the host (set-up, not
-timed), uploaded once, then each step is one J build
-(uncontract -> H2 matvec -> contract) with the density already in HBM. The
-e2e figure times the reference-signature host API (density from host memory,
-build, J to host memory) per step. Precision: mixed (bases and leaf self blocks stored as FP32
-pairs, other blocks as FP32, anchored FP32 accumulation, FP64 output sums)
-when available, else FP64; the FP64 figure is
-always reported beside it, together with the relative error of each against
-the FP64 CPU oracle.
+timed) and uploaded once. One step is a batch of BUILDS_PER_STEP J builds
+(uncontract -> H2 matvec -> contract), one per seeded density, each its own
+single-density call, with the densities already in HBM; the timed region is
+then long enough (about a second) for the clock sampler. The e2e figure
+times the reference's own entry point H2ERI_build_Coulomb on page-locked host
+buffers (density from host memory, J to host memory) for the same builds.
+Precision: mixed (bases and leaf self blocks stored as FP32 pairs, other
+blocks as FP32, anchored FP32 accumulation, FP64 output sums) when
+available, else FP64; the FP64 figure is always reported beside it, together
+with the relative error of each against the FP64 CPU oracle.
 
 --impl reference: the reference's CPU implementation of this path, timed on
 the host cores (the oracle restatement of H2ERI_build_Coulomb, OpenMP over
@@ -65,9 +67,11 @@ WORKLOADS["batch"] = {"workload": "J builds for a batch of alkanes C8..C60 (seed
                       "inputs_vs_L2": "sum of the representations > 129 MB L2"}
 WORKLOAD = dict(WORKLOADS["c30"])
 METRIC = "J builds/s C30H62 (mixed vs FP64) at relerr<=1e-8"
-# DRAM bytes (read + write) of all tile-kernel launches of one mixed C30H62 J
-# build, from one ncu capture (profiles/k_tile_C30H62_mixed_launches_traffic.md)
-TRAFFIC_J_MIXED_C30 = 1707.5e6
+# J builds per step (one single-density call each, distinct seeded densities)
+BUILDS_PER_STEP = 128
+# DRAM traffic of the tile kernels per J build, from an ncu capture of the
+# same workload: key = value lines, read at run time and named in the output
+TRAFFIC_FILE = os.path.join("profiles", "dram_traffic_J_C30H62.txt")
 METRIC_K = "K builds/s (H2ERI_build_exchange path)"
 CACHE_DIR = os.path.join(tempfile.gettempdir(), "h2eri_gb300_cache")
 
@@ -226,6 +230,11 @@ def exchange_cpu_sample(orc, h, D, stride, reps=1):
     return frac / dt, f"{len(shells)} of {nsh} outer shells N (every {stride}-th) in {dt:.1f} s, scaled by {frac:.4f}"
 
 
+def step_densities(molecules, nbf, n, seed0):
+    """The n seeded densities of one step (seeds seed0 .. seed0 + n - 1)."""
+    return np.stack([molecules.seeded_density(nbf, WORKLOAD["n_occ"], seed0 + i) for i in range(n)])
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -237,22 +246,28 @@ def run_reference(args):
     hb.build()
     orc = load_oracle()
     h, _ = representation(hg, molecules, 0, 1, lambda: None)
-    D = molecules.seeded_density(h.num_bf, WORKLOAD["n_occ"], WORKLOAD["seed"])
-    J = np.zeros_like(D)
+    Ds = step_densities(molecules, h.num_bf, BUILDS_PER_STEP, WORKLOAD["seed"])
+    J = np.zeros_like(Ds[0])
+
+    def step():
+        for i in range(BUILDS_PER_STEP):
+            orc.oracle_build_Coulomb(h.handle, Ds[i].ctypes.data, J.ctypes.data)
+
     for _ in range(args.warmup):
-        orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)
+        step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)
+        step()
     dt = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    v = args.steps / dt
+    v = args.steps * BUILDS_PER_STEP / dt
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "J builds/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic (generated alkane geometry, seeded density)", "config": dict(WORKLOAD),
+           "builds_per_step": BUILDS_PER_STEP, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (generated alkane geometry, seeded densities)", "config": dict(WORKLOAD),
            "cpu_baseline": {"value": v, "unit": "J builds/s", "cores": cores, "kind": "port",
-                            "sample": f"{args.steps} J builds of the workload"},
+                            "sample": f"{args.steps} steps of {BUILDS_PER_STEP} J builds (oracle restatement of "
+                                      f"H2ERI_build_Coulomb, OpenMP over {cores} threads)"},
            "e2e": {"value": v, "unit": "J builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     h.destroy()
@@ -516,6 +531,41 @@ def run_gpu_batch(args):
         h.destroy()
 
 
+def fp64_peak_tflops(torch):
+    """Measured FP64 rate of this GPU (cuBLAS DGEMM 4096^3 through torch,
+    best of 5): the denominator of the FP64 path's roofline."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def read_traffic():
+    """DRAM traffic per J build from the committed capture summary (key = value
+    lines), or None."""
+    path = os.path.join(REPO, TRAFFIC_FILE)
+    try:
+        kv = {}
+        with open(path) as f:
+            for ln in f:
+                if "=" in ln and not ln.lstrip().startswith("#"):
+                    k, v = ln.split("=", 1)
+                    kv[k.strip()] = v.strip()
+        return float(kv["traffic_bytes_per_build"]), TRAFFIC_FILE
+    except (OSError, KeyError, ValueError):
+        return None, None
+
+
 def run_gpu(args):
     if args.path == "exchange":
         return run_gpu_exchange(args)
@@ -541,20 +591,20 @@ def run_gpu(args):
     h, setup_s = representation(hg, molecules, rank, ws, barrier)
     L = hg.lib()
     nbf = h.num_bf
-    D = molecules.seeded_density(nbf, WORKLOAD["n_occ"], WORKLOAD["seed"])
+    B = BUILDS_PER_STEP
+    Ds = step_densities(molecules, nbf, B, WORKLOAD["seed"])
     # a dedicated stream: the library enqueues on it and the events below are
     # recorded on it (the legacy default stream would not order with the
     # library's non-blocking streams)
     stream = torch.cuda.Stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
-    dD = torch.tensor(D, device="cuda")
+    dD = torch.tensor(Ds, device="cuda")
     dJ = torch.empty_like(dD)
     torch.cuda.synchronize()
     t_up = time.perf_counter()
     h.upload()
     upload_s = time.perf_counter() - t_up
-    rep = h.report()
-    launches_per_J = int(rep["launches_per_matvec"]) + 2
+    launches_per_J = int(h.report()["launches_per_matvec"]) + 2
 
     modes = [] if args.precision == "mixed" else ["fp64"]
     if args.precision in ("auto", "mixed"):
@@ -563,11 +613,17 @@ def run_gpu(args):
         elif args.precision == "mixed":
             raise RuntimeError(L.H2ERI_gpu_last_error().decode())
 
-    def device_run(mode):
+    def one_step(nden):
+        for i in range(0, B, nden):
+            L.H2ERI_build_Coulomb_device(h.handle, nden, dD[i].data_ptr(), dJ[i].data_ptr(), sp)
+
+    def device_run(mode, nden):
+        """K timed steps of B builds, nden densities per call; ms per step."""
         L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if mode == "mixed" else hg.FP64)
+        if L.H2ERI_build_Coulomb_device(h.handle, nden, dD[0].data_ptr(), dJ[0].data_ptr(), sp) != 0:
+            raise RuntimeError(L.H2ERI_gpu_last_error().decode())
         for _ in range(args.warmup):
-            if L.H2ERI_build_Coulomb_device(h.handle, 1, dD.data_ptr(), dJ.data_ptr(), sp) != 0:
-                raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+            one_step(nden)
         torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
@@ -575,110 +631,133 @@ def run_gpu(args):
         with ClockSampler(local) as clk:
             e0.record(stream)
             for _ in range(args.steps):
-                L.H2ERI_build_Coulomb_device(h.handle, 1, dD.data_ptr(), dJ.data_ptr(), sp)
+                one_step(nden)
             e1.record(stream)
             torch.cuda.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1)
-        return ms, dJ.cpu().numpy(), clk.summary()
+        if L.H2ERI_gpu_check(h.handle) != 0:
+            raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+        return e0.elapsed_time(e1) / args.steps, dJ.cpu().numpy(), clk.summary()
 
     results = {}
     for mode in modes:
-        ms, J, clk = device_run(mode)
+        ms, J, clk = device_run(mode, 1)
         results[mode] = {"ms": ms, "J": J, "clocks": clk}
     best = "mixed" if "mixed" in results else "fp64"
+    n16 = 16
+    ms16, J16, clk16 = device_run(best, n16)
     L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if best == "mixed" else hg.FP64)
 
-    # e2e through the reference-signature host API with pinned host buffers
-    hD = torch.from_numpy(D).pin_memory()
-    hJ = torch.empty_like(hD).pin_memory()
+    # e2e: the reference's own entry point with page-locked host buffers
+    # (density read from and J written to host memory by the kernels)
+    hD = torch.from_numpy(Ds).pin_memory()
+    hJ = torch.zeros(Ds.shape, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        for i in range(B):
+            L.H2ERI_build_Coulomb(h.handle, hD[i].data_ptr(), hJ[i].data_ptr())
+
     for _ in range(args.warmup):
-        L.H2ERI_build_Coulomb_multi(h.handle, 1, hD.data_ptr(), hJ.data_ptr())
+        e2e_step()
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        L.H2ERI_build_Coulomb_multi(h.handle, 1, hD.data_ptr(), hJ.data_ptr())
+        e2e_step()
     e2e_s = time.perf_counter() - t0
     barrier()
-
-    # 16 densities per launch (alpha/beta or stacked SCF trials): one
-    # H2ERI_build_Coulomb_device call builds all 16 J in the best mode
-    n16 = 16
-    D16 = np.stack([molecules.seeded_density(nbf, WORKLOAD["n_occ"], 3000 + i) for i in range(n16)])
-    dD16 = torch.tensor(D16, device="cuda")
-    dJ16 = torch.empty_like(dD16)
-    for _ in range(args.warmup):
-        if L.H2ERI_build_Coulomb_device(h.handle, n16, dD16.data_ptr(), dJ16.data_ptr(), sp) != 0:
-            raise RuntimeError(L.H2ERI_gpu_last_error().decode())
-    torch.cuda.synchronize()
-    steps16 = max(2, args.steps // 10)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(steps16):
-        L.H2ERI_build_Coulomb_device(h.handle, n16, dD16.data_ptr(), dJ16.data_ptr(), sp)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms16 = e0.elapsed_time(e1) / steps16
-    J16 = dJ16.cpu().numpy()
+    Je2e = hJ.numpy().copy()
 
     ms_best = max_over_ranks(results[best]["ms"], dist, "cuda")
     ms_fp64 = max_over_ranks(results["fp64"]["ms"], dist, "cuda") if "fp64" in results else float("nan")
+    ms16 = max_over_ranks(ms16, dist, "cuda")
     e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     if rank != 0:
         barrier()
         return
 
     orc = load_oracle()
+    J_ref = {}
+
+    def oracle_J(i):
+        if i not in J_ref:
+            Jo = np.zeros_like(Ds[i])
+            orc.oracle_build_Coulomb(h.handle, Ds[i].ctypes.data, Jo.ctypes.data)
+            J_ref[i] = Jo
+        return J_ref[i]
+
+    def rel(J, i):
+        return float(np.linalg.norm(J - oracle_J(i)) / np.linalg.norm(oracle_J(i)))
+
+    sample = (0, B - 1)
     if args.skip_cpu:
-        J_ref = np.zeros_like(D)
-        orc.oracle_build_Coulomb(h.handle, D.ctypes.data, J_ref.ctypes.data)
         cpu_v, cpu_n, cpu_dt = None, 0, 0.0
     else:
-        cpu_v, cpu_n, cpu_dt, J_ref = cpu_baseline(orc, h, D)
-    def rel(J):
-        return float(np.linalg.norm(J - J_ref) / np.linalg.norm(J_ref))
+        cpu_v, cpu_n, cpu_dt, _ = cpu_baseline(orc, h, Ds[0])
 
-    def rel16(J, Dk):
-        Jo = np.zeros_like(Dk)
-        orc.oracle_build_Coulomb(h.handle, np.ascontiguousarray(Dk).ctypes.data, Jo.ctypes.data)
-        return float(np.linalg.norm(J - Jo) / np.linalg.norm(Jo))
-
-    step_s = ms_best / 1e3 / args.steps
-    value = replica_value(ws, args.steps, ms_best)
-    alg_bytes = rep["alg_matrix_bytes"] + rep["alg_vector_bytes"] + 2 * 8 * nbf * nbf
-    if best == "mixed":
-        rep_m = h.report()
-        alg_bytes = rep_m["alg_matrix_bytes"] + rep_m["alg_vector_bytes"] + 2 * 8 * nbf * nbf
+    value = replica_value(ws, args.steps * B, args.steps * ms_best)
+    ms_build = ms_best / B
+    rep_best = h.report()
+    alg_bytes = rep_best["alg_matrix_bytes"] + rep_best["alg_vector_bytes"] + 2 * 8 * nbf * nbf
     peak, peak_kind = peaks()
-    achieved = alg_bytes / step_s / 1e9
+    achieved = alg_bytes / (ms_build / 1e3) / 1e9
+    traffic, traffic_src = read_traffic() if (best == "mixed" and WORKLOAD["n_carbon"] == 30) else (None, None)
     clk = results[best]["clocks"]
+
+    fp64 = None
+    if "fp64" in results:
+        L.H2ERI_gpu_set_precision(h.handle, hg.FP64)
+        rep64 = h.report()
+        L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if best == "mixed" else hg.FP64)
+        ms64_build = ms_fp64 / B
+        bytes64 = rep64["alg_matrix_bytes"] + rep64["alg_vector_bytes"] + 2 * 8 * nbf * nbf
+        fpk = fp64_peak_tflops(torch)
+        tf = rep64["alg_flops"] / (ms64_build / 1e3) / 1e12
+        fp64 = {"value": ws * args.steps * B / (ms_fp64 / 1e3 * args.steps), "unit": "J builds/s",
+                "ms_per_step": ms_fp64, "ms_per_build": ms64_build,
+                "relerr_vs_fp64_oracle": max(rel(results["fp64"]["J"][i], i) for i in sample),
+                "roofline": {"bound": "fp64" if fpk * 1e12 / (rep64["alg_flops"] / bytes64) < peak * 1e9 else "hbm",
+                             "achieved": tf, "peak": fpk, "unit": "TFLOP/s", "frac": tf / fpk,
+                             "peak_kind": "measured (cuBLAS DGEMM 4096^3 in this run)",
+                             "alg_flops_per_build": rep64["alg_flops"], "alg_bytes_per_build": bytes64,
+                             "hbm_achieved_gbs": bytes64 / (ms64_build / 1e3) / 1e9,
+                             "hbm_frac": bytes64 / (ms64_build / 1e3) / 1e9 / peak,
+                             "note": "bound = min(HBM, FP64 rate x flops/byte); the FP64 FMA rate binds"},
+                "clocks": {k: results["fp64"]["clocks"][k] for k in ("sm_mhz", "sm_max_mhz", "reasons")}}
+
+    bytes16 = rep_best["alg_matrix_bytes"] + n16 * (rep_best["alg_vector_bytes"] + 2 * 8 * nbf * nbf)
     out = {
         "metric": METRIC, "value": value, "unit": "J builds/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32x2+f64" if best == "mixed" else "f64",
-        "data": "synthetic (generated alkane geometry, seeded density)",
-        "config": dict(WORKLOAD, precision=best, parallelism=f"replicas x{ws}"),
-        "fp64": ({"value": ws * args.steps / (ms_fp64 / 1e3), "unit": "J builds/s",
-                  "ms_per_step": ms_fp64 / args.steps, "relerr_vs_fp64_oracle": rel(results["fp64"]["J"])}
-                 if "fp64" in results else None),
-        "relerr_vs_fp64_oracle": rel(results[best]["J"]),
-        "e2e": {"value": ws * args.steps / e2e_s, "unit": "J builds/s", "h2d_bytes_per_step": 8 * nbf * nbf,
-                "d2h_bytes_per_step": 8 * nbf * nbf},
+        "warmup": args.warmup, "ms_per_step": ms_best, "builds_per_step": B, "ms_per_build": ms_build,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32x2+f64" if best == "mixed" else "f64", "precision": best, "parallelism": f"replicas x{ws}",
+        "data": "synthetic (generated alkane geometry, seeded densities)",
+        "config": dict(WORKLOAD),
+        "fp64": fp64,
+        "relerr_vs_fp64_oracle": max(rel(results[best]["J"][i], i) for i in sample),
+        "relerr_sample": "builds 0 and %d of the step against the FP64 CPU oracle" % (B - 1),
+        "e2e": {"value": ws * args.steps * B / e2e_s, "unit": "J builds/s",
+                "h2d_bytes_per_step": 8 * nbf * nbf * B, "d2h_bytes_per_step": 8 * nbf * nbf * B,
+                "api": "H2ERI_build_Coulomb (reference signature), page-locked host buffers",
+                "relerr_vs_fp64_oracle": max(rel(Je2e[i], i) for i in sample)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": (TRAFFIC_J_MIXED_C30 if best == "mixed" and WORKLOAD["n_carbon"] == 30 else None),
-                     "kernel": "k_tile (all tile launches of one J build)",
-                     "alg_bytes_per_step": alg_bytes, "peak_kind": peak_kind,
-                     "note": "achieved and traffic are per J build (all tile launches); the mixed tile kernels "
-                             "are latency-bound (16 warps per SM, stage barriers), see profiles/"},
+                     "traffic": traffic, "traffic_source": traffic_src,
+                     "kernel": "tile kernels k_tile_mx (all launches of one J build, timed as the step / builds)",
+                     "alg_bytes_per_build": alg_bytes, "peak_kind": peak_kind},
         "cpu_baseline": {"value": cpu_v, "unit": "J builds/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": f"{cpu_n} J builds of the workload in {cpu_dt:.1f} s (oracle, OpenMP)"},
-        "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
-        "gpu_launches": launches_per_J * args.steps,
+        "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"],
+                   "samples": clk["samples"]},
+        "gpu_launches": launches_per_J * B * args.steps,
         "phase_ms_last_host_call": {k: h.report()[k] for k in ("ms_fwd", "ms_mid", "ms_bwd", "ms_den", "ms_total")},
-        "multi_density": {"n_den": n16, "value": n16 / (ms16 / 1e3), "unit": "J builds/s",
-                          "ms_per_launch": ms16, "precision": best,
-                          "relerr_vs_fp64_oracle_max_sampled": max(rel16(J16[i], D16[i]) for i in (0, n16 - 1)),
-                          "sample": "densities 0 and 15 checked against the CPU oracle"},
+        "multi_density": {"n_den": n16, "value": ws * B / (ms16 / 1e3), "unit": "J builds/s",
+                          "ms_per_launch": ms16 * n16 / B, "precision": best,
+                          "relerr_vs_fp64_oracle_max": max(rel(J16[i], i) for i in range(n16)),
+                          "sample": "all 16 densities of the first launch against the CPU oracle",
+                          "roofline": {"bound": "hbm", "achieved": bytes16 / (ms16 * n16 / B / 1e3) / 1e9,
+                                       "peak": peak, "unit": "GB/s",
+                                       "frac": bytes16 / (ms16 * n16 / B / 1e3) / 1e9 / peak,
+                                       "alg_bytes_per_launch": bytes16},
+                          "clocks": {k: clk16[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")}},
         "setup_s": setup_s, "upload_s": upload_s,
     }
     print(json.dumps(out), flush=True)
@@ -689,6 +768,7 @@ def run_gpu(args):
 
 
 def main():
+    global BUILDS_PER_STEP
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -698,12 +778,15 @@ def main():
     ap.add_argument("--workload", default="c30", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg (profiler runs)")
     ap.add_argument("--batch-size", type=int, default=8, help="molecules of the uneven batch workload")
+    ap.add_argument("--builds-per-step", type=int, default=BUILDS_PER_STEP,
+                    help="J builds per step (one density each); smaller for profiler captures")
     ap.add_argument("--path", default="coulomb", choices=["coulomb", "exchange", "setup"],
                     help="coulomb: J builds (the headline); exchange: K builds (H2ERI_build_exchange); "
                          "setup: seconds per host set-up (CPU only)")
     args = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[args.workload])
+    BUILDS_PER_STEP = max(16, args.builds_per_step)
     if args.warmup < 3:
         args.warmup = 3
     if args.path == "setup":

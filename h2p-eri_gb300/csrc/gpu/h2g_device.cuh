@@ -122,6 +122,7 @@ struct DevRep {
     cudaEvent_t ev_t[8] = {nullptr};
     float last_ms[5] = {0, 0, 0, 0, 0};   /* fwd, mid, bwd, den, total */
     int precision = 0;
+    double *noalloc_work = nullptr;   /* device address of the fixed scratch array (matvec without allocation) */
     void *kstate = nullptr;      /* exchange plan and buffers, built on first use */
     double k_work_bytes = 0.0;   /* exchange work-tensor budget, 0 = from free memory */
 };

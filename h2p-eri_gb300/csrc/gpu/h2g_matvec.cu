@@ -4,8 +4,9 @@
  * src/H2ERI_build_Coulomb.c:26-152).
  *
  * Every stored matrix (nested basis U, coupling block B, near-field block D,
- * or one factor of a low-rank B/D) is cut into 64 x 128 tiles. One CTA runs
- * one tile and performs the products the reference does for that block:
+ * or one factor of a low-rank B/D) is cut into tiles of up to kChunkRows (512)
+ * rows by kTileCols (128) columns. One CTA runs one tile (FP64) or two
+ * (mixed formats) and performs the products the reference does for a block:
  *   upward sweep   (src/H2ERI_matvec.c:93-175)   T-product with U
  *   B intermediate (src/H2ERI_matvec.c:299-407)  N and T products (bi-GEMV)
  *   downward sweep (src/H2ERI_matvec.c:663-757)  N-product with U
@@ -717,6 +718,8 @@ __global__ void k_contract(const int *__restrict__ map, int nbf, const double *_
 static std::mutex g_mu;
 static std::unordered_map<const void *, DevRep *> g_reps;
 
+static int noalloc_scratch(int dev, double **out);   /* below, with H2ERI_matvec_device_noalloc */
+
 namespace {
 
 /* Location of one stored matrix in the FP64 arena and in the mixed arena of
@@ -1186,6 +1189,14 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaEventCreateWithFlags(&d->ev_bjoin, cudaEventDisableTiming));
     for (auto &e : d->ev_t) CUDA_TRY(cudaEventCreate(&e));
 
+    /* the address of the fixed scratch array of H2ERI_matvec_device_noalloc
+     * on this device, resolved here so that the allocation-free call itself
+     * only reads it (the lookup may load this module's device code) */
+    {
+        int rc = noalloc_scratch(d->device, &d->noalloc_work);
+        if (rc) return rc;
+    }
+
     d->krnl = krnl;
     d->n_node = n_node;
     d->num_bf = nbf;
@@ -1541,6 +1552,45 @@ extern "C" int H2ERI_gpu_selftest_wait_timeout(long long cycles)
     return rc;
 }
 
+/* The same bounded wait, enqueued on `stream` (NULL = the structure's own
+ * stream) and reporting into the error word of a structure, the way the
+ * mixed-mode tile kernels of the asynchronous entry points report: nothing is
+ * checked here; H2ERI_gpu_check reports it afterwards. */
+extern "C" int H2ERI_gpu_selftest_wait_timeout_async(H2ERI_p h2eri, long long cycles, void *stream)
+{
+    if (cycles < 0) { set_error("cycles < 0"); return 3; }
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : d->s_main;
+    k_wait_probe<<<1, 32, 0, s>>>(d->err_flag_dev, cycles);
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+/* Waits for the structure's own streams and reports what its kernels
+ * recorded since the last check: an expired bounded wait (or a refused
+ * shared-memory layout) in any kernel enqueued by the asynchronous entry
+ * points (the _device variants, H2ERI_matvec_device_noalloc), which return
+ * before their kernels run. Returns 0 when nothing was recorded, 11 (and
+ * sets the message) otherwise; the record is cleared. The caller
+ * synchronises its own stream first. */
+extern "C" int H2ERI_gpu_check(H2ERI_p h2eri)
+{
+    if (h2eri == nullptr) { set_error("null H2ERI handle"); return 1; }
+    DevRep *d = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_reps.find(h2eri);
+        if (it == g_reps.end()) return 0;   /* nothing of it ever ran on the GPU */
+        d = it->second;
+    }
+    CUDA_TRY(cudaStreamSynchronize(d->s_main));
+    CUDA_TRY(cudaStreamSynchronize(d->s_aux));
+    for (int i = 1; i < kNfLanes; i++) CUDA_TRY(cudaStreamSynchronize(d->s_nf[i]));
+    return check_kernel_flag(d);
+}
+
 extern "C" int H2ERI_gpu_upload(H2ERI_p h2eri)
 {
     DevRep *d;
@@ -1723,11 +1773,11 @@ extern "C" int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n)
     for (const Range &r : d->den) launches += r.count > 0;
     for (const Range &r : d->mid) launches += r.count > 0;
     double mbytes = d->precision == H2ERI_GPU_MIXED ? d->alg_bytes_matrix_mixed : d->alg_bytes_matrix;
-    double vals[13] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
+    double vals[14] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
                        (double)d->bytes_U, (double)d->bytes_B, (double)d->bytes_D,
                        d->last_ms[0], d->last_ms[1], d->last_ms[2], d->last_ms[3], d->last_ms[4],
-                       (double)d->precision};
-    int m = std::min(n, 13);
+                       (double)d->precision, (double)(2.0 * d->rank_total + d->lr_total)};
+    int m = std::min(n, 14);
     for (int i = 0; i < m; i++) out[i] = vals[i];
     return m;
 }
@@ -1791,19 +1841,39 @@ static int noalloc_scratch(int dev, double **out)
 
 }  // namespace h2g
 
+/* Scratch limit of the allocation-free matvec: the array's size, or a lower
+ * value from H2G_NOALLOC_LIMIT (doubles), which can only lower it. The lower
+ * limit lets a caller (or a test) see the rejection of an oversized
+ * representation without building one. */
+static size_t noalloc_limit()
+{
+    size_t lim = kNoAllocScratchDoubles;
+    if (const char *e = std::getenv("H2G_NOALLOC_LIMIT")) {
+        char *end = nullptr;
+        const unsigned long long v = std::strtoull(e, &end, 10);
+        if (end != e && *end == '\0' && v < lim) lim = (size_t)v;
+    }
+    return lim;
+}
+
 /* y = A x for one vector on device arrays, without allocating device memory:
  * the representation must already be on the GPU (H2ERI_gpu_upload, or any
  * earlier hot-path call) and the intermediates use the library's fixed
  * scratch array. For callers that must not allocate after set-up: a host
  * application that hands the library a fixed device-memory budget, or one
  * whose memory pool is owned elsewhere, and latency-critical loops where
- * cudaMalloc/cudaFree would synchronise the device. The first call on a
- * device looks up the scratch array's address (see noalloc_scratch); make
- * that first call before any stream capture. */
+ * cudaMalloc/cudaFree would synchronise the device. The scratch array's
+ * device address is looked up when the structure is uploaded, so this call
+ * only reads it. A bounded-wait expiry inside the mixed-mode kernels is
+ * reported by H2ERI_gpu_check after the stream has been synchronised. */
 extern "C" int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, void *stream)
 {
     H2gRange nvtx_range("H2ERI_matvec_device_noalloc");
     if (h2eri == nullptr) { set_error("null H2ERI handle"); return 1; }
+    if (d_x == nullptr || d_y == nullptr) {
+        set_error("H2ERI_matvec_device_noalloc: null input or output vector");
+        return 3;
+    }
     DevRep *d = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_mu);
@@ -1819,10 +1889,10 @@ extern "C" int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, dou
             return 2;
         }
     }
-    const size_t need = (size_t)2 * d->rank_total + d->lr_total;
-    if (need > kNoAllocScratchDoubles) {
+    const size_t need = (size_t)2 * d->rank_total + d->lr_total, limit = noalloc_limit();
+    if (need > limit) {
         set_error("H2ERI_matvec_device_noalloc: needs " + std::to_string(need) + " doubles of scratch, limit " +
-                  std::to_string(kNoAllocScratchDoubles));
+                  std::to_string(limit));
         return 4;
     }
     int dev = -1;
@@ -1831,9 +1901,11 @@ extern "C" int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, dou
         set_error("H2ERI_matvec_device_noalloc: current device differs from the device holding the structure");
         return 5;
     }
-    double *work = nullptr;
-    int rc = noalloc_scratch(dev, &work);
-    if (rc) return rc;
+    double *work = d->noalloc_work;
+    if (work == nullptr) {
+        set_error("H2ERI_matvec_device_noalloc: scratch address not resolved at upload");
+        return 10;
+    }
 
     const size_t per_r = (size_t)d->rank_total;
     VecArgs va;
@@ -1855,7 +1927,7 @@ extern "C" int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, dou
     CUDA_TRY(cudaMemsetAsync(work, 0, need * sizeof(double), sm));      /* scratch keeps the last call's values */
     CUDA_TRY(cudaMemsetAsync(d_y, 0, (size_t)d->krnl * sizeof(double), sm));
     CUDA_TRY(cudaEventRecord(d->ev_zero, sm));
-    rc = launch_near_field(d, va, 1);
+    const int rc = launch_near_field(d, va, 1);
     if (rc) return rc;
     for (const Range &r : d->fwd) launch_range(d, r, va, 1, sm);
     for (const Range &r : d->mid) launch_range(d, r, va, 1, sm);

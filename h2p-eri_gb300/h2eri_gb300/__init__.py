@@ -97,6 +97,8 @@ SIGNATURES = {
     "H2ERI_gpu_set_exchange_memory": (ctypes.c_int, [_vp, ctypes.c_double]),
     "H2ERI_gpu_report": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     "H2ERI_matvec_device_noalloc": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "H2ERI_gpu_check": (ctypes.c_int, [_vp]),
+    "H2ERI_gpu_selftest_wait_timeout_async": (ctypes.c_int, [_vp, ctypes.c_longlong, _vp]),
     "H2ERI_save_representation": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "H2ERI_load_representation": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
 }
@@ -253,7 +255,7 @@ class H2ERI:
         if n < 0:
             _check(-n, "gpu_report")
         keys = ["launches_per_matvec", "alg_matrix_bytes", "alg_vector_bytes", "alg_flops", "arena_U", "arena_B",
-                "arena_D", "ms_fwd", "ms_mid", "ms_bwd", "ms_den", "ms_total", "precision"]
+                "arena_D", "ms_fwd", "ms_mid", "ms_bwd", "ms_den", "ms_total", "precision", "noalloc_scratch_doubles"]
         return dict(zip(keys, out[:n].tolist()))
 
     def print_statistic(self):

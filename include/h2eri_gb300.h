@@ -88,6 +88,20 @@ const char *H2ERI_gpu_last_error(void);
  * CUDA error. The device stays usable afterwards. */
 int H2ERI_gpu_selftest_wait_timeout(long long cycles);
 
+/* The same wait enqueued on a stream (void* cudaStream_t, NULL = the
+ * structure's own), recording its expiry in the structure's error word the
+ * way the kernels of the asynchronous entry points do; returns after
+ * enqueueing (0) and leaves the report to H2ERI_gpu_check. */
+int H2ERI_gpu_selftest_wait_timeout_async(H2ERI_p h2eri, long long cycles, void *stream);
+/* After asynchronous calls (the _device variants and
+ * H2ERI_matvec_device_noalloc return before their kernels run): waits for
+ * the structure's own streams and returns 11, with a message in
+ * H2ERI_gpu_last_error, if any of its kernels gave up a bounded wait (or
+ * found its shared memory misaligned and did nothing) since the last check;
+ * 0 otherwise. The record is cleared. Synchronise the stream passed to the
+ * asynchronous calls first. The host-array calls check by themselves. */
+int H2ERI_gpu_check(H2ERI_p h2eri);
+
 /* y = A x for nvec vectors stored back to back ([nvec][krnl_mat_size]),
  * host arrays. Returns 0 on success. */
 int H2ERI_matvec_multi(H2ERI_p h2eri, int nvec, const double *x, double *y);
@@ -137,10 +151,13 @@ int H2ERI_exchange_plan_check(H2ERI_p h2eri, double device_bytes, double *out, i
  * device). Requires the structure to be on the GPU already
  * (H2ERI_gpu_upload). The intermediates live in one fixed 16 MiB device
  * array shared by all calls; larger representations (2 * sum of ranks +
- * low-rank intermediates > 2^21 doubles) are rejected with an error. Each
- * call clears the array first; calls whose GPU work overlaps race on it. The
- * first call on a device looks up the array's address and should come before
- * any stream capture. Returns 0 on success. */
+ * low-rank intermediates > 2^21 doubles, H2ERI_gpu_report out[13]) are
+ * rejected with an error (status 4; H2G_NOALLOC_LIMIT=<doubles> in the
+ * environment lowers the limit, never raises it). Null vectors are rejected
+ * (status 3). Each call clears the array first; calls whose GPU work
+ * overlaps race on it. The array's device address is looked up when the
+ * structure is uploaded, so the call itself only reads it. Returns 0 after
+ * enqueueing; H2ERI_gpu_check reports a kernel's expired wait afterwards. */
 int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, void *stream);
 
 /* Figures of the device copy, for reports. out[0] kernel launches per matvec
@@ -148,7 +165,8 @@ int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, v
  * out[2] algorithmic vector bytes per vector, out[3] flops per vector,
  * out[4..6] arena bytes of U, B, D, out[7..11] last timed phase durations
  * in ms (upward, coupling, downward, near field, total), out[12] far-field
- * precision mode. Returns the number of values written (<= n), or < 0. */
+ * precision mode, out[13] scratch doubles one matvec of one vector needs.
+ * Returns the number of values written (<= n), or < 0. */
 int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n);
 
 /* Save / load the H2 representation (tree, pair lists, U, B, D and the

@@ -49,3 +49,33 @@ def test_damaged_structure_rejected_before_any_launch(library, tmp_path):
         h.s.mat_cluster[2 * leaf], h.s.mat_cluster[2 * leaf + 1] = r0, r1
     finally:
         h.destroy()
+
+
+def test_async_expiry_reported_by_gpu_check(library, alk26, oracle_lib):
+    """The asynchronous entry points return before their kernels run; a wait
+    that expires inside them is recorded in the structure's error word and
+    reported by H2ERI_gpu_check after the stream is synchronised (then
+    cleared), while a normal asynchronous build leaves nothing to report."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    alk26.upload()
+    s = torch.cuda.Stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    assert library.H2ERI_gpu_check(alk26.handle) == 0
+    assert library.H2ERI_gpu_selftest_wait_timeout_async(alk26.handle, 200_000, sp) == 0
+    s.synchronize()
+    assert library.H2ERI_gpu_check(alk26.handle) == 11
+    assert b"bounded wait" in library.H2ERI_gpu_last_error()
+    assert library.H2ERI_gpu_check(alk26.handle) == 0          # cleared
+    D = hg.molecules.seeded_density(alk26.num_bf, 20, 4322)
+    dD = torch.tensor(D, device="cuda")
+    dJ = torch.empty_like(dD)
+    for mode in (hg.MIXED, hg.FP64):
+        alk26.set_precision(mode)
+        assert library.H2ERI_build_Coulomb_device(alk26.handle, 1, dD.data_ptr(), dJ.data_ptr(), sp) == 0
+        s.synchronize()
+        assert library.H2ERI_gpu_check(alk26.handle) == 0
+    Jo = np.zeros_like(D)
+    oracle_lib.oracle_build_Coulomb(alk26.handle, D.ctypes.data, Jo.ctypes.data)
+    assert relerr(dJ.cpu().numpy(), Jo) < 1e-12
+    assert library.H2ERI_gpu_selftest_wait_timeout_async(alk26.handle, -1, sp) == 3

@@ -94,3 +94,28 @@ def test_oracle_K_matches_golden(alk26, oracle_lib):
     K = np.zeros_like(D)
     oracle_lib.oracle_build_exchange(alk26.handle, D.ctypes.data, K.ctypes.data)
     assert relerr(K, Kg) < 5e-6
+
+
+def test_reference_fixture_loads_and_oracle_reproduces_it(oracle_lib):
+    """The committed fixture made by the reference itself (its own set-up,
+    matvec, J and K on a 40-atom hydrogen chain, tests/golden/
+    make_ref_fixture.py): the representation loads, and the oracle on it
+    reproduces the reference's numbers. The GPU tests compare with the same
+    numbers directly."""
+    h = hg.H2ERI.load(os.path.join(GOLDEN, "ref_h40.h2r"))
+    try:
+        n = h.num_bf
+        x = np.fromfile(os.path.join(GOLDEN, "ref_h40_x.bin"))
+        assert x.size == h.krnl_mat_size
+        y = np.zeros_like(x)
+        oracle_lib.oracle_matvec(h.handle, x.ctypes.data, y.ctypes.data)
+        assert relerr(y, np.fromfile(os.path.join(GOLDEN, "ref_h40_y.bin"))) < 1e-13
+        D = np.fromfile(os.path.join(GOLDEN, "ref_h40_D.bin")).reshape(n, n)
+        J = np.zeros_like(D)
+        K = np.zeros_like(D)
+        oracle_lib.oracle_build_Coulomb(h.handle, D.ctypes.data, J.ctypes.data)
+        oracle_lib.oracle_build_exchange(h.handle, D.ctypes.data, K.ctypes.data)
+        assert relerr(J, np.fromfile(os.path.join(GOLDEN, "ref_h40_J.bin")).reshape(n, n)) < 1e-13
+        assert relerr(K, np.fromfile(os.path.join(GOLDEN, "ref_h40_K.bin")).reshape(n, n)) < 1e-13
+    finally:
+        h.destroy()
