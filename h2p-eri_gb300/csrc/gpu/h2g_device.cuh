@@ -44,6 +44,27 @@ struct Tile {
 };
 static_assert(sizeof(Tile) == 48, "tile descriptor layout");
 
+/* One tile of the multi-density tensor-core kernel: rows [r0, r0 + nr),
+ * columns [c0, c0 + nc) (nr, nc <= 128) of a stored matrix in its mixed
+ * arena (a2: element offset of the tile origin, ld2: leading dimension),
+ * the same optional products as Tile, the tile's power-of-two scale
+ * exponents (128 row and 128 column int8 values at scales + 256 * index),
+ * and the byte offset of its pre-computed bf16 slices in the slice arena
+ * (4 slices x ceil(nc / 64) column blocks x ceil(nr / 8) swizzle atoms of
+ * 1 KB, in that order). */
+struct TileM {
+    uint64_t a2;
+    uint64_t s_off;
+    int32_t ld2;
+    int16_t nr, nc;
+    int32_t in0, out0, in1, out1;
+    uint8_t k_in0, k_out0, k_in1, k_out1;
+    int32_t fmt;
+};
+static_assert(sizeof(TileM) == 48, "multi-density tile descriptor layout");
+constexpr int kMmaRows = 128;      /* rows and columns of a TileM */
+constexpr int kMmaMinVec = 2;      /* densities per launch from which the tensor-core kernel runs */
+
 /* Storage formats of the stored matrices. */
 enum MatFmt : int {
     FMT_F64 = 0,    /* double                                               */
@@ -69,6 +90,14 @@ struct VecArgs {
     double *base[VK_COUNT];
     long long stride[VK_COUNT];
 };
+
+#ifdef __CUDACC__
+/* Element off of vector v of a vector space (device code). */
+__device__ __forceinline__ double *vec_ptr(const VecArgs &va, uint8_t kind, int off, int v)
+{
+    return va.base[kind] + (long long)v * va.stride[kind] + off;
+}
+#endif
 
 struct Range {
     int first = 0, count = 0;
@@ -123,6 +152,18 @@ struct DevRep {
     float last_ms[5] = {0, 0, 0, 0, 0};   /* fwd, mid, bwd, den, total */
     int precision = 0;
     double *noalloc_work = nullptr;   /* device address of the fixed scratch array (matvec without allocation) */
+    /* multi-density tensor-core plan (mixed mode): 128 x 128 tiles with the
+     * same phases as the tile plan, their scale exponents and slices */
+    TileM *mtiles = nullptr;
+    int8_t *mscales = nullptr;
+    unsigned char *mslices = nullptr;
+    size_t mslice_bytes = 0;
+    int n_mtiles = 0;
+    std::vector<TileM> mtiles_host;
+    std::vector<Range> mfwd, mmid, mbwd, mden;
+    int mma_levels = 5;          /* slice levels of the multi-density kernel (4 or 5) */
+    int mma_min_vec = kMmaMinVec;
+    int n_sm = 0;
     void *kstate = nullptr;      /* exchange plan and buffers, built on first use */
     double k_work_bytes = 0.0;   /* exchange work-tensor budget, 0 = from free memory */
 };

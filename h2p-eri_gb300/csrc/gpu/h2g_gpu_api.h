@@ -28,6 +28,10 @@ int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStre
                     bool den_in_host = false);   /* den_in_host: page-locked host memory, read in place */
 /* exchange state attached to a representation */
 void free_exchange_state(DevRep *d);
+/* multi-density tensor-core kernel (h2g_mma.cu) */
+int mma_init(DevRep *d);
+int mma_make_slices(DevRep *d);
+void launch_range_mma(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s);
 /* precision switch (mixed far-field arenas) */
 int set_precision_mode(DevRep *d, H2ERI_p h, int mode);
 

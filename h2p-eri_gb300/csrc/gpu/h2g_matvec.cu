@@ -59,10 +59,6 @@ void set_error(const std::string &msg) { t_last_error = msg; }
 /* Kernels                                                                   */
 /* ======================================================================== */
 
-__device__ __forceinline__ double *vec_ptr(const VecArgs &va, uint8_t kind, int off, int v)
-{
-    return va.base[kind] + (long long)v * va.stride[kind] + off;
-}
 
 /* Column owned by lane `lane` in slot k (0..3) of a 128-column tile strip. */
 template <int FMT>
@@ -728,6 +724,7 @@ struct MatLoc {
     size_t a = 0, a2 = 0;
     int ld = 0, ld2 = 0;
     int map = -1;          /* tensor map of the mixed-arena copy (index of its PackItem) */
+    int fmt = FMT_F32;     /* mixed-arena format */
 };
 
 /* Packs matrices into the FP64 arena now and records where each goes in the
@@ -745,6 +742,7 @@ struct Packer {
     {
         const int sr = trans ? ncol : nrow, sc = trans ? nrow : ncol;   /* stored shape */
         MatLoc m;
+        m.fmt = mixed_fmt;
         m.ld = (sc + 1) & ~1;
         m.a = (host.size() + 3) & ~size_t(3);
         host.resize(m.a + (size_t)sr * m.ld, 0.0);
@@ -771,6 +769,7 @@ struct Packer {
 
 struct Planner {
     std::vector<Tile> tiles;
+    std::vector<TileM> mt;   /* the same products in 128 x 128 tiles (multi-density kernel) */
     void add(const MatLoc &m, int nrow, int ncol, uint8_t kin0, int in0, uint8_t kout0, int out0,
              uint8_t kin1, int in1, uint8_t kout1, int out1)
     {
@@ -788,6 +787,19 @@ struct Planner {
                 if (kout0 != VK_NONE) { t.k_in0 = kin0; t.in0 = in0 + c0; t.k_out0 = kout0; t.out0 = out0 + r0; }
                 if (kout1 != VK_NONE) { t.k_in1 = kin1; t.in1 = in1 + r0; t.k_out1 = kout1; t.out1 = out1 + c0; }
                 tiles.push_back(t);
+            }
+        for (int r0 = 0; r0 < nrow; r0 += kMmaRows)
+            for (int c0 = 0; c0 < ncol; c0 += kMmaRows) {
+                TileM t;
+                std::memset(&t, 0, sizeof(t));
+                t.a2 = m.a2 + (size_t)r0 * m.ld2 + c0;
+                t.ld2 = m.ld2;
+                t.fmt = m.fmt;
+                t.nr = (int16_t)std::min(kMmaRows, nrow - r0);
+                t.nc = (int16_t)std::min(kMmaRows, ncol - c0);
+                if (kout0 != VK_NONE) { t.k_in0 = kin0; t.in0 = in0 + c0; t.k_out0 = kout0; t.out0 = out0 + r0; }
+                if (kout1 != VK_NONE) { t.k_in1 = kin1; t.in1 = in1 + r0; t.k_out1 = kout1; t.out1 = out1 + c0; }
+                mt.push_back(t);
             }
     }
 };
@@ -878,6 +890,9 @@ static void free_rep(DevRep *d)
     cudaFree(d->tmaps);
     if (d->err_flag) cudaFreeHost(d->err_flag);
     cudaFree(d->tiles);
+    cudaFree(d->mtiles);
+    cudaFree(d->mscales);
+    cudaFree(d->mslices);
     cudaFree(d->unc_map);
     cudaFree(d->con_map);
     cudaFree(d->work);
@@ -987,6 +1002,11 @@ static int build_rep(H2ERI_p h, DevRep *d)
     Planner midst[3], dend[3], deno[kNfLanes][3];
     double lane_load[kNfLanes] = {0.0};
     std::vector<Tile> all;
+    std::vector<TileM> mall;
+    d->mfwd.clear();
+    d->mbwd.clear();
+    d->mmid.clear();
+    d->mden.clear();
     double mat_bytes = 0.0, mat_bytes_mixed = 0.0, vec_bytes = 0.0, flops = 0.0;
     d->fwd.clear();
     d->bwd.clear();
@@ -1020,6 +1040,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
         Range r{(int)all.size(), (int)p.tiles.size(), true};
         all.insert(all.end(), p.tiles.begin(), p.tiles.end());
         d->fwd.push_back(r);
+        d->mfwd.push_back(Range{(int)mall.size(), (int)p.mt.size(), true});
+        mall.insert(mall.end(), p.mt.begin(), p.mt.end());
     }
 
     /* coupling blocks (src/H2ERI_matvec.c:299-407) */
@@ -1052,6 +1074,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
     for (int k = 0; k < 3; k++) {
         d->mid.push_back(Range{(int)all.size(), (int)midst[k].tiles.size(), false});
         all.insert(all.end(), midst[k].tiles.begin(), midst[k].tiles.end());
+        d->mmid.push_back(Range{(int)mall.size(), (int)midst[k].mt.size(), false});
+        mall.insert(mall.end(), midst[k].mt.begin(), midst[k].mt.end());
     }
 
     /* downward sweep, shallowest level first (src/H2ERI_matvec.c:679-738) */
@@ -1074,6 +1098,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
         Range r{(int)all.size(), (int)p.tiles.size(), true};
         all.insert(all.end(), p.tiles.begin(), p.tiles.end());
         d->bwd.push_back(r);
+        d->mbwd.push_back(Range{(int)mall.size(), (int)p.mt.size(), true});
+        mall.insert(mall.end(), p.mt.begin(), p.mt.end());
     }
 
     /* near field (src/H2ERI_matvec.c:572-660) */
@@ -1115,6 +1141,8 @@ static int build_rep(H2ERI_p h, DevRep *d)
             Planner &p = ln == 0 ? dend[k] : deno[ln][k];
             d->den.push_back(Range{(int)all.size(), (int)p.tiles.size(), ln == 0, ln});
             all.insert(all.end(), p.tiles.begin(), p.tiles.end());
+            d->mden.push_back(Range{(int)mall.size(), (int)p.mt.size(), ln == 0, ln});
+            mall.insert(mall.end(), p.mt.begin(), p.mt.end());
         }
 
     d->alg_bytes_matrix = mat_bytes;
@@ -1137,6 +1165,19 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaMemcpy(d->arena, pk.host.data(), d->arena_elems * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMalloc(&d->tiles, std::max<size_t>(all.size(), 1) * sizeof(Tile)));
     if (!all.empty()) CUDA_TRY(cudaMemcpy(d->tiles, all.data(), all.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    d->n_mtiles = (int)mall.size();
+    {
+        /* offsets of the tiles' pre-computed slices (1 KB aligned) */
+        size_t off = 0;
+        for (TileM &t : mall) {
+            t.s_off = off;
+            off += (size_t)4 * ((t.nc + 63) / 64) * ((t.nr + 7) / 8) * 1024;
+        }
+        d->mslice_bytes = off;
+    }
+    CUDA_TRY(cudaMalloc(&d->mtiles, std::max<size_t>(mall.size(), 1) * sizeof(TileM)));
+    if (!mall.empty()) CUDA_TRY(cudaMemcpy(d->mtiles, mall.data(), mall.size() * sizeof(TileM), cudaMemcpyHostToDevice));
+    d->mtiles_host = std::move(mall);
 
     /* J assembly maps */
     const int nbf = h->num_bf, num_sp = h->num_sp;
@@ -1169,6 +1210,10 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
     CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
     CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
+    {
+        int rc = mma_init(d);
+        if (rc) return rc;
+    }
     /* The tree sweeps are a chain of dependent launches (the critical path);
      * the near field is one large independent batch. Giving the chain's
      * stream the higher priority lets near-field tiles fill only the SMs the
@@ -1234,6 +1279,10 @@ int get_rep(H2ERI_p h, DevRep **out)
     cudaGetDevice(&d->device);
     int rc = build_rep(h, d);
     if (rc != 0) { free_rep(d); return rc; }
+    /* H2G_MMA_LEVELS=4|5: slice levels of the multi-density kernel;
+     * H2G_MMA_MIN_VEC=n: densities per launch from which it runs (default 2) */
+    if (const char *lv = std::getenv("H2G_MMA_LEVELS")) d->mma_levels = std::atoi(lv) == 4 ? 4 : 5;
+    if (const char *mv = std::getenv("H2G_MMA_MIN_VEC")) d->mma_min_vec = std::max(2, std::atoi(mv));
     /* H2G_PRECISION=mixed starts the structure in the mixed mode, for callers
      * of the reference's entry points that do not call the extensions */
     if (const char *pe = std::getenv("H2G_PRECISION")) {
@@ -1336,6 +1385,63 @@ static int build_tensor_maps(DevRep *d)
     return 0;
 }
 
+/* Power-of-two equilibration of every multi-density tile (from the values
+ * as stored in the mixed arenas): row exponents e_r with max_c |A_rc| <
+ * 2^e_r, then column exponents f_c with max_r |A_rc| 2^-e_r < 2^f_c, so the
+ * scaled tile A_rc 2^-(e_r + f_c) lies in (-1, 1); 128 row then 128 column
+ * int8 values per tile, clamped to [-126, 126] (zero rows and columns get
+ * 0). Each tile is also checked against its arena before upload. */
+static int mma_scales(DevRep *d, const std::vector<float> &h32, const std::vector<float2> &h32x2)
+{
+    const int n = d->n_mtiles;
+    std::vector<int8_t> sc((size_t)std::max(n, 1) * 256, 0);
+    const float *f2 = reinterpret_cast<const float *>(h32x2.data());
+    bool bad = false;
+#pragma omp parallel for schedule(dynamic, 16) reduction(|| : bad)
+    for (int t = 0; t < n; t++) {
+        const TileM &T = d->mtiles_host[t];
+        const bool pair = T.fmt == FMT_F32X2;
+        const size_t lim = pair ? h32x2.size() : h32.size();
+        if (T.nr < 1 || T.nr > kMmaRows || T.nc < 1 || T.nc > kMmaRows || T.ld2 < T.nc ||
+            T.a2 + (size_t)(T.nr - 1) * T.ld2 + (size_t)T.nc > lim) {
+            bad = true;
+            continue;
+        }
+        auto val = [&](int r, int c) -> double {
+            const size_t pos = T.a2 + (size_t)r * T.ld2 + c;
+            if (!pair) return (double)h32[pos];
+            const size_t e = pos & ~size_t(1), k = pos & 1;
+            return (double)f2[2 * e + k] + (double)f2[2 * e + 2 + k];
+        };
+        auto expo = [](double m) -> int {
+            if (!(m > 0.0)) return 0;
+            int ex;
+            std::frexp(m, &ex);   /* m < 2^ex */
+            return std::min(126, std::max(-126, ex));
+        };
+        int8_t *out = sc.data() + (size_t)t * 256;
+        int er[kMmaRows] = {0};
+        for (int r = 0; r < T.nr; r++) {
+            double m = 0.0;
+            for (int c = 0; c < T.nc; c++) m = std::max(m, std::fabs(val(r, c)));
+            er[r] = expo(m);
+            out[r] = (int8_t)er[r];
+        }
+        for (int c = 0; c < T.nc; c++) {
+            double m = 0.0;
+            for (int r = 0; r < T.nr; r++) m = std::max(m, std::ldexp(std::fabs(val(r, c)), -er[r]));
+            out[128 + c] = (int8_t)expo(m);
+        }
+    }
+    if (bad) {
+        set_error("multi-density tile outside its mixed arena (damaged plan)");
+        return 3;
+    }
+    CUDA_TRY(cudaMalloc(&d->mscales, sc.size()));
+    CUDA_TRY(cudaMemcpy(d->mscales, sc.data(), sc.size(), cudaMemcpyHostToDevice));
+    return 0;
+}
+
 /* Fill the mixed arenas from the host blocks (first use of mixed mode). */
 static int pack_mixed(DevRep *d)
 {
@@ -1367,6 +1473,10 @@ static int pack_mixed(DevRep *d)
     CUDA_TRY(cudaMemcpy(d->arena32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMalloc(&d->arena32x2, h32x2.size() * sizeof(float2)));
     CUDA_TRY(cudaMemcpy(d->arena32x2, h32x2.data(), h32x2.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    int rc = mma_scales(d, h32, h32x2);
+    if (rc) return rc;
+    rc = mma_make_slices(d);
+    if (rc) return rc;
     return build_tensor_maps(d);
 }
 
@@ -1386,11 +1496,16 @@ int set_precision_mode(DevRep *d, H2ERI_p h, int mode)
  * low-priority stream, so the few long CTAs at the end of one stage do not
  * leave the others waiting at a launch boundary. All lanes start after
  * ev_zero and are joined into s_aux, which records ev_join. */
-static int launch_near_field(DevRep *d, const VecArgs &va, int nvec, bool timed = false)
+static int launch_near_field(DevRep *d, const VecArgs &va, int nvec, bool timed = false, bool mma = false)
 {
     for (int ln = 1; ln < kNfLanes; ln++) CUDA_TRY(cudaStreamWaitEvent(d->s_nf[ln], d->ev_zero, 0));
     CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_zero, 0));
-    for (const Range &r : d->den) launch_range(d, r, va, nvec, r.lane == 0 ? d->s_aux : d->s_nf[r.lane]);
+    for (size_t i = 0; i < d->den.size(); i++) {
+        const Range &r = d->den[i];
+        cudaStream_t ls = r.lane == 0 ? d->s_aux : d->s_nf[r.lane];
+        if (mma) launch_range_mma(d, d->mden[i], va, nvec, ls);
+        else launch_range(d, r, va, nvec, ls);
+    }
     for (int ln = 1; ln < kNfLanes; ln++) {
         CUDA_TRY(cudaEventRecord(d->ev_nf[ln], d->s_nf[ln]));
         CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_nf[ln], 0));
@@ -1429,14 +1544,21 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     CUDA_TRY(cudaMemsetAsync(y, 0, (size_t)d->krnl * nvec * sizeof(double), sm));
     CUDA_TRY(cudaEventRecord(d->ev_zero, sm));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], sm));
-    rc = launch_near_field(d, va, nvec, timed);
+    /* several densities in the mixed mode: the tensor-core kernel, all
+     * densities (up to 16 per pass) sharing each tile's slices */
+    const bool mma = d->precision == H2ERI_GPU_MIXED && nvec >= d->mma_min_vec && d->mslices != nullptr;
+    auto launch = [&](const Range &r) {
+        if (mma) launch_range_mma(d, r, va, nvec, sm);
+        else launch_range(d, r, va, nvec, sm);
+    };
+    rc = launch_near_field(d, va, nvec, timed, mma);
     if (rc) return rc;
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[0], sm));
-    for (const Range &r : d->fwd) launch_range(d, r, va, nvec, sm);
+    for (const Range &r : (mma ? d->mfwd : d->fwd)) launch(r);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[1], sm));
-    for (const Range &r : d->mid) launch_range(d, r, va, nvec, sm);
+    for (const Range &r : (mma ? d->mmid : d->mid)) launch(r);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[2], sm));
-    for (const Range &r : d->bwd) launch_range(d, r, va, nvec, sm);
+    for (const Range &r : (mma ? d->mbwd : d->bwd)) launch(r);
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[3], sm));
     CUDA_TRY(cudaStreamWaitEvent(sm, d->ev_join, 0));
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[4], sm));

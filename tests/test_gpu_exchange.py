@@ -107,3 +107,31 @@ def test_exchange_mixed_precision(alk26, oracle_lib):
     err = relerr(K32, K64)
     print(f"mixed K relerr vs FP64 oracle: {err:.3e}")
     assert err < TOL_MIXED_K
+
+
+@pytest.mark.slow
+def test_exchange_3d_methane_cluster(library, oracle_lib, tmp_path):
+    """A 3-D system: 8 CH4 on a jittered 2 x 2 x 2 lattice (4.0 A, random
+    orientations; 280 Cartesian bf), QR tolerance 1e-7. Every molecule has
+    neighbours on all sides, so nodes carry far more coupling and near-field
+    work than on a chain. FP64 K against the oracle at 1e-12, mixed K at
+    1e-7."""
+    p = str(tmp_path / "ch4x8.mol")
+    hg.molecules.write_methane_cluster(p, shape=(2, 2, 2))
+    h = hg.H2ERI.from_mol(p, qr_tol=1e-7)
+    try:
+        n = h.num_bf
+        D = hg.molecules.seeded_density(n, 40, 5000)
+        Ko = oracle_K(oracle_lib, h, D)
+        K64 = h.build_exchange(D)
+        h.set_precision(hg.MIXED)
+        try:
+            Km = h.build_exchange(D)
+        finally:
+            h.set_precision(hg.FP64)
+        e64, em = relerr(K64, Ko), relerr(Km, Ko)
+        print(f"(CH4)8 3-D cluster K: FP64 {e64:.2e}, mixed {em:.2e}")
+        assert e64 < TOL_FP64
+        assert em < TOL_MIXED_K
+    finally:
+        h.destroy()

@@ -60,3 +60,26 @@ def test_methane_cluster_geometry():
     assert d[other].min() > 1.2
     syms2, xyz2 = molecules.methane_cluster_coords()
     np.testing.assert_array_equal(xyz, xyz2)
+
+
+def test_methane_cluster_geometry():
+    """48 CH4 on a jittered 4 x 4 x 3 lattice: tetrahedral molecules with
+    C-H 1.09 A, centres within the jitter of their sites, no two atoms of
+    different molecules closer than 1.2 A, reproducible from the seed."""
+    syms, xyz = molecules.methane_cluster_coords()
+    assert syms.count("C") == 48 and syms.count("H") == 192
+    c, h = xyz[:48], xyz[48:].reshape(48, 4, 3)
+    for m in range(48):
+        d = np.linalg.norm(h[m] - c[m], axis=1)
+        np.testing.assert_allclose(d, 1.09, atol=1e-12)
+        u = (h[m] - c[m]) / 1.09
+        g = u @ u.T
+        np.testing.assert_allclose(g[np.triu_indices(4, 1)], -1.0 / 3.0, atol=1e-12)
+    sites = np.array([[i, j, k] for i in range(4) for j in range(4) for k in range(3)], dtype=float) * 4.0
+    assert np.abs(c - sites).max() <= 0.2
+    mol_of = np.arange(48).tolist() + np.repeat(np.arange(48), 4).tolist()
+    d = np.linalg.norm(xyz[:, None, :] - xyz[None, :, :], axis=2)
+    other = np.array(mol_of)[:, None] != np.array(mol_of)[None, :]
+    assert d[other].min() > 1.2
+    syms2, xyz2 = molecules.methane_cluster_coords()
+    np.testing.assert_array_equal(xyz, xyz2)
