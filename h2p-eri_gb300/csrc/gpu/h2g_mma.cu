@@ -222,11 +222,14 @@ struct MmaSmem {
 };
 static_assert(MmaSmem::LAUNCH <= 227 * 1024, "shared memory of the multi-density kernel");
 
-/* Byte offset of vector digit slice j of side (0: N, 1: T) in buffer b,
- * relative to the start of the vector region. */
-__host__ __device__ constexpr uint32_t vslice(int b, int side, int j)
+/* Vector digits of side (0: N, 1: T) in buffer b: K-major bf16 operands
+ * whose rows are (digit j, density v) -> row 16 j + v, so that the digits
+ * j = 0 .. n - 1 of all densities form one operand of 16 n rows. Byte
+ * offset, relative to the vector region, of K block kb (64 entries) of
+ * digit j; the 8-row swizzle atoms of consecutive digits are contiguous. */
+__host__ __device__ constexpr uint32_t vslice(int b, int side, int kb, int j)
 {
-    return (uint32_t)((b * 2 + side) * kSXMax + j) * kSliceV;
+    return (uint32_t)(((b * 2 + side) * 2 + kb) * kSXMax + j) * (kSliceV / 2);
 }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
@@ -482,7 +485,6 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
     } else if (warp == 1) {
         /* ---------------- MMA issue ---------------- */
         if (lane == 0) {
-            constexpr uint32_t idN = umma::idesc_bf16(128, kMV, 0, 0), idT = umma::idesc_bf16(128, kMV, 1, 0);
             const uint64_t dN0 = umma::sdesc(sA, 16, 1024), dT0 = umma::sdesc(sA, 16384, 1024);
             const uint64_t dV0 = umma::sdesc(sV, 16, 1024);
             int committed = 0;
@@ -498,23 +500,23 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
                 for (int i = 0; i < kSA; i++) {
                     if (!wait(full(i), (uint32_t)(k & 1))) { ok = false; break; }
                     umma::fence_after_sync();
-#pragma unroll 1
-                    for (int j = 0; j < SX && i + j < NLEV; j++) {
-                        const int lv = i + j;
-                        const uint64_t bx = dV0 + (vslice(b, 0, j) >> 4), by = dV0 + (vslice(b, 1, j) >> 4);
+                    /* slice i times the digits j = 0 .. NLEV - 1 - i of all
+                     * densities in one MMA of N = 16 (NLEV - i): its columns
+                     * are the accumulators of levels i .. NLEV - 1, in order.
+                     * Every level is first written by slice 0 at K step 0. */
+                    const uint32_t idN = umma::idesc_bf16(128, kMV * (NLEV - i), 0, 0);
+                    const uint32_t idT = umma::idesc_bf16(128, kMV * (NLEV - i), 1, 0);
 #pragma unroll
-                        for (int kk = 0; kk < 8; kk++) {
-                            /* level lv is first written by slice 0 (j = lv), K step 0 */
-                            const bool acc = !(i == 0 && kk == 0);
-                            const uint32_t vk = (uint32_t)((kk >> 2) * 2048 + (kk & 3) * 32) >> 4;
-                            if (opN)
-                                umma::mma_bf16(tb + lv * kMV,
-                                               dN0 + (((uint32_t)i * kSliceA + (kk >> 2) * 16384 + (kk & 3) * 32) >> 4),
-                                               bx + vk, idN, acc);
-                            if (opT)
-                                umma::mma_bf16(tb + (NLEV + lv) * kMV, dT0 + (((uint32_t)i * kSliceA + kk * 2048) >> 4),
-                                               by + vk, idT, acc);
-                        }
+                    for (int kk = 0; kk < 8; kk++) {
+                        const bool acc = !(i == 0 && kk == 0);
+                        const uint32_t vk = (uint32_t)(kk & 3) * 32;
+                        if (opN)
+                            umma::mma_bf16(tb + i * kMV,
+                                           dN0 + (((uint32_t)i * kSliceA + (kk >> 2) * 16384 + (kk & 3) * 32) >> 4),
+                                           dV0 + ((vslice(b, 0, kk >> 2, 0) + vk) >> 4), idN, acc);
+                        if (opT)
+                            umma::mma_bf16(tb + (NLEV + i) * kMV, dT0 + (((uint32_t)i * kSliceA + kk * 2048) >> 4),
+                                           dV0 + ((vslice(b, 1, kk >> 2, 0) + vk) >> 4), idT, acc);
                     }
                     umma::mma_commit(freed(i));   /* slice i may be reloaded once these are done */
                 }
@@ -601,8 +603,8 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
                     const int e = lane + 32 * j;
 #pragma unroll
                     for (int s = 0; s < SX; s++)
-                        *reinterpret_cast<__nv_bfloat16 *>(sm + MmaSmem::OFF_V + vslice(b, side, s) + umma::kmajor_off(v, e, 2048)) =
-                            __float2bfloat16_rn(d[s]);
+                        *reinterpret_cast<__nv_bfloat16 *>(sm + MmaSmem::OFF_V + vslice(b, side, e >> 6, s) +
+                                                           umma::kmajor_off(v, e & 63, 0)) = __float2bfloat16_rn(d[s]);
                 }
             }
             umma::fence_async_smem();
