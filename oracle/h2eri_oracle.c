@@ -27,10 +27,23 @@
 
 #include "h2eri_types.h"
 
-/* y += A x, A row-major nrow x ncol with leading dimension lda */
+/* y += A x, A row-major nrow x ncol with leading dimension lda; two rows
+ * per pass over x */
 static void gemv_n(int nrow, int ncol, const double *A, int lda, const double *x, double *y)
 {
-    for (int i = 0; i < nrow; i++) {
+    int i = 0;
+    for (; i + 1 < nrow; i += 2) {
+        const double *a0 = A + (size_t)i * lda, *a1 = a0 + lda;
+        double s0 = 0.0, s1 = 0.0;
+        #pragma omp simd reduction(+ : s0, s1)
+        for (int j = 0; j < ncol; j++) {
+            s0 += a0[j] * x[j];
+            s1 += a1[j] * x[j];
+        }
+        y[i] += s0;
+        y[i + 1] += s1;
+    }
+    for (; i < nrow; i++) {
         const double *a = A + (size_t)i * lda;
         double s = 0.0;
         #pragma omp simd reduction(+ : s)
@@ -39,10 +52,17 @@ static void gemv_n(int nrow, int ncol, const double *A, int lda, const double *x
     }
 }
 
-/* y += A^T x */
+/* y += A^T x; two rows per pass over y */
 static void gemv_t(int nrow, int ncol, const double *A, int lda, const double *x, double *y)
 {
-    for (int i = 0; i < nrow; i++) {
+    int i = 0;
+    for (; i + 1 < nrow; i += 2) {
+        const double *a0 = A + (size_t)i * lda, *a1 = a0 + lda;
+        const double x0 = x[i], x1 = x[i + 1];
+        #pragma omp simd
+        for (int j = 0; j < ncol; j++) y[j] += x0 * a0[j] + x1 * a1[j];
+    }
+    for (; i < nrow; i++) {
         const double *a = A + (size_t)i * lda;
         const double xi = x[i];
         #pragma omp simd
@@ -50,11 +70,26 @@ static void gemv_t(int nrow, int ncol, const double *A, int lda, const double *x
     }
 }
 
-/* out0 += A in0 and out1 += A^T in1 with one pass over A */
+/* out0 += A in0 and out1 += A^T in1 with one pass over A, two rows at a
+ * time (the reference's CBLAS_BI_GEMV, src/H2ERI_matvec.c:24-63) */
 static void bi_gemv(int nrow, int ncol, const double *A, int lda, const double *in0, const double *in1,
                     double *out0, double *out1)
 {
-    for (int i = 0; i < nrow; i++) {
+    int i = 0;
+    for (; i + 1 < nrow; i += 2) {
+        const double *a0 = A + (size_t)i * lda, *a1 = a0 + lda;
+        const double x0 = in1[i], x1 = in1[i + 1];
+        double s0 = 0.0, s1 = 0.0;
+        #pragma omp simd reduction(+ : s0, s1)
+        for (int j = 0; j < ncol; j++) {
+            s0 += a0[j] * in0[j];
+            s1 += a1[j] * in0[j];
+            out1[j] += x0 * a0[j] + x1 * a1[j];
+        }
+        out0[i] += s0;
+        out0[i + 1] += s1;
+    }
+    for (; i < nrow; i++) {
         const double *a = A + (size_t)i * lda;
         const double x1 = in1[i];
         double s = 0.0;
