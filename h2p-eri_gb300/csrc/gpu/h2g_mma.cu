@@ -195,9 +195,10 @@ namespace h2g {
  *   warp 1   issues the MMAs, slice by slice as the copies land, into one of
  *            two tensor-memory buffers, then commits (mmadone[b]);
  *   warps 2-15 turn the densities' vector entries into digits (two
- *            shared-memory buffers, vfull[b]) and run the epilogue of the
- *            previous tile (warps 4-11: tensor-memory loads, tempty[b],
- *            level combination, FP64 atomics).
+ *            shared-memory buffers, vfull[b]), every load of a tile issued
+ *            before the first is used; warps 4-11 then run the epilogue of
+ *            the previous tile (tensor-memory loads, tempty[b], level
+ *            combination, FP64 atomics) while the next tiles are in flight.
  * Every wait is bounded (about a second); on expiry the kernel records it
  * in the error word, skips the remaining work, waits once more (bounded)
  * for copies and MMAs in flight and frees its tensor memory.
@@ -209,8 +210,9 @@ constexpr int kSXMax = 5;                 /* largest number of vector digits  */
 constexpr uint32_t kSliceA = 32768;       /* one 128 x 128 bf16 slice         */
 constexpr uint32_t kSliceV = 4096;        /* one 16 x 128 bf16 vector slice   */
 constexpr uint32_t kTmemCols = 512;
-constexpr int kNWorkers = 14;             /* warps 2..15                      */
-constexpr int kEpiWarps = 8;              /* warps 4..11                      */
+constexpr int kNWorkers = 14;             /* digit warps 2..15                */
+constexpr int kEpiWarps = 8;              /* epilogue warps 4..11             */
+constexpr int kPairsPerWorker = (2 * 16 + kNWorkers - 1) / kNWorkers;   /* (side, density) pairs */
 
 struct MmaSmem {
     static constexpr uint32_t OFF_V = kSA * kSliceA;                          /* [2][side][kSXMax] slices */
@@ -276,30 +278,34 @@ __device__ __forceinline__ int pow2_exp(unsigned long long mx)
 }
 
 /* The SX signed 8-bit digits of x / 2^E (|x| <= 2^E), most significant
- * first: x / 2^E ~ sum_j d_j 2^-8(j+1), |d_0| <= 256, |d_j| <= 128 after. */
+ * first: x / 2^E ~ sum_j d_j 2^-8(j+1), |d_0| <= 256, |d_j| <= 128 after
+ * that, from the signed fixed-point value
+ * q = round(x 2^(8 SX - E)) in 64 bits, biased by 128 in every digit below
+ * the top so that the balanced digits d_j in [-128, 127] (j >= 1) are the
+ * plain bytes of q + bias minus 128, and the top digit is what remains
+ * above them (|d_0| <= 256). Bytes become floats through the exponent
+ * field (2^23 + byte is exact), without conversion instructions. */
 template <int SX>
 __device__ __forceinline__ void dbl_digits(long long bits, int E, float (&d)[SX])
 {
     const unsigned long long a = (unsigned long long)bits & 0x7FFFFFFFFFFFFFFFull;
     const int ex = (int)(a >> 52);
-    unsigned long long q = 0;
+    long long q = 0;
     if (ex != 0) {
         const unsigned long long m = (a & 0xFFFFFFFFFFFFFull) | (1ull << 52);
         const int sh = 1075 + E - 8 * SX - ex;   /* >= 52 - 8 SX > 0 */
-        if (sh < 64) q = (m + (1ull << (sh - 1))) >> sh;
+        if (sh < 64) q = (long long)((m + (1ull << (sh - 1))) >> sh);
+        if (bits < 0) q = -q;
     }
-    int dig[SX];
+    constexpr unsigned long long bias = 0x8080808080808080ull >> (8 * (9 - SX));   /* 128 in bytes 0 .. SX - 2 */
+    const long long qb = q + (long long)bias;
 #pragma unroll
-    for (int j = SX - 1; j > 0; j--) {
-        int v = (int)(q & 255u);
-        q >>= 8;
-        if (v >= 128) { v -= 256; q += 1; }
-        dig[j] = v;
+    for (int j = 1; j < SX; j++) {
+        const unsigned byte = (unsigned)(qb >> (8 * (SX - 1 - j))) & 255u;
+        d[j] = __int_as_float(0x4B000000 | byte) - 8388736.0f;   /* 2^23 + 128 */
     }
-    dig[0] = (int)q;
-    const bool neg = bits < 0;
-#pragma unroll
-    for (int j = 0; j < SX; j++) d[j] = (float)(neg ? -dig[j] : dig[j]);
+    const int top = (int)(qb >> (8 * (SX - 1)));                   /* in [-256, 256] */
+    d[0] = __int_as_float(0x4B000000 + (top + 256)) - 8388864.0f;  /* 2^23 + 256 */
 }
 
 /* I * 2^e2 as a double, built with integer operations (the FP64 pipe of
@@ -529,16 +535,18 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
         }
     } else {
         /* ---------------- vector digits and epilogue ---------------- */
-        const int wk = warp - 2;
         const bool epi = warp >= 4 && warp < 4 + kEpiWarps;
+        const int wk = warp - 2;                            /* 0 .. kNWorkers - 1 */
+        const int side = (warp - 4) >> 2, q = warp & 3;    /* epilogue warps */
+        const int idx = 32 * q + lane;                      /* row (N) or column (T) of the tile */
         auto epilogue = [&](int k) {
             const int t = blockIdx.x + k * gridDim.x;
             const TileM T = tiles[t];
-            const int side = (warp - 4) >> 2, q = warp & 3, b = k & 1;
+            const int b = k & 1;
             const bool on = side == 0 ? T.k_out0 != VK_NONE : T.k_out1 != VK_NONE;
+            const int e_sc = scales[(size_t)t * 256 + side * 128 + idx];
             if (!wait(mmadone(b), (uint32_t)((k >> 1) & 1))) return;
             umma::fence_after_sync();
-            const int idx = 32 * q + lane;                  /* row (N) or column (T) of the tile */
             const int lim = side == 0 ? T.nr : T.nc;
             uint32_t acc[2][NLEV][8];
 #pragma unroll
@@ -549,7 +557,6 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
             __syncwarp();
             if (lane == 0) mbar_arrive(tempty(b));        /* the MMAs of tile k + 2 may overwrite the buffer */
             if (!on || idx >= lim) return;
-            const int e_sc = scales[(size_t)t * 256 + side * 128 + idx];
             double *outb = side == 0 ? vec_ptr(va, T.k_out0, T.out0, 0) : vec_ptr(va, T.k_out1, T.out1, 0);
             const long long ostride = va.stride[side == 0 ? T.k_out0 : T.k_out1];
             const int *mu = smu + (k & 3) * 32 + side * 16;
@@ -567,53 +574,67 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
                     atomicAdd(outb + (long long)(vg + v) * ostride + idx, i64_ldexp(I, e_sc + mu[v] - 8 * NLEV - 8));
                 }
         };
-        for (int k = 0; k < nk; k++) {
-            const int t = blockIdx.x + k * gridDim.x;
-            const TileM T = tiles[t];
-            const int b = k & 1;
-            /* digits of tile k into vector buffer b, once the MMAs of tile k - 2 that read it are done */
-            if (k >= 2 && !wait(mmadone(b), (uint32_t)(((k - 2) >> 1) & 1))) break;
-            for (int p = wk; p < 2 * kMV; p += kNWorkers) {
-                const int side = p >> 4, v = p & 15;
-                const bool on = side == 0 ? T.k_out0 != VK_NONE : T.k_out1 != VK_NONE;
-                if (!on) continue;
-                const int lim = side == 0 ? T.nc : T.nr;
-                long long xb[4];
-                unsigned long long mx = 0;
+        {
+            const int e0 = 4 * lane;                            /* this lane's 4 entries */
+            for (int k = 0; k < nk; k++) {
+                const int t = blockIdx.x + k * gridDim.x;
+                const TileM T = tiles[t];
+                const int b = k & 1;
+                /* every entry of this warp's (side, density) pairs, scaled by
+                 * the tile's exponents (N side: x_c 2^f_c; T side: y_r 2^e_r),
+                 * loaded before any is used */
+                long long xb[kPairsPerWorker][4];
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const int e = lane + 32 * j;
-                    xb[j] = 0;
-                    if (v < nv && e < lim) {
-                        const double *src = side == 0 ? vec_ptr(va, T.k_in0, T.in0, vg + v) : vec_ptr(va, T.k_in1, T.in1, vg + v);
-                        /* N side: x_c 2^f_c; T side: y_r 2^e_r */
-                        xb[j] = dbl_scale_bits(__double_as_longlong(src[e]),
-                                               scales[(size_t)t * 256 + (side == 0 ? 128 : 0) + e]);
+                for (int pp = 0; pp < kPairsPerWorker; pp++) {
+                    const int p = wk + pp * kNWorkers;
+                    const int side = p >> 4, v = p & 15;
+                    const bool on = p < 2 * kMV && (side == 0 ? T.k_out0 != VK_NONE : T.k_out1 != VK_NONE) && v < nv;
+                    const int lim = side == 0 ? T.nc : T.nr;
+                    const double *src = on ? (side == 0 ? vec_ptr(va, T.k_in0, T.in0, vg + v) : vec_ptr(va, T.k_in1, T.in1, vg + v))
+                                           : nullptr;
+                    const char4 ex = *reinterpret_cast<const char4 *>(scales + (size_t)t * 256 + (side == 0 ? 128 : 0) + e0);
+                    const int exs[4] = {ex.x, ex.y, ex.z, ex.w};
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        xb[pp][u] = 0;
+                        if (on && e0 + u < lim) xb[pp][u] = dbl_scale_bits(__double_as_longlong(src[e0 + u]), exs[u]);
                     }
-                    mx = max(mx, (unsigned long long)xb[j] & 0x7FFFFFFFFFFFFFFFull);
                 }
+                /* the buffer is free once the MMAs of tile k - 2 that read it are done */
+                if (k >= 2 && !wait(mmadone(b), (uint32_t)(((k - 2) >> 1) & 1))) break;
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-                const int E = pow2_exp(mx);
-                if (lane == 0) smu[(k & 3) * 32 + side * 16 + v] = E;
+                for (int pp = 0; pp < kPairsPerWorker; pp++) {
+                    const int p = wk + pp * kNWorkers;
+                    if (p >= 2 * kMV) break;
+                    const int side = p >> 4, v = p & 15;
+                    if (!(side == 0 ? T.k_out0 != VK_NONE : T.k_out1 != VK_NONE)) continue;
+                    unsigned long long mx = 0;
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    float d[SX];
-                    dbl_digits<SX>(xb[j], E, d);
-                    const int e = lane + 32 * j;
+                    for (int u = 0; u < 4; u++) mx = max(mx, (unsigned long long)xb[pp][u] & 0x7FFFFFFFFFFFFFFFull);
 #pragma unroll
-                    for (int s = 0; s < SX; s++)
-                        *reinterpret_cast<__nv_bfloat16 *>(sm + MmaSmem::OFF_V + vslice(b, side, e >> 6, s) +
-                                                           umma::kmajor_off(v, e & 63, 0)) = __float2bfloat16_rn(d[s]);
+                    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                    const int E = pow2_exp(mx);
+                    if (lane == 0) smu[(k & 3) * 32 + side * 16 + v] = E;
+                    float d[4][SX];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) dbl_digits<SX>(xb[pp][u], E, d[u]);
+                    unsigned char *dst = sm + MmaSmem::OFF_V + umma::kmajor_off(v, e0 & 63, 0);
+#pragma unroll
+                    for (int sl = 0; sl < SX; sl++) {
+                        __nv_bfloat162 p0 = __floats2bfloat162_rn(d[0][sl], d[1][sl]);
+                        __nv_bfloat162 p1 = __floats2bfloat162_rn(d[2][sl], d[3][sl]);
+                        *reinterpret_cast<uint2 *>(dst + vslice(b, side, e0 >> 6, sl)) =
+                            make_uint2(*reinterpret_cast<uint32_t *>(&p0), *reinterpret_cast<uint32_t *>(&p1));
+                    }
                 }
+                umma::fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(vfull(b));
+                if (epi && k >= 1) epilogue(k - 1);
+                if (*dead) break;
             }
-            umma::fence_async_smem();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(vfull(b));
-            if (epi && k >= 1) epilogue(k - 1);
-            if (*dead) break;
+            if (epi && nk >= 1 && !*dead) epilogue(nk - 1);
         }
-        if (epi && nk >= 1 && !*dead) epilogue(nk - 1);
     }
     umma::fence_before_sync();
     __syncthreads();
