@@ -49,9 +49,10 @@ static_assert(sizeof(Tile) == 48, "tile descriptor layout");
  * arena (a2: element offset of the tile origin, ld2: leading dimension),
  * the same optional products as Tile, the tile's power-of-two scale
  * exponents (128 row and 128 column int8 values at scales + 256 * index),
- * and the byte offset of its pre-computed bf16 slices in the slice arena
+ * the byte offset of its pre-computed bf16 slices in the slice arena
  * (4 slices x ceil(nc / 64) column blocks x ceil(nr / 8) swizzle atoms of
- * 1 KB, in that order). */
+ * 1 KB, in that order; in a batch plan, the slices' device address), and
+ * in a batch plan the index of the structure whose vectors it uses. */
 struct TileM {
     uint64_t a2;
     uint64_t s_off;
@@ -60,8 +61,10 @@ struct TileM {
     int32_t in0, out0, in1, out1;
     uint8_t k_in0, k_out0, k_in1, k_out1;
     int32_t fmt;
+    int32_t mol;
+    int32_t pad_;
 };
-static_assert(sizeof(TileM) == 48, "multi-density tile descriptor layout");
+static_assert(sizeof(TileM) == 56, "multi-density tile descriptor layout");
 constexpr int kMmaRows = 128;      /* rows and columns of a TileM */
 constexpr int kMmaMinVec = 2;      /* densities per launch from which the tensor-core kernel runs */
 
@@ -98,6 +101,14 @@ __device__ __forceinline__ double *vec_ptr(const VecArgs &va, uint8_t kind, int 
     return va.base[kind] + (long long)v * va.stride[kind] + off;
 }
 #endif
+
+/* One structure of a batch plan: its vector spaces and its number of
+ * densities. */
+struct BatchMol {
+    VecArgs va;
+    int nvec;
+    int pad_;
+};
 
 struct Range {
     int first = 0, count = 0;

@@ -28,10 +28,21 @@ int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStre
                     bool den_in_host = false);   /* den_in_host: page-locked host memory, read in place */
 /* exchange state attached to a representation */
 void free_exchange_state(DevRep *d);
+int ensure_work(DevRep *d, int nvec);
+int enqueue_uncontract(DevRep *d, int n_den, const double *den, cudaStream_t s);
+int enqueue_contract(DevRep *d, int n_den, double *J, cudaStream_t s);
+/* batched J over several structures in shared launches (h2g_batch.cu) */
+bool batch_merged_eligible(int n, DevRep *const *reps, const int *n_den);
+int batch_coulomb_merged(int n, DevRep *const *reps, const int *n_den, const double *const *d_dens,
+                         double *const *d_Js, cudaStream_t s);
+void batch_forget(const DevRep *d);
 /* multi-density tensor-core kernel (h2g_mma.cu) */
 int mma_init(DevRep *d);
 int mma_make_slices(DevRep *d);
 void launch_range_mma(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s);
+/* a range of a batch plan: tiles, their scales and the structures' table */
+void launch_batch_mma(const TileM *tiles, const int8_t *scales, const BatchMol *mols, int count, int levels, int n_sm,
+                      unsigned *err, cudaStream_t s);
 /* precision switch (mixed far-field arenas) */
 int set_precision_mode(DevRep *d, H2ERI_p h, int mode);
 

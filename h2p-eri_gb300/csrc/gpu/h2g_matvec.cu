@@ -915,6 +915,7 @@ static void free_rep(DevRep *d)
     for (auto &e : d->ev_t)
         if (e) cudaEventDestroy(e);
     free_exchange_state(d);
+    batch_forget(d);
     if (cur >= 0) cudaSetDevice(cur);
     delete d;
 }
@@ -1300,7 +1301,7 @@ int get_rep(H2ERI_p h, DevRep **out)
     return 0;
 }
 
-static int ensure_work(DevRep *d, int nvec)
+int ensure_work(DevRep *d, int nvec)
 {
     if (nvec <= d->nvec_cap) return 0;
     cudaFree(d->work);
@@ -1613,6 +1614,27 @@ static int ensure_den(DevRep *d, int n_den)
     return 0;
 }
 
+/* x = uncontracted densities (device arrays) into the structure's x buffer,
+ * and J from its y buffer: the J-assembly launches of enqueue_coulomb, for
+ * the merged batch path. */
+int enqueue_uncontract(DevRep *d, int n_den, const double *den, cudaStream_t s)
+{
+    const long long n2 = (long long)d->num_bf * d->num_bf;
+    dim3 g1((d->krnl + 255) / 256 < 4096 ? (d->krnl + 255) / 256 : 4096, n_den);
+    k_uncontract<<<g1, 256, 0, s>>>(d->unc_map, d->krnl, den, n2, d->xbuf, d->krnl);
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+int enqueue_contract(DevRep *d, int n_den, double *J, cudaStream_t s)
+{
+    const long long n2 = (long long)d->num_bf * d->num_bf;
+    long long nb = (n2 + 255) / 256;
+    dim3 g2((unsigned)std::min<long long>(nb, 8192), n_den);
+    k_contract<<<g2, 256, 0, s>>>(d->con_map, d->num_bf, d->ybuf, d->krnl, J, n2);
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
 int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStream_t s, bool timed,
                     bool den_in_host)
 {
@@ -1789,10 +1811,13 @@ extern "C" int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double
     return enqueue_coulomb(d, n_den, d_den, d_J, s, false);
 }
 
-/* J for several structures at once. Every structure's build runs on its
- * own pair of streams, forked from `stream` and joined back to it, so the
- * builds of small and large molecules overlap on the GPU. All device
- * buffers are set up before anything is enqueued. */
+/* J for several structures at once. In the mixed mode (every structure
+ * with at most 16 densities) the H2 products of all structures run in
+ * shared launches of the tensor-core kernel, one per phase (h2g_batch.cu).
+ * Otherwise every structure's build runs on its own pair of streams, forked
+ * from `stream` and joined back to it, so the builds of small and large
+ * molecules overlap on the GPU. All device buffers are set up before
+ * anything is enqueued. */
 extern "C" int H2ERI_build_Coulomb_batch(int n, H2ERI_p *h2eris, const int *n_den, const double *const *d_dens,
                                          double *const *d_Js, void *stream)
 {
@@ -1815,6 +1840,9 @@ extern "C" int H2ERI_build_Coulomb_batch(int n, H2ERI_p *h2eris, const int *n_de
         if (rc) return rc;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    /* mixed mode with at most 16 densities per structure: every structure's
+     * tiles in shared tensor-core launches, phase by phase */
+    if (batch_merged_eligible(n, reps.data(), n_den)) return batch_coulomb_merged(n, reps.data(), n_den, d_dens, d_Js, s);
     for (int i = 0; i < n; i++) {
         DevRep *d = reps[i];
         CUDA_TRY(cudaEventRecord(d->ev_bfork, s));

@@ -412,9 +412,15 @@ __global__ void __launch_bounds__(256) k_make_slices(const TileM *__restrict__ t
 
 template <int NLEV>
 __global__ void __launch_bounds__(kMT, 1)
-k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__ VecArgs va, int nvec,
-           const unsigned char *__restrict__ slices, const int8_t *__restrict__ scales, unsigned *err)
+k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__ VecArgs va0, int nvec0,
+           const unsigned char *__restrict__ slices, const int8_t *__restrict__ scales, unsigned *err,
+           const BatchMol *__restrict__ mols)
 {
+    /* one structure: va0 / nvec0 and slice offsets into `slices`; a batch
+     * (mols != nullptr): every tile names its structure, and its slice
+     * offset is the slices' device address (slices is null) */
+    auto tva = [&](const TileM &T) -> const VecArgs & { return mols ? mols[T.mol].va : va0; };
+    auto tnv = [&](const TileM &T) { return min(kMV, (mols ? mols[T.mol].nvec : nvec0) - (int)blockIdx.y * kMV); };
     constexpr int SX = NLEV;                     /* vector digits */
     constexpr int TPB = 2 * NLEV * kMV;          /* TMEM columns per buffer */
     static_assert(SX <= kSXMax && 2 * TPB <= (int)kTmemCols, "layout");
@@ -433,7 +439,6 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int vg = blockIdx.y * kMV;
-    const int nv = min(kMV, nvec - vg);
     const int nk = (n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;   /* tiles of this CTA */
 
     /* the slice buffer starts zeroed: rows and columns that a partial tile
@@ -478,8 +483,10 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
                     if (k > 0 && !wait(freed(i), (uint32_t)((k - 1) & 1))) { ok = false; break; }
                     mbar_expect_tx(full(i), chunk * nb);
                     for (int b = 0; b < nb; b++)
-                        bulk_g2s(sA + i * kSliceA + b * 16384, slices + T.s_off + ((size_t)i * nb + b) * chunk, chunk,
-                                 full(i));
+                        bulk_g2s(sA + i * kSliceA + b * 16384,
+                                 reinterpret_cast<const unsigned char *>((uintptr_t)slices + T.s_off) +
+                                     ((size_t)i * nb + b) * chunk,
+                                 chunk, full(i));
                 }
                 if (!ok) break;
                 issued = k + 1;
@@ -545,6 +552,8 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
             const int b = k & 1;
             const bool on = side == 0 ? T.k_out0 != VK_NONE : T.k_out1 != VK_NONE;
             const int e_sc = scales[(size_t)t * 256 + side * 128 + idx];
+            const VecArgs &va = tva(T);
+            const int nv = tnv(T);
             if (!wait(mmadone(b), (uint32_t)((k >> 1) & 1))) return;
             umma::fence_after_sync();
             const int lim = side == 0 ? T.nr : T.nc;
@@ -580,6 +589,8 @@ k_tile_mma(const TileM *__restrict__ tiles, int n_tiles, const __grid_constant__
                 const int t = blockIdx.x + k * gridDim.x;
                 const TileM T = tiles[t];
                 const int b = k & 1;
+                const VecArgs &va = tva(T);
+                const int nv = tnv(T);
                 /* every entry of this warp's (side, density) pairs, scaled by
                  * the tile's exponents (N side: x_c 2^f_c; T side: y_r 2^e_r),
                  * loaded before any is used */
@@ -692,9 +703,24 @@ void launch_range_mma(const DevRep *d, const Range &r, const VecArgs &va, int nv
     const int8_t *sc = d->mscales + (size_t)r.first * 256;
     const int launch = (int)MmaSmem::LAUNCH;
     if (d->mma_levels == 4)
-        k_tile_mma<4><<<grid, kMT, launch, s>>>(t, r.count, va, nvec, d->mslices, sc, d->err_flag_dev);
+        k_tile_mma<4><<<grid, kMT, launch, s>>>(t, r.count, va, nvec, d->mslices, sc, d->err_flag_dev, nullptr);
     else
-        k_tile_mma<5><<<grid, kMT, launch, s>>>(t, r.count, va, nvec, d->mslices, sc, d->err_flag_dev);
+        k_tile_mma<5><<<grid, kMT, launch, s>>>(t, r.count, va, nvec, d->mslices, sc, d->err_flag_dev, nullptr);
+}
+
+/* One range of a batch plan (every structure with at most 16 densities). */
+void launch_batch_mma(const TileM *tiles, const int8_t *scales, const BatchMol *mols, int count, int levels, int n_sm,
+                      unsigned *err, cudaStream_t s)
+{
+    if (count <= 0) return;
+    const dim3 grid((unsigned)std::min(count, std::max(n_sm, 1)), 1);
+    VecArgs none;
+    std::memset(&none, 0, sizeof(none));
+    const int launch = (int)MmaSmem::LAUNCH;
+    if (levels == 4)
+        k_tile_mma<4><<<grid, kMT, launch, s>>>(tiles, count, none, 0, nullptr, scales, err, mols);
+    else
+        k_tile_mma<5><<<grid, kMT, launch, s>>>(tiles, count, none, 0, nullptr, scales, err, mols);
 }
 
 }  // namespace h2g

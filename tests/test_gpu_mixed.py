@@ -176,3 +176,45 @@ def test_precision_from_environment(tmp_path, oracle_lib, library, monkeypatch):
         assert b"H2G_PRECISION" in library.H2ERI_gpu_last_error()
     finally:
         h.destroy()
+
+
+def test_batch_in_shared_launches(small_mols, alk26, alk32, oracle_lib, library, monkeypatch):
+    """Five structures of different sizes, two densities each, in one
+    H2ERI_build_Coulomb_batch call in the mixed mode: their tiles run in
+    shared tensor-core launches, phase by phase (one launch carries tiles of
+    every structure). Every J matches the FP64 oracle to the mixed-mode
+    tolerance and the per-structure path (each structure on its own streams,
+    H2G_BATCH_MERGED=0) to 1e-12: the same kernel, only the order of the
+    output atomics differs. A second call reuses the batch plan."""
+    torch = pytest.importorskip("torch")
+    hs = [small_mols["CH4"], small_mols["C2H6"], small_mols["C4H10"], alk26, alk32]
+    n = len(hs)
+    dens = [np.stack([hg.molecules.seeded_density(h.num_bf, 3 + k, 900 + 10 * k + i) for i in range(2)])
+            for k, h in enumerate(hs)]
+    for h in hs:
+        h.set_precision(hg.MIXED)
+    try:
+        dDs = [torch.tensor(D, device="cuda") for D in dens]
+        harr = (ctypes.c_void_p * n)(*[h.handle.value for h in hs])
+        narr = (ctypes.c_int * n)(*([2] * n))
+        darr = (ctypes.c_void_p * n)(*[t.data_ptr() for t in dDs])
+        s = torch.cuda.current_stream()
+        out = {}
+        for mode in ("1", "0", "1"):
+            monkeypatch.setenv("H2G_BATCH_MERGED", mode)
+            dJs = [torch.full_like(t, float("nan")) for t in dDs]
+            jarr = (ctypes.c_void_p * n)(*[t.data_ptr() for t in dJs])
+            rc = library.H2ERI_build_Coulomb_batch(n, harr, narr, darr, jarr, ctypes.c_void_p(s.cuda_stream))
+            assert rc == 0, library.H2ERI_gpu_last_error()
+            torch.cuda.synchronize()
+            out.setdefault(mode, []).append([t.cpu().numpy() for t in dJs])
+        assert all(library.H2ERI_gpu_check(h.handle) == 0 for h in hs)
+    finally:
+        for h in hs:
+            h.set_precision(hg.FP64)
+    merged, single = out["1"][0], out["0"][0]
+    for k, h in enumerate(hs):
+        for i in range(2):
+            assert relerr(merged[k][i], oracle_J(oracle_lib, h, dens[k][i])) < TOL_MIXED, (k, i)
+            assert relerr(merged[k][i], single[k][i]) < 1e-12, (k, i)
+            assert relerr(out["1"][1][k][i], merged[k][i]) < 1e-12, (k, i)
