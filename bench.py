@@ -613,6 +613,19 @@ def run_gpu(args):
         elif args.precision == "mixed":
             raise RuntimeError(L.H2ERI_gpu_last_error().decode())
 
+    # the autotuner picks the launch choices of this structure (tile rows,
+    # tiles per CTA, near-field lanes, tensor-core kernel for several
+    # densities) by timing every candidate on the device; not timed here
+    tuned = {}
+    if not args.no_autotune:
+        t_tune = time.perf_counter()
+        for mode in modes:
+            L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if mode == "mixed" else hg.FP64)
+            tuned[f"{mode}_1"] = h.autotune(1)
+            if mode == "mixed":
+                tuned["mixed_16"] = h.autotune(16)
+        tuned["tuning_s"] = time.perf_counter() - t_tune
+
     def one_step(nden):
         for i in range(0, B, nden):
             L.H2ERI_build_Coulomb_device(h.handle, nden, dD[i].data_ptr(), dJ[i].data_ptr(), sp)
@@ -758,6 +771,7 @@ def run_gpu(args):
                                        "frac": bytes16 / (ms16 * n16 / B / 1e3) / 1e9 / peak,
                                        "alg_bytes_per_launch": bytes16},
                           "clocks": {k: clk16[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")}},
+        "autotune": tuned,
         "setup_s": setup_s, "upload_s": upload_s,
     }
     print(json.dumps(out), flush=True)
@@ -777,6 +791,7 @@ def main():
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--workload", default="c30", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline leg (profiler runs)")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch choices instead of tuned ones")
     ap.add_argument("--batch-size", type=int, default=8, help="molecules of the uneven batch workload")
     ap.add_argument("--builds-per-step", type=int, default=BUILDS_PER_STEP,
                     help="J builds per step (one density each); smaller for profiler captures")

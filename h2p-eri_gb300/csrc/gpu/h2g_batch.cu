@@ -186,8 +186,10 @@ bool batch_merged_eligible(int n, DevRep *const *reps, const int *n_den)
         if (std::strcmp(e, "0") == 0) return false;
     for (int i = 0; i < n; i++) {
         const DevRep *d = reps[i];
-        if (d->precision != H2ERI_GPU_MIXED || d->mslices == nullptr || n_den[i] < 1 || n_den[i] > 16 ||
-            d->device != reps[0]->device)
+        /* the structure's own choice (default or tuned) must be the
+         * tensor-core kernel at this density count */
+        if (d->precision != H2ERI_GPU_MIXED || d->mslices == nullptr || n_den[i] < d->cfg.mma_min_vec ||
+            n_den[i] > 16 || d->device != reps[0]->device)
             return false;
     }
     return true;

@@ -68,6 +68,27 @@ static_assert(sizeof(TileM) == 56, "multi-density tile descriptor layout");
 constexpr int kMmaRows = 128;      /* rows and columns of a TileM */
 constexpr int kMmaMinVec = 2;      /* densities per launch from which the tensor-core kernel runs */
 
+/* One product of the launch plan (a stored matrix, its location in the
+ * arenas and the vector ranges of its N and T sides), kept so that the tile
+ * plan can be rebuilt with other tile shapes (autotuning). */
+struct PlanRec {
+    uint64_t a, a2;
+    int ld, ld2, map, fmt;
+    int nrow, ncol;
+    int in0, out0, in1, out1;
+    uint8_t kin0, kout0, kin1, kout1;
+};
+
+/* Launch choices of one structure, picked by the autotuner
+ * (H2ERI_gpu_autotune) or left at their defaults. */
+struct TuneCfg {
+    int chunk_rows = 512;      /* rows per tile of the single-density tile kernels (128, 256, 512) */
+    int tiles_per_cta = 2;     /* mixed single-density kernel: tiles per CTA (1 or 2)               */
+    int nf_concurrent = 1;     /* near-field lanes on their own streams (1) or one stream (0)       */
+    int mma_min_vec = 2;       /* densities per launch from which the tensor-core kernel runs       */
+    int mma_grid_div = 1;      /* tensor-core launches use n_SM / mma_grid_div CTAs                  */
+};
+
 /* Storage formats of the stored matrices. */
 enum MatFmt : int {
     FMT_F64 = 0,    /* double                                               */
@@ -173,8 +194,10 @@ struct DevRep {
     std::vector<TileM> mtiles_host;
     std::vector<Range> mfwd, mmid, mbwd, mden;
     int mma_levels = 5;          /* slice levels of the multi-density kernel (4 or 5) */
-    int mma_min_vec = kMmaMinVec;
     int n_sm = 0;
+    /* the products behind every range of fwd, mid, bwd, den (same order), for re-planning */
+    std::vector<std::vector<PlanRec>> rec_fwd, rec_mid, rec_bwd, rec_den;
+    TuneCfg cfg;                 /* launch choices (autotuned or default) */
     void *kstate = nullptr;      /* exchange plan and buffers, built on first use */
     double k_work_bytes = 0.0;   /* exchange work-tensor budget, 0 = from free memory */
 };

@@ -29,6 +29,10 @@ int enqueue_coulomb(DevRep *d, int n_den, const double *den, double *J, cudaStre
 /* exchange state attached to a representation */
 void free_exchange_state(DevRep *d);
 int ensure_work(DevRep *d, int nvec);
+/* single-density tile plan rebuilt with other tile rows (autotuning) */
+int replan_tiles(DevRep *d, int rows);
+/* launch choices from the tuning cache (H2G_TUNE_FILE), at upload */
+void tune_apply_cached(DevRep *d);
 int enqueue_uncontract(DevRep *d, int n_den, const double *den, cudaStream_t s);
 int enqueue_contract(DevRep *d, int n_den, double *J, cudaStream_t s);
 /* batched J over several structures in shared launches (h2g_batch.cu) */

@@ -767,27 +767,42 @@ struct Packer {
     }
 };
 
+/* The tiles of one planned product: chunks of `rows` rows by kTileCols
+ * columns. */
+void gen_tiles(const PlanRec &q, int rows, std::vector<Tile> &tiles)
+{
+    for (int r0 = 0; r0 < q.nrow; r0 += rows)
+        for (int c0 = 0; c0 < q.ncol; c0 += kTileCols) {
+            Tile t;
+            std::memset(&t, 0, sizeof(t));
+            t.a = q.a + (size_t)r0 * q.ld + c0;
+            /* mixed formats: tensor-map coordinates of the tile (TMA loads) */
+            t.a2 = ((uint64_t)(uint32_t)c0 << 32) | (uint32_t)r0;
+            t.ld = q.ld;
+            t.ld2 = q.map;
+            t.nr = (int16_t)std::min(rows, q.nrow - r0);
+            t.nc = (int16_t)std::min(kTileCols, q.ncol - c0);
+            if (q.kout0 != VK_NONE) { t.k_in0 = q.kin0; t.in0 = q.in0 + c0; t.k_out0 = q.kout0; t.out0 = q.out0 + r0; }
+            if (q.kout1 != VK_NONE) { t.k_in1 = q.kin1; t.in1 = q.in1 + r0; t.k_out1 = q.kout1; t.out1 = q.out1 + c0; }
+            tiles.push_back(t);
+        }
+}
+
 struct Planner {
     std::vector<Tile> tiles;
     std::vector<TileM> mt;   /* the same products in 128 x 128 tiles (multi-density kernel) */
+    std::vector<PlanRec> recs;
     void add(const MatLoc &m, int nrow, int ncol, uint8_t kin0, int in0, uint8_t kout0, int out0,
              uint8_t kin1, int in1, uint8_t kout1, int out1)
     {
-        for (int r0 = 0; r0 < nrow; r0 += kChunkRows)
-            for (int c0 = 0; c0 < ncol; c0 += kTileCols) {
-                Tile t;
-                std::memset(&t, 0, sizeof(t));
-                t.a = m.a + (size_t)r0 * m.ld + c0;
-                /* mixed formats: tensor-map coordinates of the tile (TMA loads) */
-                t.a2 = ((uint64_t)(uint32_t)c0 << 32) | (uint32_t)r0;
-                t.ld = m.ld;
-                t.ld2 = m.map;
-                t.nr = (int16_t)std::min(kChunkRows, nrow - r0);
-                t.nc = (int16_t)std::min(kTileCols, ncol - c0);
-                if (kout0 != VK_NONE) { t.k_in0 = kin0; t.in0 = in0 + c0; t.k_out0 = kout0; t.out0 = out0 + r0; }
-                if (kout1 != VK_NONE) { t.k_in1 = kin1; t.in1 = in1 + r0; t.k_out1 = kout1; t.out1 = out1 + c0; }
-                tiles.push_back(t);
-            }
+        PlanRec q;
+        std::memset(&q, 0, sizeof(q));
+        q.a = m.a; q.a2 = m.a2; q.ld = m.ld; q.ld2 = m.ld2; q.map = m.map; q.fmt = m.fmt;
+        q.nrow = nrow; q.ncol = ncol;
+        q.kin0 = kin0; q.in0 = in0; q.kout0 = kout0; q.out0 = out0;
+        q.kin1 = kin1; q.in1 = in1; q.kout1 = kout1; q.out1 = out1;
+        recs.push_back(q);
+        gen_tiles(q, kChunkRows, tiles);
         for (int r0 = 0; r0 < nrow; r0 += kMmaRows)
             for (int c0 = 0; c0 < ncol; c0 += kMmaRows) {
                 TileM t;
@@ -1008,6 +1023,10 @@ static int build_rep(H2ERI_p h, DevRep *d)
     d->mbwd.clear();
     d->mmid.clear();
     d->mden.clear();
+    d->rec_fwd.clear();
+    d->rec_mid.clear();
+    d->rec_bwd.clear();
+    d->rec_den.clear();
     double mat_bytes = 0.0, mat_bytes_mixed = 0.0, vec_bytes = 0.0, flops = 0.0;
     d->fwd.clear();
     d->bwd.clear();
@@ -1043,6 +1062,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
         d->fwd.push_back(r);
         d->mfwd.push_back(Range{(int)mall.size(), (int)p.mt.size(), true});
         mall.insert(mall.end(), p.mt.begin(), p.mt.end());
+        d->rec_fwd.push_back(std::move(p.recs));
     }
 
     /* coupling blocks (src/H2ERI_matvec.c:299-407) */
@@ -1077,6 +1097,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
         all.insert(all.end(), midst[k].tiles.begin(), midst[k].tiles.end());
         d->mmid.push_back(Range{(int)mall.size(), (int)midst[k].mt.size(), false});
         mall.insert(mall.end(), midst[k].mt.begin(), midst[k].mt.end());
+        d->rec_mid.push_back(std::move(midst[k].recs));
     }
 
     /* downward sweep, shallowest level first (src/H2ERI_matvec.c:679-738) */
@@ -1101,6 +1122,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
         d->bwd.push_back(r);
         d->mbwd.push_back(Range{(int)mall.size(), (int)p.mt.size(), true});
         mall.insert(mall.end(), p.mt.begin(), p.mt.end());
+        d->rec_bwd.push_back(std::move(p.recs));
     }
 
     /* near field (src/H2ERI_matvec.c:572-660) */
@@ -1144,6 +1166,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
             all.insert(all.end(), p.tiles.begin(), p.tiles.end());
             d->mden.push_back(Range{(int)mall.size(), (int)p.mt.size(), ln == 0, ln});
             mall.insert(mall.end(), p.mt.begin(), p.mt.end());
+            d->rec_den.push_back(std::move(p.recs));
         }
 
     d->alg_bytes_matrix = mat_bytes;
@@ -1254,6 +1277,45 @@ static int build_rep(H2ERI_p h, DevRep *d)
     return 0;
 }
 
+/* Rebuild the single-density tile plan with tiles of `rows` rows (a
+ * multiple of 64, at most kChunkRows), from the recorded products: same
+ * ranges, same arenas. Waits for the device first (the old tile list may be
+ * in use). */
+int replan_tiles(DevRep *d, int rows)
+{
+    if (rows < 64 || rows > kChunkRows || rows % 64 != 0) {
+        set_error("tile rows must be a multiple of 64 in [64, " + std::to_string(kChunkRows) + "]");
+        return 3;
+    }
+    if (rows == d->cfg.chunk_rows && d->tiles != nullptr) return 0;
+    std::vector<Tile> all;
+    auto emit = [&](std::vector<Range> &rr, const std::vector<std::vector<PlanRec>> &recs) {
+        for (size_t k = 0; k < rr.size() && k < recs.size(); k++) {
+            rr[k].first = (int)all.size();
+            for (const PlanRec &q : recs[k]) gen_tiles(q, rows, all);
+            rr[k].count = (int)all.size() - rr[k].first;
+        }
+    };
+    emit(d->fwd, d->rec_fwd);
+    emit(d->mid, d->rec_mid);
+    emit(d->bwd, d->rec_bwd);
+    emit(d->den, d->rec_den);
+    std::string why;
+    if (!plan_in_bounds(all, d->arena_elems, d->krnl, d->rank_total, d->lr_total, why)) {
+        set_error(why);
+        return 3;
+    }
+    CUDA_TRY(cudaDeviceSynchronize());
+    Tile *nt = nullptr;
+    CUDA_TRY(cudaMalloc(&nt, std::max<size_t>(all.size(), 1) * sizeof(Tile)));
+    if (!all.empty()) CUDA_TRY(cudaMemcpy(nt, all.data(), all.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    cudaFree(d->tiles);
+    d->tiles = nt;
+    d->n_tiles = (int)all.size();
+    d->cfg.chunk_rows = rows;
+    return 0;
+}
+
 /* Look up (and if needed create) the device representation of h. */
 int get_rep(H2ERI_p h, DevRep **out)
 {
@@ -1280,10 +1342,18 @@ int get_rep(H2ERI_p h, DevRep **out)
     cudaGetDevice(&d->device);
     int rc = build_rep(h, d);
     if (rc != 0) { free_rep(d); return rc; }
+    tune_apply_cached(d);   /* launch choices tuned earlier for this shape (H2G_TUNE_FILE) */
     /* H2G_MMA_LEVELS=4|5: slice levels of the multi-density kernel;
      * H2G_MMA_MIN_VEC=n: densities per launch from which it runs (default 2) */
     if (const char *lv = std::getenv("H2G_MMA_LEVELS")) d->mma_levels = std::atoi(lv) == 4 ? 4 : 5;
-    if (const char *mv = std::getenv("H2G_MMA_MIN_VEC")) d->mma_min_vec = std::max(2, std::atoi(mv));
+    if (const char *mv = std::getenv("H2G_MMA_MIN_VEC")) d->cfg.mma_min_vec = std::max(2, std::atoi(mv));
+    /* H2G_TILE_ROWS=128|256|512, H2G_TILES_PER_CTA=1|2: fixed launch choices
+     * instead of the defaults or the tuned ones */
+    if (const char *tr = std::getenv("H2G_TILE_ROWS")) {
+        rc = replan_tiles(d, std::atoi(tr));
+        if (rc) { free_rep(d); return rc; }
+    }
+    if (const char *tp = std::getenv("H2G_TILES_PER_CTA")) d->cfg.tiles_per_cta = std::atoi(tp) == 1 ? 1 : 2;
     /* H2G_PRECISION=mixed starts the structure in the mixed mode, for callers
      * of the reference's entry points that do not call the extensions */
     if (const char *pe = std::getenv("H2G_PRECISION")) {
@@ -1328,9 +1398,10 @@ static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int
         if (d->precision == H2ERI_GPU_FP64)
             k_tile<FMT_F64><<<grid, kTileThreads, kTileSmemLaunch, s>>>(t, d->arena, va);
         else {
-            /* two tiles per CTA: tiles y and y + half of this launch */
+            /* two tiles per CTA: tiles y and y + half of this launch (one
+             * per CTA when the grid covers every tile) */
             const int n = std::min(kMaxGridY, r.count - f);
-            dim3 g2(nvec, (n + 1) / 2);
+            dim3 g2(nvec, d->cfg.tiles_per_cta == 1 ? n : (n + 1) / 2);
             if (r.pair)
                 k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev);
             else
@@ -1488,7 +1559,9 @@ int set_precision_mode(DevRep *d, H2ERI_p h, int mode)
         int rc = pack_mixed(d);
         if (rc) return rc;
     }
+    const bool changed = d->precision != mode;
     d->precision = mode;
+    if (changed) tune_apply_cached(d);   /* choices tuned earlier for this shape and precision */
     return 0;
 }
 
@@ -1503,7 +1576,7 @@ static int launch_near_field(DevRep *d, const VecArgs &va, int nvec, bool timed 
     CUDA_TRY(cudaStreamWaitEvent(d->s_aux, d->ev_zero, 0));
     for (size_t i = 0; i < d->den.size(); i++) {
         const Range &r = d->den[i];
-        cudaStream_t ls = r.lane == 0 ? d->s_aux : d->s_nf[r.lane];
+        cudaStream_t ls = (r.lane == 0 || !d->cfg.nf_concurrent) ? d->s_aux : d->s_nf[r.lane];
         if (mma) launch_range_mma(d, d->mden[i], va, nvec, ls);
         else launch_range(d, r, va, nvec, ls);
     }
@@ -1547,7 +1620,7 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], sm));
     /* several densities in the mixed mode: the tensor-core kernel, all
      * densities (up to 16 per pass) sharing each tile's slices */
-    const bool mma = d->precision == H2ERI_GPU_MIXED && nvec >= d->mma_min_vec && d->mslices != nullptr;
+    const bool mma = d->precision == H2ERI_GPU_MIXED && nvec >= d->cfg.mma_min_vec && d->mslices != nullptr;
     auto launch = [&](const Range &r) {
         if (mma) launch_range_mma(d, r, va, nvec, sm);
         else launch_range(d, r, va, nvec, sm);
@@ -1923,11 +1996,13 @@ extern "C" int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n)
     for (const Range &r : d->den) launches += r.count > 0;
     for (const Range &r : d->mid) launches += r.count > 0;
     double mbytes = d->precision == H2ERI_GPU_MIXED ? d->alg_bytes_matrix_mixed : d->alg_bytes_matrix;
-    double vals[14] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
+    double vals[19] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
                        (double)d->bytes_U, (double)d->bytes_B, (double)d->bytes_D,
                        d->last_ms[0], d->last_ms[1], d->last_ms[2], d->last_ms[3], d->last_ms[4],
-                       (double)d->precision, (double)(2.0 * d->rank_total + d->lr_total)};
-    int m = std::min(n, 14);
+                       (double)d->precision, (double)(2.0 * d->rank_total + d->lr_total),
+                       (double)d->cfg.chunk_rows, (double)d->cfg.tiles_per_cta, (double)d->cfg.nf_concurrent,
+                       (double)d->cfg.mma_min_vec, (double)d->cfg.mma_grid_div};
+    int m = std::min(n, 19);
     for (int i = 0; i < m; i++) out[i] = vals[i];
     return m;
 }

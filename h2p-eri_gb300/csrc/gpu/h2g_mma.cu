@@ -698,7 +698,8 @@ int mma_make_slices(DevRep *d)
 void launch_range_mma(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s)
 {
     if (r.count <= 0) return;
-    const dim3 grid((unsigned)std::min(r.count, std::max(d->n_sm, 1)), (unsigned)((nvec + kMV - 1) / kMV));
+    const int ctas = std::max(1, d->n_sm / std::max(1, d->cfg.mma_grid_div));
+    const dim3 grid((unsigned)std::min(r.count, ctas), (unsigned)((nvec + kMV - 1) / kMV));
     const TileM *t = d->mtiles + r.first;
     const int8_t *sc = d->mscales + (size_t)r.first * 256;
     const int launch = (int)MmaSmem::LAUNCH;

@@ -160,13 +160,34 @@ int H2ERI_exchange_plan_check(H2ERI_p h2eri, double device_bytes, double *out, i
  * enqueueing; H2ERI_gpu_check reports a kernel's expired wait afterwards. */
 int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, void *stream);
 
+/* Autotuner (no counterpart in the reference): runs every candidate launch
+ * configuration of this structure at n_den densities per launch in its
+ * current precision on the device, times each with CUDA events, and keeps
+ * the fastest. Candidates: rows per tile of the single-density kernels
+ * (512, 256, 128), tiles per CTA (2, 1; mixed mode), near-field lanes on
+ * their own streams or one; for several densities in the mixed mode also
+ * the tensor-core kernel (n_SM or n_SM / 2 CTAs per launch) against the
+ * single-density kernels. The choice is cached per structure shape,
+ * precision and density-count class in the process and, with
+ * H2G_TUNE_FILE=<path> in the environment, in that file, which later
+ * processes read when a structure of the same shape is uploaded or changes
+ * precision. Synchronises the device; takes about 0.1-1 s. out: [0] ms per
+ * matvec with the choice, [1] ms before tuning, [2] candidates timed,
+ * [3..7] the choice (tile rows, tiles per CTA, near-field lanes concurrent,
+ * density count from which the tensor-core kernel runs, its CTA divisor),
+ * [8..] ms of each candidate. Returns the number of values written, or < 0. */
+int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n);
+
 /* Figures of the device copy, for reports. out[0] kernel launches per matvec
  * call (one vector block), out[1] algorithmic matrix bytes read per matvec,
  * out[2] algorithmic vector bytes per vector, out[3] flops per vector,
  * out[4..6] arena bytes of U, B, D, out[7..11] last timed phase durations
  * in ms (upward, coupling, downward, near field, total), out[12] far-field
- * precision mode, out[13] scratch doubles one matvec of one vector needs.
- * Returns the number of values written (<= n), or < 0. */
+ * precision mode, out[13] scratch doubles one matvec of one vector needs,
+ * out[14..18] the launch choices in use (tile rows, tiles per CTA,
+ * near-field lanes concurrent, density count from which the tensor-core
+ * kernel runs, its CTA divisor; see H2ERI_gpu_autotune). Returns the number
+ * of values written (<= n), or < 0. */
 int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n);
 
 /* Save / load the H2 representation (tree, pair lists, U, B, D and the
