@@ -470,13 +470,20 @@ def run_gpu_batch(args):
     log(f"set-up of {len(hs)} molecules (host, not timed): {setup_s:.1f} s")
     best = "mixed" if args.precision in ("auto", "mixed") else "fp64"
     dDs, dJs, Ds = [], [], []
+    choices = {}
+    t_tune = time.perf_counter()
     for k, h in enumerate(hs):
         L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if best == "mixed" else hg.FP64)
+        if not args.no_autotune:
+            c = h.autotune(2)["choice"]
+            key = ",".join(f"{a}={b}" for a, b in sorted(c.items()))
+            choices[key] = choices.get(key, 0) + 1
         n_occ = (8 * lengths[k] + 2) // 2   # electrons of C_nH_2n+2 / 2
         D = np.stack([molecules.seeded_density(h.num_bf, n_occ, 4000 + 10 * k + i) for i in range(2)])
         Ds.append(D)
         dDs.append(torch.tensor(D, device="cuda"))
         dJs.append(torch.empty_like(dDs[-1]))
+    tune_s = time.perf_counter() - t_tune
     n = len(hs)
     harr = (ctypes.c_void_p * n)(*[h.handle.value for h in hs])
     narr = (ctypes.c_int * n)(*([2] * n))
@@ -523,6 +530,7 @@ def run_gpu_batch(args):
            "config": dict(WORKLOAD, molecules=[f"C{m}H{2 * m + 2}" for m in lengths], precision=best,
                           sample=f"{n} molecules (lengths from U{{8..60}}, seed 4242); 2 densities each"),
            "one_by_one_ms_per_step": ms_seq, "batch_speedup": ms_seq / ms,
+           "autotune": {"choices_at_2_densities": choices, "tuning_and_upload_s": tune_s},
            "relerr_vs_fp64_oracle_sampled": max(errs),
            "clocks": {"sm_mhz": c["sm_mhz"], "sm_max_mhz": c["sm_max_mhz"], "reasons": c["reasons"]},
            "setup_s": setup_s}

@@ -12,7 +12,11 @@
  *   downward sweep, level k   (k-th level from the top of each structure)
  * Each structure keeps its own order of phases, so its dependencies hold,
  * while every launch carries the tiles of all structures: about 18 launches
- * of the multi-density kernel for the whole batch. Each tile names its
+ * of the multi-density kernel for the whole batch. Where the structures'
+ * launch choices (default or tuned) put their density count on the
+ * single-density kernels instead, the same merge is made of their tile
+ * plans for the mixed single-density kernel (near-field stages split by
+ * storage format). Each tile names its
  * structure (vector spaces and number of densities in a small table) and
  * carries the device address of its slices. The plan is built once for a
  * set of structures and their densities per structure, and reused while
@@ -42,18 +46,24 @@ namespace h2g {
 namespace {
 
 struct BatchPlan {
+    bool simt = false;                  /* single-density tile kernel (else the tensor-core kernel) */
     std::vector<const DevRep *> reps;
     std::vector<int> n_den;
     std::vector<const void *> bufs;     /* x, y and work buffers each plan entry points at */
-    TileM *tiles = nullptr;
+    std::vector<const void *> plans;    /* the structures' tile lists the plan was made from */
+    TileM *tiles = nullptr;             /* tensor-core plan */
     int8_t *scales = nullptr;
+    Tile *stiles = nullptr;             /* single-density plan: tiles and concatenated tensor maps */
+    void *maps = nullptr;
     BatchMol *mols = nullptr;
-    std::vector<Range> phases;          /* launch order */
+    std::vector<Range> phases;          /* launch order (pair: float-pair format, single-density plan) */
     int n_tiles = 0;
     ~BatchPlan()
     {
         cudaFree(tiles);
         cudaFree(scales);
+        cudaFree(stiles);
+        cudaFree(maps);
         cudaFree(mols);
     }
 };
@@ -79,19 +89,94 @@ VecArgs rep_vecargs(const DevRep *d, int nvec)
     return va;
 }
 
-bool same_plan(const BatchPlan *p, int n, DevRep *const *reps, const int *n_den)
+bool same_plan(const BatchPlan *p, bool simt, int n, DevRep *const *reps, const int *n_den)
 {
-    if (p == nullptr || (int)p->reps.size() != n) return false;
+    if (p == nullptr || p->simt != simt || (int)p->reps.size() != n) return false;
     for (int i = 0; i < n; i++)
         if (p->reps[i] != reps[i] || p->n_den[i] != n_den[i] || p->bufs[3 * i] != reps[i]->xbuf ||
-            p->bufs[3 * i + 1] != reps[i]->ybuf || p->bufs[3 * i + 2] != reps[i]->work)
+            p->bufs[3 * i + 1] != reps[i]->ybuf || p->bufs[3 * i + 2] != reps[i]->work ||
+            p->plans[i] != (const void *)reps[i]->tiles)
             return false;
     return true;
 }
 
-int build_plan(int n, DevRep *const *reps, const int *n_den, BatchPlan **out)
+/* The single-density batch plan: phases near field stage s (float pairs,
+ * then single floats), upward levels, coupling stages, downward levels,
+ * each with the tiles of every structure; tensor-map indices shifted into
+ * the concatenated map array, the structure index in Tile::a. */
+int build_plan_simt(int n, DevRep *const *reps, const int *n_den, BatchPlan *p)
+{
+    std::vector<Tile> all;
+    std::vector<int> map_off(n, 0);
+    size_t n_maps = 0;
+    for (int i = 0; i < n; i++) {
+        map_off[i] = (int)n_maps;
+        n_maps += std::max<size_t>(reps[i]->mixed_items.size(), 1);
+    }
+    auto merge = [&](bool pair, auto pick) {
+        Range r;
+        r.first = (int)all.size();
+        r.pair = pair;
+        for (int i = 0; i < n; i++) {
+            const DevRep *d = reps[i];
+            for (const Range *q : pick(d)) {
+                if (q == nullptr || q->count <= 0) continue;
+                for (int t = 0; t < q->count; t++) {
+                    Tile m = d->tiles_host[q->first + t];
+                    m.a = (uint64_t)i;
+                    m.ld2 += map_off[i];
+                    all.push_back(m);
+                }
+            }
+        }
+        r.count = (int)all.size() - r.first;
+        if (r.count > 0) p->phases.push_back(r);
+    };
+    for (int s = 0; s < 3; s++) {
+        merge(true, [&](const DevRep *d) { return std::vector<const Range *>{&d->den[s]}; });
+        merge(false, [&](const DevRep *d) {
+            std::vector<const Range *> v;
+            for (int ln = 1; ln < kNfLanes; ln++) v.push_back(&d->den[ln * 3 + s]);
+            return v;
+        });
+    }
+    size_t nf = 0, nb = 0;
+    for (int i = 0; i < n; i++) {
+        nf = std::max(nf, reps[i]->fwd.size());
+        nb = std::max(nb, reps[i]->bwd.size());
+    }
+    for (size_t k = 0; k < nf; k++)
+        merge(true, [&](const DevRep *d) { return std::vector<const Range *>{k < d->fwd.size() ? &d->fwd[k] : nullptr}; });
+    for (int s = 0; s < 3; s++)
+        merge(false, [&](const DevRep *d) { return std::vector<const Range *>{&d->mid[s]}; });
+    for (size_t k = 0; k < nb; k++)
+        merge(true, [&](const DevRep *d) { return std::vector<const Range *>{k < d->bwd.size() ? &d->bwd[k] : nullptr}; });
+    p->n_tiles = (int)all.size();
+    const size_t map_bytes = 128;   /* sizeof(CUtensorMap) */
+    if (cudaMalloc(&p->stiles, std::max<size_t>(all.size(), 1) * sizeof(Tile)) != cudaSuccess ||
+        cudaMalloc(&p->maps, std::max<size_t>(n_maps, 1) * map_bytes) != cudaSuccess) {
+        set_error("batch plan: device memory");
+        return 10;
+    }
+    if (!all.empty() && cudaMemcpy(p->stiles, all.data(), all.size() * sizeof(Tile), cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("batch plan: tile upload");
+        return 10;
+    }
+    for (int i = 0; i < n; i++) {
+        const size_t cnt = std::max<size_t>(reps[i]->mixed_items.size(), 1);
+        if (cudaMemcpy(static_cast<char *>(p->maps) + (size_t)map_off[i] * map_bytes, reps[i]->tmaps, cnt * map_bytes,
+                       cudaMemcpyDeviceToDevice) != cudaSuccess) {
+            set_error("batch plan: tensor map copy");
+            return 10;
+        }
+    }
+    return 0;
+}
+
+int build_plan(bool simt, int n, DevRep *const *reps, const int *n_den, BatchPlan **out)
 {
     BatchPlan *p = new BatchPlan();
+    p->simt = simt;
     std::vector<TileM> all;
     std::vector<std::pair<const int8_t *, int>> sc_src;   /* per merged range piece: source scales, count */
     std::vector<BatchMol> mols(n);
@@ -101,9 +186,22 @@ int build_plan(int n, DevRep *const *reps, const int *n_den, BatchPlan **out)
         p->bufs.push_back(reps[i]->xbuf);
         p->bufs.push_back(reps[i]->ybuf);
         p->bufs.push_back(reps[i]->work);
+        p->plans.push_back(reps[i]->tiles);
         mols[i].va = rep_vecargs(reps[i], n_den[i]);
         mols[i].nvec = n_den[i];
         mols[i].pad_ = 0;
+    }
+    auto fail = [&](int rc) { delete p; return rc; };
+    if (cudaMalloc(&p->mols, (size_t)std::max(n, 1) * sizeof(BatchMol)) != cudaSuccess ||
+        cudaMemcpy(p->mols, mols.data(), (size_t)n * sizeof(BatchMol), cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("batch plan: structure table upload");
+        return fail(10);
+    }
+    if (simt) {
+        int rc = build_plan_simt(n, reps, n_den, p);
+        if (rc) return fail(rc);
+        *out = p;
+        return 0;
     }
     /* one merged phase: the given range of every structure, in order */
     auto merge = [&](auto pick) {
@@ -148,10 +246,8 @@ int build_plan(int n, DevRep *const *reps, const int *n_den, BatchPlan **out)
             return std::vector<const Range *>{k < d->mbwd.size() ? &d->mbwd[k] : nullptr};
         });
     p->n_tiles = (int)all.size();
-    auto fail = [&](int rc) { delete p; return rc; };
     if (cudaMalloc(&p->tiles, std::max<size_t>(all.size(), 1) * sizeof(TileM)) != cudaSuccess ||
-        cudaMalloc(&p->scales, std::max<size_t>(all.size(), 1) * 256) != cudaSuccess ||
-        cudaMalloc(&p->mols, (size_t)std::max(n, 1) * sizeof(BatchMol)) != cudaSuccess) {
+        cudaMalloc(&p->scales, std::max<size_t>(all.size(), 1) * 256) != cudaSuccess) {
         set_error("batch plan: device memory");
         return fail(10);
     }
@@ -169,30 +265,30 @@ int build_plan(int n, DevRep *const *reps, const int *n_den, BatchPlan **out)
         }
         pos += (size_t)sp.second;
     }
-    if (cudaMemcpy(p->mols, mols.data(), (size_t)n * sizeof(BatchMol), cudaMemcpyHostToDevice) != cudaSuccess) {
-        set_error("batch plan: structure table upload");
-        return fail(10);
-    }
     *out = p;
     return 0;
 }
 
 }  // namespace
 
-bool batch_merged_eligible(int n, DevRep *const *reps, const int *n_den)
+/* 1: every structure runs the tensor-core kernel at its density count (its
+ * own choice, default or tuned); 2: every structure runs the mixed
+ * single-density kernels and all have the same density count; 0: neither
+ * (each structure then runs on its own streams). */
+int batch_merged_kind(int n, DevRep *const *reps, const int *n_den)
 {
-    if (n < 1) return false;
+    if (n < 1) return 0;
     if (const char *e = std::getenv("H2G_BATCH_MERGED"))
-        if (std::strcmp(e, "0") == 0) return false;
+        if (std::strcmp(e, "0") == 0) return 0;
+    bool mma = true, simt = true;
     for (int i = 0; i < n; i++) {
         const DevRep *d = reps[i];
-        /* the structure's own choice (default or tuned) must be the
-         * tensor-core kernel at this density count */
-        if (d->precision != H2ERI_GPU_MIXED || d->mslices == nullptr || n_den[i] < d->cfg.mma_min_vec ||
-            n_den[i] > 16 || d->device != reps[0]->device)
-            return false;
+        if (d->precision != H2ERI_GPU_MIXED || d->device != reps[0]->device || d->tmaps == nullptr) return 0;
+        if (d->mslices == nullptr || n_den[i] < d->cfg.mma_min_vec || n_den[i] > 16) mma = false;
+        if (n_den[i] >= d->cfg.mma_min_vec && d->mslices != nullptr) simt = false;
+        if (n_den[i] != n_den[0]) simt = false;
     }
-    return true;
+    return mma ? 1 : (simt ? 2 : 0);
 }
 
 void batch_forget(const DevRep *d)
@@ -211,18 +307,19 @@ void batch_forget(const DevRep *d)
  * all structures phase by phase in shared launches, J contracted per
  * structure. Kernel errors (an expired bounded wait) are recorded in the
  * first structure's error word (H2ERI_gpu_check). */
-int batch_coulomb_merged(int n, DevRep *const *reps, const int *n_den, const double *const *d_dens,
+int batch_coulomb_merged(int kind, int n, DevRep *const *reps, const int *n_den, const double *const *d_dens,
                          double *const *d_Js, cudaStream_t s)
 {
     std::lock_guard<std::mutex> lk(g_bmu);
+    const bool simt = kind == 2;
     for (int i = 0; i < n; i++) {
         int rc = ensure_work(reps[i], n_den[i]);
         if (rc) return rc;
     }
-    if (!same_plan(g_bplan, n, reps, n_den)) {
+    if (!same_plan(g_bplan, simt, n, reps, n_den)) {
         delete g_bplan;
         g_bplan = nullptr;
-        int rc = build_plan(n, reps, n_den, &g_bplan);
+        int rc = build_plan(simt, n, reps, n_den, &g_bplan);
         if (rc) return rc;
     }
     const BatchPlan *p = g_bplan;
@@ -234,9 +331,14 @@ int batch_coulomb_merged(int n, DevRep *const *reps, const int *n_den, const dou
         int rc = enqueue_uncontract(d, n_den[i], d_dens[i], s);
         if (rc) return rc;
     }
-    for (const Range &r : p->phases)
-        launch_batch_mma(p->tiles + r.first, p->scales + (size_t)r.first * 256, p->mols, r.count, reps[0]->mma_levels,
-                         reps[0]->n_sm, reps[0]->err_flag_dev, s);
+    for (const Range &r : p->phases) {
+        if (simt)
+            launch_batch_mx(p->stiles + r.first, r.count, r.pair, p->maps, p->mols, n_den[0],
+                            reps[0]->cfg.tiles_per_cta, reps[0]->err_flag_dev, s);
+        else
+            launch_batch_mma(p->tiles + r.first, p->scales + (size_t)r.first * 256, p->mols, r.count,
+                             reps[0]->mma_levels, reps[0]->n_sm, reps[0]->err_flag_dev, s);
+    }
     BCUDA_TRY(cudaGetLastError());
     for (int i = 0; i < n; i++) {
         int rc = enqueue_contract(reps[i], n_den[i], d_Js[i], s);

@@ -159,6 +159,7 @@ struct DevRep {
     /* plan */
     Tile *tiles = nullptr;
     int n_tiles = 0;
+    std::vector<Tile> tiles_host;   /* host copy of the tile plan (batch plans) */
     std::vector<Range> fwd;     /* deepest level first */
     std::vector<Range> bwd;     /* shallowest level first */
     std::vector<Range> mid;     /* coupling blocks, stages 1..3 */

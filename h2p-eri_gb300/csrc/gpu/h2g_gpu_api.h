@@ -36,14 +36,17 @@ void tune_apply_cached(DevRep *d);
 int enqueue_uncontract(DevRep *d, int n_den, const double *den, cudaStream_t s);
 int enqueue_contract(DevRep *d, int n_den, double *J, cudaStream_t s);
 /* batched J over several structures in shared launches (h2g_batch.cu) */
-bool batch_merged_eligible(int n, DevRep *const *reps, const int *n_den);
-int batch_coulomb_merged(int n, DevRep *const *reps, const int *n_den, const double *const *d_dens,
+int batch_merged_kind(int n, DevRep *const *reps, const int *n_den);
+int batch_coulomb_merged(int kind, int n, DevRep *const *reps, const int *n_den, const double *const *d_dens,
                          double *const *d_Js, cudaStream_t s);
 void batch_forget(const DevRep *d);
 /* multi-density tensor-core kernel (h2g_mma.cu) */
 int mma_init(DevRep *d);
 int mma_make_slices(DevRep *d);
 void launch_range_mma(const DevRep *d, const Range &r, const VecArgs &va, int nvec, cudaStream_t s);
+/* a merged range of a batch plan on the mixed single-density kernel */
+void launch_batch_mx(const Tile *tiles, int count, bool pair, const void *maps, const BatchMol *mols, int nvec,
+                     int tiles_per_cta, unsigned *err, cudaStream_t s);
 /* a range of a batch plan: tiles, their scales and the structures' table */
 void launch_batch_mma(const TileM *tiles, const int8_t *scales, const BatchMol *mols, int count, int levels, int n_sm,
                       unsigned *err, cudaStream_t s);

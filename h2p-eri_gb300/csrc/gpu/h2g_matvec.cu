@@ -374,8 +374,11 @@ constexpr size_t kMxSmem = (sizeof(MxSmem) + 127) & ~size_t(127);
 template <int FMT>
 __global__ void __launch_bounds__(kTileThreads, 2)
 k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ VecArgs va,
-          const CUtensorMap *__restrict__ maps, unsigned *err)
+          const CUtensorMap *__restrict__ maps, unsigned *err, const BatchMol *__restrict__ mols)
 {
+    /* one structure: va; a batch (mols != nullptr): each tile's structure
+     * index is in its FP64 arena offset, which the mixed kernel never reads */
+    auto tva = [&](const Tile &t) -> const VecArgs & { return mols ? mols[t.a].va : va; };
     constexpr int EB = FmtInfo<FMT>::ebytes;
     constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage: 64 or 32   */
     constexpr int RB = kTileCols * EB;                    /* bytes per stage row        */
@@ -442,13 +445,13 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
         const bool n0 = t.k_out0 != VK_NONE, n1 = t.k_out1 != VK_NONE;
         if (tid < kTileCols) {
             float h = 0.f, l = 0.f;
-            if (n0 && tid < t.nc) split(vec_ptr(va, t.k_in0, t.in0, v)[tid], h, l);
+            if (n0 && tid < t.nc) split(vec_ptr(tva(t), t.k_in0, t.in0, v)[tid], h, l);
             X.x0h[tid] = h; X.x0l[tid] = l;
         }
         if (n1)
             for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
                 float h = 0.f, l = 0.f;
-                if (r < t.nr) split(vec_ptr(va, t.k_in1, t.in1, v)[r], h, l);
+                if (r < t.nr) split(vec_ptr(tva(t), t.k_in1, t.in1, v)[r], h, l);
                 X.x1h[r] = h; X.x1l[r] = l;
             }
     }
@@ -591,7 +594,7 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
                         pk_dfadd(ch[j], cl[j], oh, ol);
                     }
                 if (trl == 0) {
-                    double *out1 = vec_ptr(va, t.k_out1, t.out1, v);
+                    double *out1 = vec_ptr(tva(t), t.k_out1, t.out1, v);
                     if (FMT == FMT_F32) {
                         const int c = tb * 32 + tq * 4;
                         if (c < t.nc) atomic_add_pair(out1 + c, ch[0].x, cl[0].x);
@@ -623,7 +626,7 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
                     float h = P[rr].x, l = P[rr].y;
 #pragma unroll
                     for (int q = 1; q < NCG; q++) dfadd(h, l, P[q * SR + rr].x, P[q * SR + rr].y);
-                    atomic_add_pair(vec_ptr(va, t.k_out0, t.out0, v) + grow, h, l);
+                    atomic_add_pair(vec_ptr(tva(t), t.k_out0, t.out0, v) + grow, h, l);
                 }
                 if (lane == 0) sm.grp_cnt[slot][ng] = 0;
             }
@@ -1189,6 +1192,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaMemcpy(d->arena, pk.host.data(), d->arena_elems * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMalloc(&d->tiles, std::max<size_t>(all.size(), 1) * sizeof(Tile)));
     if (!all.empty()) CUDA_TRY(cudaMemcpy(d->tiles, all.data(), all.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    d->tiles_host = all;
     d->n_mtiles = (int)mall.size();
     {
         /* offsets of the tiles' pre-computed slices (1 KB aligned) */
@@ -1312,6 +1316,7 @@ int replan_tiles(DevRep *d, int rows)
     cudaFree(d->tiles);
     d->tiles = nt;
     d->n_tiles = (int)all.size();
+    d->tiles_host = std::move(all);
     d->cfg.chunk_rows = rows;
     return 0;
 }
@@ -1403,10 +1408,30 @@ static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int
             const int n = std::min(kMaxGridY, r.count - f);
             dim3 g2(nvec, d->cfg.tiles_per_cta == 1 ? n : (n + 1) / 2);
             if (r.pair)
-                k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev);
+                k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev, nullptr);
             else
-                k_tile_mx<FMT_F32><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev);
+                k_tile_mx<FMT_F32><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev, nullptr);
         }
+    }
+}
+
+/* One merged range of a batch plan on the mixed single-density kernel:
+ * tiles of every structure (structure index in Tile::a), the structures'
+ * tensor maps concatenated, nvec densities each. */
+void launch_batch_mx(const Tile *tiles, int count, bool pair, const void *maps, const BatchMol *mols, int nvec,
+                     int tiles_per_cta, unsigned *err, cudaStream_t s)
+{
+    constexpr int kMaxGridY = 65535;
+    VecArgs none;
+    std::memset(&none, 0, sizeof(none));
+    for (int f = 0; f < count; f += kMaxGridY) {
+        const int n = std::min(kMaxGridY, count - f);
+        dim3 g2(nvec, tiles_per_cta == 1 ? n : (n + 1) / 2);
+        const CUtensorMap *m = reinterpret_cast<const CUtensorMap *>(maps);
+        if (pair)
+            k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kMxSmem, s>>>(tiles + f, n, none, m, err, mols);
+        else
+            k_tile_mx<FMT_F32><<<g2, kTileThreads, kMxSmem, s>>>(tiles + f, n, none, m, err, mols);
     }
 }
 
@@ -1884,9 +1909,9 @@ extern "C" int H2ERI_build_Coulomb_device(H2ERI_p h2eri, int n_den, const double
     return enqueue_coulomb(d, n_den, d_den, d_J, s, false);
 }
 
-/* J for several structures at once. In the mixed mode (every structure
- * with at most 16 densities) the H2 products of all structures run in
- * shared launches of the tensor-core kernel, one per phase (h2g_batch.cu).
+/* J for several structures at once. In the mixed mode the H2 products of
+ * all structures run in shared launches, one per phase, of the kernel their
+ * launch choices name for their density count (h2g_batch.cu).
  * Otherwise every structure's build runs on its own pair of streams, forked
  * from `stream` and joined back to it, so the builds of small and large
  * molecules overlap on the GPU. All device buffers are set up before
@@ -1915,7 +1940,8 @@ extern "C" int H2ERI_build_Coulomb_batch(int n, H2ERI_p *h2eris, const int *n_de
     cudaStream_t s = (cudaStream_t)stream;
     /* mixed mode with at most 16 densities per structure: every structure's
      * tiles in shared tensor-core launches, phase by phase */
-    if (batch_merged_eligible(n, reps.data(), n_den)) return batch_coulomb_merged(n, reps.data(), n_den, d_dens, d_Js, s);
+    if (const int kind = batch_merged_kind(n, reps.data(), n_den))
+        return batch_coulomb_merged(kind, n, reps.data(), n_den, d_dens, d_Js, s);
     for (int i = 0; i < n; i++) {
         DevRep *d = reps[i];
         CUDA_TRY(cudaEventRecord(d->ev_bfork, s));

@@ -218,3 +218,47 @@ def test_batch_in_shared_launches(small_mols, alk26, alk32, oracle_lib, library,
             assert relerr(merged[k][i], oracle_J(oracle_lib, h, dens[k][i])) < TOL_MIXED, (k, i)
             assert relerr(merged[k][i], single[k][i]) < 1e-12, (k, i)
             assert relerr(out["1"][1][k][i], merged[k][i]) < 1e-12, (k, i)
+
+
+def test_batch_in_shared_launches_single_density_kernels(oracle_lib, library, monkeypatch, tmp_path):
+    """The same shared-launch batch when the structures' launch choices put
+    two densities on the single-density kernels (as the tuner does for
+    short chains): their tile plans are merged phase by phase for the mixed
+    tile kernel, with the tensor maps of all structures in one array. Tile
+    shapes differ between structures (256 and 512 rows)."""
+    torch = pytest.importorskip("torch")
+    monkeypatch.setenv("H2G_MMA_MIN_VEC", "3")
+    hs = []
+    try:
+        for k, nc in enumerate((1, 3, 5, 8)):
+            p = str(tmp_path / f"c{nc}.mol")
+            hg.molecules.write_alkane(p, nc)
+            monkeypatch.setenv("H2G_TILE_ROWS", "256" if k % 2 else "512")
+            h = hg.H2ERI.from_mol(p, qr_tol=1e-6)
+            h.set_precision(hg.MIXED)
+            hs.append(h)
+        n = len(hs)
+        dens = [np.stack([hg.molecules.seeded_density(h.num_bf, 2 + k, 950 + 10 * k + i) for i in range(2)])
+                for k, h in enumerate(hs)]
+        dDs = [torch.tensor(D, device="cuda") for D in dens]
+        harr = (ctypes.c_void_p * n)(*[h.handle.value for h in hs])
+        narr = (ctypes.c_int * n)(*([2] * n))
+        darr = (ctypes.c_void_p * n)(*[t.data_ptr() for t in dDs])
+        s = torch.cuda.current_stream()
+        out = {}
+        for mode in ("1", "0"):
+            monkeypatch.setenv("H2G_BATCH_MERGED", mode)
+            dJs = [torch.full_like(t, float("nan")) for t in dDs]
+            jarr = (ctypes.c_void_p * n)(*[t.data_ptr() for t in dJs])
+            rc = library.H2ERI_build_Coulomb_batch(n, harr, narr, darr, jarr, ctypes.c_void_p(s.cuda_stream))
+            assert rc == 0, library.H2ERI_gpu_last_error()
+            torch.cuda.synchronize()
+            out[mode] = [t.cpu().numpy() for t in dJs]
+        assert all(library.H2ERI_gpu_check(h.handle) == 0 for h in hs)
+        for k, h in enumerate(hs):
+            for i in range(2):
+                assert relerr(out["1"][k][i], oracle_J(oracle_lib, h, dens[k][i])) < TOL_MIXED, (k, i)
+                assert relerr(out["1"][k][i], out["0"][k][i]) < 1e-12, (k, i)
+    finally:
+        for h in hs:
+            h.destroy()
