@@ -60,6 +60,13 @@ WORKLOADS = {
             "inputs_vs_L2": "H2 representation ~0.28 GB read per step > 129 MB L2",
             "k_cpu_stride": 2, "k_check_full": True},
 }
+# the 3-D exchange case: a seeded cluster of 48 CH4 (a water cluster needs
+# oxygen basis data, which is not available), K builds
+WORKLOADS["ch4x48"] = {"workload": "K build, 3-D cluster of 48 CH4 (4x4x3 jittered cubic lattice 4 A apart, "
+                                   "seeded orientations), cc-pVDZ cartesian (1680 bf), QR tol 1e-7, 1 density "
+                                   "n_occ=240", "molecule": "(CH4)48", "cluster": [4, 4, 3], "qr_tol": 1e-7,
+                       "n_occ": 240, "seed": 5000, "k_cpu_stride": 128,
+                       "inputs_vs_L2": "H2 representation and K intermediates > 129 MB L2"}
 # uneven batch: alkanes with lengths drawn from C8..C60 (seeded), two densities
 # each; BATCH_SIZE molecules (the set-up of each runs on the host first)
 WORKLOADS["batch"] = {"workload": "J builds for a batch of alkanes C8..C60 (seeded lengths), cc-pVDZ cartesian, "
@@ -87,14 +94,32 @@ def dist_env():
     return ws, rank, local
 
 
+def workload_name():
+    if "cluster" in WORKLOAD:
+        return "ch4c" + "x".join(str(n) for n in WORKLOAD["cluster"])
+    return f"alk{WORKLOAD['n_carbon']}"
+
+
+def geometry_kind():
+    return "CH4 cluster" if "cluster" in WORKLOAD else "alkane"
+
+
+def write_workload_mol(molecules, path):
+    """The workload's molecule as a .mol file: an alkane or a CH4 cluster."""
+    if "cluster" in WORKLOAD:
+        molecules.write_methane_cluster(path, tuple(WORKLOAD["cluster"]), seed=WORKLOAD["seed"])
+    else:
+        molecules.write_alkane(path, WORKLOAD["n_carbon"])
+
+
 def representation(hg, molecules, rank, ws, barrier):
     """Build (rank 0) or load the cached representation of the workload."""
     os.makedirs(CACHE_DIR, exist_ok=True)
-    path = os.path.join(CACHE_DIR, f"alk{WORKLOAD['n_carbon']}_{WORKLOAD['qr_tol']:g}.h2r")
+    path = os.path.join(CACHE_DIR, f"{workload_name()}_{WORKLOAD['qr_tol']:g}.h2r")
     setup_s = None
     if rank == 0 and not os.path.exists(path):
-        mol = os.path.join(CACHE_DIR, f"alk{WORKLOAD['n_carbon']}.mol")
-        molecules.write_alkane(mol, WORKLOAD["n_carbon"])
+        mol = os.path.join(CACHE_DIR, f"{workload_name()}.mol")
+        write_workload_mol(molecules, mol)
         t0 = time.perf_counter()
         h = hg.H2ERI.from_mol(mol, qr_tol=WORKLOAD["qr_tol"])
         setup_s = time.perf_counter() - t0
@@ -292,7 +317,7 @@ def run_reference_exchange(args):
     out = {"impl": "reference", "metric": METRIC_K, "value": v, "unit": "K builds/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic (generated alkane geometry, seeded density)", "config": dict(WORKLOAD, path="exchange"),
+           "data": f"synthetic (generated {geometry_kind()} geometry, seeded density)", "config": dict(WORKLOAD, path="exchange"),
            "cpu_baseline": {"value": v, "unit": "K builds/s", "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": v, "unit": "K builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -311,8 +336,8 @@ def run_setup(args):
     import h2eri_gb300 as hg
     from h2eri_gb300 import build as hb, molecules
     hb.build()
-    mol = os.path.join(tempfile.mkdtemp(), f"alk{WORKLOAD['n_carbon']}.mol")
-    molecules.write_alkane(mol, WORKLOAD["n_carbon"])
+    mol = os.path.join(tempfile.mkdtemp(), f"{workload_name()}.mol")
+    write_workload_mol(molecules, mol)
     qr = WORKLOAD["qr_tol"]
     if args.impl == "reference":
         from oracle import build_ref
@@ -340,7 +365,7 @@ def run_setup(args):
     out = {"metric": f"host set-up seconds {WORKLOAD['molecule']} (H2ERI_build_H2 and the calls before it)",
            "value": statistics.median(times), "unit": "s", "higher_is_better": False, "steps": steps,
            "warmup": 1, "samples_s": [round(t, 3) for t in times], "cores": cores, "dtype": "f64",
-           "data": "synthetic (generated alkane geometry)", "config": dict(WORKLOAD)}
+           "data": f"synthetic (generated {geometry_kind()} geometry)", "config": dict(WORKLOAD)}
     if args.impl == "reference":
         out["impl"] = "reference"
     print(json.dumps(out), flush=True)
@@ -422,7 +447,7 @@ def run_gpu_exchange(args):
         "metric": METRIC_K, "value": args.steps / (ms / 1e3), "unit": "K builds/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if best == "fp64" else "f32+f64",
-        "data": "synthetic (generated alkane geometry, seeded density)",
+        "data": f"synthetic (generated {geometry_kind()} geometry, seeded density)",
         "config": dict(WORKLOAD, path="exchange", precision=best, parallelism="replicas x1"),
         "relerr_vs_fp64": rel(K),
         "relerr_reference": "FP64 CPU oracle" if WORKLOAD.get("k_check_full", False) else "FP64 GPU path",
@@ -721,7 +746,7 @@ def run_gpu(args):
     alg_bytes = rep_best["alg_matrix_bytes"] + rep_best["alg_vector_bytes"] + 2 * 8 * nbf * nbf
     peak, peak_kind = peaks()
     achieved = alg_bytes / (ms_build / 1e3) / 1e9
-    traffic, traffic_src = read_traffic() if (best == "mixed" and WORKLOAD["n_carbon"] == 30) else (None, None)
+    traffic, traffic_src = read_traffic() if (best == "mixed" and WORKLOAD.get("n_carbon") == 30) else (None, None)
     clk = results[best]["clocks"]
 
     fp64 = None

@@ -371,14 +371,19 @@ constexpr size_t kMxSmem = (sizeof(MxSmem) + 127) & ~size_t(127);
  * ~2^-48 for FMT_F32X2; plain FP32 FMA chains roughly double it, measured
  * 1.2e-8 vs 5e-9 on C10H22). Every output element is converted to FP64 once
  * and added with FP64 atomics. */
-template <int FMT>
+template <int FMT, bool BATCH>
 __global__ void __launch_bounds__(kTileThreads, 2)
 k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ VecArgs va,
           const CUtensorMap *__restrict__ maps, unsigned *err, const BatchMol *__restrict__ mols)
 {
-    /* one structure: va; a batch (mols != nullptr): each tile's structure
-     * index is in its FP64 arena offset, which the mixed kernel never reads */
-    auto tva = [&](const Tile &t) -> const VecArgs & { return mols ? mols[t.a].va : va; };
+    /* one structure (BATCH false): va; a batch: each tile's structure index
+     * is in its FP64 arena offset, which the mixed kernel never reads. A
+     * template parameter, so that the single-structure kernel keeps its
+     * registers. */
+    auto tva = [&](const Tile &t) -> const VecArgs & {
+        if constexpr (BATCH) return mols[t.a].va;
+        else return va;
+    };
     constexpr int EB = FmtInfo<FMT>::ebytes;
     constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage: 64 or 32   */
     constexpr int RB = kTileCols * EB;                    /* bytes per stage row        */
@@ -1236,8 +1241,10 @@ static int build_rep(H2ERI_p h, DevRep *d)
     *d->err_flag = 0;
     CUDA_TRY(cudaHostGetDevicePointer((void **)&d->err_flag_dev, d->err_flag, 0));
     CUDA_TRY(cudaFuncSetAttribute(k_tile<FMT_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemLaunch));
-    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
-    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
     {
         int rc = mma_init(d);
         if (rc) return rc;
@@ -1408,9 +1415,9 @@ static void launch_range(const DevRep *d, const Range &r, const VecArgs &va, int
             const int n = std::min(kMaxGridY, r.count - f);
             dim3 g2(nvec, d->cfg.tiles_per_cta == 1 ? n : (n + 1) / 2);
             if (r.pair)
-                k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev, nullptr);
+                k_tile_mx<FMT_F32X2, false><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev, nullptr);
             else
-                k_tile_mx<FMT_F32><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev, nullptr);
+                k_tile_mx<FMT_F32, false><<<g2, kTileThreads, kMxSmem, s>>>(t, n, va, maps, d->err_flag_dev, nullptr);
         }
     }
 }
@@ -1429,9 +1436,9 @@ void launch_batch_mx(const Tile *tiles, int count, bool pair, const void *maps, 
         dim3 g2(nvec, tiles_per_cta == 1 ? n : (n + 1) / 2);
         const CUtensorMap *m = reinterpret_cast<const CUtensorMap *>(maps);
         if (pair)
-            k_tile_mx<FMT_F32X2><<<g2, kTileThreads, kMxSmem, s>>>(tiles + f, n, none, m, err, mols);
+            k_tile_mx<FMT_F32X2, true><<<g2, kTileThreads, kMxSmem, s>>>(tiles + f, n, none, m, err, mols);
         else
-            k_tile_mx<FMT_F32><<<g2, kTileThreads, kMxSmem, s>>>(tiles + f, n, none, m, err, mols);
+            k_tile_mx<FMT_F32, true><<<g2, kTileThreads, kMxSmem, s>>>(tiles + f, n, none, m, err, mols);
     }
 }
 

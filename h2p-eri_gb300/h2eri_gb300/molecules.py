@@ -140,40 +140,3 @@ def methane_cluster_coords(shape=(4, 4, 3), spacing=4.0, jitter=0.2, seed=5000, 
 def write_methane_cluster(path, shape=(4, 4, 3), spacing=4.0, jitter=0.2, seed=5000):
     syms, xyz = methane_cluster_coords(shape, spacing, jitter, seed)
     return write_mol(path, syms, xyz)
-
-
-def _random_rotation(rng):
-    """A uniformly random rotation matrix (normalised Gaussian quaternion)."""
-    q = rng.standard_normal(4)
-    a, b, c, d = q / np.linalg.norm(q)
-    return np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
-                     [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
-                     [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
-
-
-def methane_cluster_coords(shape=(4, 4, 3), spacing=4.0, jitter=0.2, seed=5000, ch=1.09):
-    """A 3-D cluster of CH4 molecules (Angstrom): one molecule per site of a
-    cubic lattice of `shape` with `spacing` (4.0 A: liquid methane, 0.42
-    g/cm^3, 63.4 A^3 per molecule), each centre moved by a uniform jitter in
-    [-jitter, jitter] per axis and each molecule turned by a random rotation
-    (numpy default_rng(seed)); tetrahedral CH4 with C-H = ch. It stands in for
-    a water cluster where no oxygen basis data is available: the same 3-D
-    neighbourhood structure (every molecule surrounded on all sides) with the
-    C and H cc-pVDZ shells. 48 molecules give 1680 Cartesian basis functions.
-    Returns (symbols, coords[natom, 3]), carbons first."""
-    rng = np.random.default_rng(seed)
-    tet = np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], dtype=np.float64) / math.sqrt(3.0) * ch
-    cs, hs = [], []
-    for i in range(shape[0]):
-        for j in range(shape[1]):
-            for k in range(shape[2]):
-                c = np.array([i, j, k], dtype=np.float64) * spacing + rng.uniform(-jitter, jitter, 3)
-                R = _random_rotation(rng)
-                cs.append(c)
-                hs.extend(c + R @ t for t in tet)
-    return ["C"] * len(cs) + ["H"] * len(hs), np.array(cs + hs)
-
-
-def write_methane_cluster(path, shape=(4, 4, 3), spacing=4.0, jitter=0.2, seed=5000):
-    syms, xyz = methane_cluster_coords(shape, spacing, jitter, seed)
-    return write_mol(path, syms, xyz)
