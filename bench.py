@@ -637,7 +637,6 @@ def run_gpu(args):
     t_up = time.perf_counter()
     h.upload()
     upload_s = time.perf_counter() - t_up
-    launches_per_J = int(h.report()["launches_per_matvec"]) + 2
 
     modes = [] if args.precision == "mixed" else ["fp64"]
     if args.precision in ("auto", "mixed"):
@@ -693,6 +692,10 @@ def run_gpu(args):
     n16 = 16
     ms16, J16, clk16 = device_run(best, n16)
     L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if best == "mixed" else hg.FP64)
+    # kernels per single-density J build with the choices in use: the H2
+    # matvec's launches plus the uncontract and contract kernels
+    rep_best = h.report()
+    launches_per_J = int(rep_best["launches_per_matvec"]) + 2
 
     # e2e: the reference's own entry point with page-locked host buffers
     # (density read from and J written to host memory by the kernels)
@@ -787,7 +790,9 @@ def run_gpu(args):
                 "relerr_vs_fp64_oracle": max(rel(Je2e[i], i) for i in sample)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_source": traffic_src,
-                     "kernel": "tile kernels k_tile_mx (all launches of one J build, timed as the step / builds)",
+                     "kernel": ("persistent tile kernel k_tile_px (one launch per J build, timed as the step / "
+                                "builds)" if rep_best["persist"] and best == "mixed" else
+                                "tile kernels k_tile_mx (all launches of one J build, timed as the step / builds)"),
                      "alg_bytes_per_build": alg_bytes, "peak_kind": peak_kind},
         "cpu_baseline": {"value": cpu_v, "unit": "J builds/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": f"{cpu_n} J builds of the workload in {cpu_dt:.1f} s (oracle, OpenMP)"},

@@ -87,6 +87,36 @@ struct TuneCfg {
     int nf_concurrent = 1;     /* near-field lanes on their own streams (1) or one stream (0)       */
     int mma_min_vec = 2;       /* densities per launch from which the tensor-core kernel runs       */
     int mma_grid_div = 1;      /* tensor-core launches use n_SM / mma_grid_div CTAs                  */
+    int persist = 1;           /* mixed single-density path: one persistent launch (1) or a launch  */
+                               /* per range on the stream lanes (0)                                 */
+};
+
+/* One work item of the persistent mixed-mode kernel: a tile of the plan for
+ * one vector, the range (group) whose completion counter it advances, the
+ * range that must be complete before it reads its input vectors (-1: none)
+ * and the storage format of its matrix. */
+struct PItem {
+    int32_t tile;
+    int16_t group, dep;
+    int16_t v, fmt;
+    int32_t pad_;
+};
+static_assert(sizeof(PItem) == 16, "work item layout");
+
+/* Work list of the persistent kernel for one vector count: the items in
+ * claim order, the item count of every range, and the control words
+ * (ticket, abort flag, per-range completion counters), zeroed before each
+ * launch. */
+struct PxPlan {
+    PItem *items = nullptr;
+    int n_items = 0;
+    int *gneed = nullptr;
+    int n_groups = 0;
+    int *ctl = nullptr;
+    int ctl_ints = 0;
+    int nvec = 0;
+    int grid = 0;
+    double sim_ms = 0.0;   /* makespan of the host schedule simulation */
 };
 
 /* Storage formats of the stored matrices. */
@@ -196,6 +226,7 @@ struct DevRep {
     std::vector<Range> mfwd, mmid, mbwd, mden;
     int mma_levels = 5;          /* slice levels of the multi-density kernel (4 or 5) */
     int n_sm = 0;
+    PxPlan px;                   /* persistent kernel's work list (mixed mode, built on first use) */
     /* the products behind every range of fwd, mid, bwd, den (same order), for re-planning */
     std::vector<std::vector<PlanRec>> rec_fwd, rec_mid, rec_bwd, rec_den;
     TuneCfg cfg;                 /* launch choices (autotuned or default) */

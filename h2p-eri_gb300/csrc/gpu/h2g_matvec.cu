@@ -23,7 +23,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
+#include <queue>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -347,6 +349,192 @@ struct MxSmem {
 };
 constexpr size_t kMxSmem = (sizeof(MxSmem) + 127) & ~size_t(127);
 
+/* One stage of a tile in the mixed-mode kernels (FP32 formats): the stage
+ * in ring slot `slot` holds rows [k SR, k SR + SR) of tile t (SR = 64 rows
+ * of single floats or 32 rows of float pairs). N side: out0 += A x0 over the
+ * stage's rows (lane per row, one box per warp, box partials merged by the
+ * last warp of the row group); T side: the column sums over the stage's rows
+ * are folded into the warp's float-pair accumulators ch / cl, which are
+ * reduced and added to out1 after the tile's last stage (`last`). Products
+ * are accumulated in anchored chains (h2g_farith.cuh). */
+template <int FMT>
+__device__ __forceinline__ void mx_stage(MxSmem &sm, int slot, const Tile &t, const MxInputs &X, int k, bool last,
+                                         double *out0, double *out1, float2 (&ch)[2], float2 (&cl)[2])
+{
+    constexpr int EB = FmtInfo<FMT>::ebytes;
+    constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage: 64 or 32   */
+    constexpr int RB = kTileCols * EB;                    /* bytes per stage row        */
+    constexpr int NB = RB / kTmaBoxBytes;                 /* boxes per stage: 4 or 8    */
+    constexpr int BOXB = SR * kTmaBoxBytes;               /* bytes per box              */
+    constexpr int NG = SR / 32;                           /* N-side 32-row groups       */
+    constexpr int NCG = 8 / NG;                           /* boxes (warps) per group    */
+    static_assert(NCG == NB, "one box per N-side warp");
+    constexpr int TC = (FMT == FMT_F32) ? 4 : 8;          /* T side: chunks per warp row */
+    constexpr int TL = 32 / TC;                           /* T side: row lanes          */
+    constexpr int TR = SR / TL;                           /* T side: rows per lane      */
+    static_assert(TR == 8, "T-side lane layout");
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ng = warp % NG, cg = warp / NG;
+    const int tb = (FMT == FMT_F32) ? warp >> 1 : warp;                 /* T side: box      */
+    /* T side: chunk and row lane. A 16-byte load is served per quarter warp
+     * (8 lanes), which must hit 8 different chunk positions: with 4 chunks
+     * per row lane (single floats) a quarter warp takes rows r and r + 4,
+     * whose swizzles map the 4 chunks to the two halves of the line. */
+    const int tq = ((FMT == FMT_F32) ? (warp & 1) * 4 : 0) + lane % TC;
+    const int trl = (FMT == FMT_F32) ? (lane >> 3) + 4 * ((lane >> 2) & 1) : lane / TC;
+    const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
+    const unsigned char *buf = sm.ring[slot];
+    const int nr = t.nr;
+    if (opN && k * SR + ng * 32 < nr) {
+        /* the lane's row over one box: two anchored chains (even and odd
+         * columns), bounded by their own sums |a| |xh| */
+        const int rr = ng * 32 + lane;
+        const unsigned char *rowp = buf + cg * BOXB + rr * kTmaBoxBytes;
+        float4 q[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) q[j] = *reinterpret_cast<const float4 *>(rowp + 16 * (j ^ (rr & 7)));
+        float2 b0 = make_float2(0.f, 0.f), b1 = b0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int cc = cg * 8 + j;
+            if (FMT == FMT_F32) {
+                const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
+                b0 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(make_float2(xh.x, xh.y)), b0);
+                b1 = pk_fma(pk_abs(make_float2(q[j].z, q[j].w)), pk_abs(make_float2(xh.z, xh.w)), b1);
+            } else {
+                const float2 xh = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
+                if (j & 1) b1 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(xh), b1);
+                else b0 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(xh), b0);
+            }
+        }
+        /* two chains per half on one anchor (bounded by both): their high
+         * parts are multiples of one ulp below 2^(k-2) and add exactly */
+        const float2 s0 = anchor2(pk_add(b0, b1)), z = make_float2(0.f, 0.f);
+        float2 sa = s0, sb = s0, la1 = z, la2 = z, lb1 = z, lb2 = z;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int cc = cg * 8 + j;
+            if (FMT == FMT_F32) {
+                const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
+                const float4 xl = *reinterpret_cast<const float4 *>(X.x0l + 4 * cc);
+                pk_aacc1(sa, la1, la2, make_float2(q[j].x, q[j].y), make_float2(xh.x, xh.y), make_float2(xl.x, xl.y));
+                pk_aacc1(sb, lb1, lb2, make_float2(q[j].z, q[j].w), make_float2(xh.z, xh.w), make_float2(xl.z, xl.w));
+            } else {
+                const float2 xh = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
+                const float2 xl = *reinterpret_cast<const float2 *>(X.x0l + 2 * cc);
+                if (j & 1) pk_aacc2(sb, lb1, lb2, make_float2(q[j].x, q[j].y), make_float2(q[j].z, q[j].w), xh, xl);
+                else pk_aacc2(sa, la1, la2, make_float2(q[j].x, q[j].y), make_float2(q[j].z, q[j].w), xh, xl);
+            }
+        }
+        const float2 hi = pk_add(pk_sub(sa, s0), pk_sub(sb, s0));   /* exact */
+        const float2 lo = pk_add(pk_add(la1, la2), pk_add(lb1, lb2));
+        float h = hi.x, l = lo.x;
+        dfadd(h, l, hi.y, lo.y);
+        sm.npart[slot][cg * SR + rr] = make_float2(h, l);
+    }
+
+    if (opT) {
+        /* the lane's chunk over rows trl + TL i of the stage: anchored
+         * chains per column, folded into the tile's float-pair column
+         * sums once per stage. Rows past the tile have zero inputs. */
+        float4 q[TR];
+#pragma unroll
+        for (int i = 0; i < TR; i++) {
+            const int rr = trl + TL * i;
+            q[i] = *reinterpret_cast<const float4 *>(buf + tb * BOXB + rr * kTmaBoxBytes + 16 * (tq ^ (rr & 7)));
+        }
+        const float *x1h = X.x1h + k * SR + trl, *x1l = X.x1l + k * SR + trl;
+        float2 b0 = make_float2(0.f, 0.f), b1 = b0;
+#pragma unroll
+        for (int i = 0; i < TR; i++) {
+            const float2 xa = bcast(fabsf(x1h[TL * i]));
+            if (FMT == FMT_F32) {
+                b0 = pk_fma(pk_abs(make_float2(q[i].x, q[i].y)), xa, b0);
+                b1 = pk_fma(pk_abs(make_float2(q[i].z, q[i].w)), xa, b1);
+            } else {
+                b0 = pk_fma(pk_abs(make_float2(q[i].x, q[i].y)), xa, b0);
+            }
+        }
+        if (FMT == FMT_F32) {
+            const float2 s0 = anchor2(b0), s1 = anchor2(b1), z = make_float2(0.f, 0.f);
+            float2 sa = s0, sb = s1, la1 = z, la2 = z, lb1 = z, lb2 = z;
+#pragma unroll
+            for (int i = 0; i < TR; i++) {
+                const float2 xh = bcast(x1h[TL * i]), xl = bcast(x1l[TL * i]);
+                pk_aacc1(sa, la1, la2, make_float2(q[i].x, q[i].y), xh, xl);
+                pk_aacc1(sb, lb1, lb2, make_float2(q[i].z, q[i].w), xh, xl);
+            }
+            pk_dfadd(ch[0], cl[0], pk_sub(sa, s0), pk_add(la1, la2));
+            pk_dfadd(ch[1], cl[1], pk_sub(sb, s1), pk_add(lb1, lb2));
+        } else {
+            /* two chains over alternate rows on one anchor: their high
+             * parts are multiples of one ulp below 2^(k-2), so they add
+             * exactly */
+            const float2 s0 = anchor2(b0), z = make_float2(0.f, 0.f);
+            float2 sa = s0, sb = s0, la1 = z, la2 = z, lb1 = z, lb2 = z;
+#pragma unroll
+            for (int i = 0; i < TR; i += 2) {
+                const float2 xh0 = bcast(x1h[TL * i]), xl0 = bcast(x1l[TL * i]);
+                const float2 xh1 = bcast(x1h[TL * (i + 1)]), xl1 = bcast(x1l[TL * (i + 1)]);
+                pk_aacc2(sa, la1, la2, make_float2(q[i].x, q[i].y), make_float2(q[i].z, q[i].w), xh0, xl0);
+                pk_aacc2(sb, lb1, lb2, make_float2(q[i + 1].x, q[i + 1].y), make_float2(q[i + 1].z, q[i + 1].w), xh1,
+                         xl1);
+            }
+            pk_dfadd(ch[0], cl[0], pk_add(pk_sub(sa, s0), pk_sub(sb, s0)),
+                     pk_add(pk_add(la1, la2), pk_add(lb1, lb2)));
+        }
+        if (last) {
+            /* tile done: reduce the column sums over the row lanes */
+#pragma unroll
+            for (int off = TC; off < 32; off <<= 1)
+#pragma unroll
+                for (int j = 0; j < (FMT == FMT_F32 ? 2 : 1); j++) {
+                    const float2 oh = make_float2(__shfl_xor_sync(0xffffffffu, ch[j].x, off),
+                                                  __shfl_xor_sync(0xffffffffu, ch[j].y, off));
+                    const float2 ol = make_float2(__shfl_xor_sync(0xffffffffu, cl[j].x, off),
+                                                  __shfl_xor_sync(0xffffffffu, cl[j].y, off));
+                    pk_dfadd(ch[j], cl[j], oh, ol);
+                }
+            if (trl == 0) {
+                if (FMT == FMT_F32) {
+                    const int c = tb * 32 + tq * 4;
+                    if (c < t.nc) atomic_add_pair(out1 + c, ch[0].x, cl[0].x);
+                    if (c + 1 < t.nc) atomic_add_pair(out1 + c + 1, ch[0].y, cl[0].y);
+                    if (c + 2 < t.nc) atomic_add_pair(out1 + c + 2, ch[1].x, cl[1].x);
+                    if (c + 3 < t.nc) atomic_add_pair(out1 + c + 3, ch[1].y, cl[1].y);
+                } else {
+                    const int c = tb * 16 + tq * 2;
+                    if (c < t.nc) atomic_add_pair(out1 + c, ch[0].x, cl[0].x);
+                    if (c + 1 < t.nc) atomic_add_pair(out1 + c + 1, ch[0].y, cl[0].y);
+                }
+            }
+        }
+    }
+
+    __syncwarp();
+    if (opN) {
+        /* the last warp of the row group merges the group's box partials */
+        int last = 0;
+        if (lane == 0) {
+            __threadfence_block();
+            last = atomicAdd(&sm.grp_cnt[slot][ng], 1) == NCG - 1;
+        }
+        if (__shfl_sync(0xffffffffu, last, 0)) {
+            __threadfence_block();
+            const int rr = ng * 32 + lane, grow = k * SR + rr;
+            if (grow < nr) {
+                const float2 *P = sm.npart[slot];
+                float h = P[rr].x, l = P[rr].y;
+#pragma unroll
+                for (int q = 1; q < NCG; q++) dfadd(h, l, P[q * SR + rr].x, P[q * SR + rr].y);
+                atomic_add_pair(out0 + grow, h, l);
+            }
+            if (lane == 0) sm.grp_cnt[slot][ng] = 0;
+        }
+        __syncwarp();
+    }
+}
+
 /* Mixed-mode tile kernel (FP32 formats), two tiles per CTA. Stages arrive
  * by TMA as NB swizzled boxes of SR rows x 128 bytes (16-byte chunk q of box
  * row r at q ^ (r & 7)) into a kStages-deep ring that runs across both
@@ -380,9 +568,9 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
      * is in its FP64 arena offset, which the mixed kernel never reads. A
      * template parameter, so that the single-structure kernel keeps its
      * registers. */
-    auto tva = [&](const Tile &t) -> const VecArgs & {
-        if constexpr (BATCH) return mols[t.a].va;
-        else return va;
+    auto vp = [&](const Tile &t, uint8_t kind, int off) -> double * {
+        if constexpr (BATCH) return vec_ptr(mols[t.a].va, kind, off, (int)blockIdx.x);
+        else return vec_ptr(va, kind, off, (int)blockIdx.x);
     };
     constexpr int EB = FmtInfo<FMT>::ebytes;
     constexpr int SR = kStageBytes / (kTileCols * EB);   /* rows per stage: 64 or 32   */
@@ -390,24 +578,17 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
     constexpr int NB = RB / kTmaBoxBytes;                 /* boxes per stage: 4 or 8    */
     constexpr int BOXB = SR * kTmaBoxBytes;               /* bytes per box              */
     constexpr int BOXW = kTmaBoxBytes / EB;               /* elements per box row       */
-    constexpr int NG = SR / 32;                           /* N-side 32-row groups       */
-    constexpr int NCG = 8 / NG;                           /* boxes (warps) per group    */
-    static_assert(NCG == NB, "one box per N-side warp");
     constexpr int NW = kTileThreads / 32;
-    constexpr int TC = (FMT == FMT_F32) ? 4 : 8;          /* T side: chunks per warp row */
-    constexpr int TL = 32 / TC;                           /* T side: row lanes          */
-    constexpr int TR = SR / TL;                           /* T side: rows per lane      */
-    static_assert(TR == 8, "T-side lane layout");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     MxSmem &sm = *reinterpret_cast<MxSmem *>(smem_raw);
     volatile int *dead = &sm.dead;
 
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, lane = tid & 31;
     if (smem_addr(sm.ring) & 1023u) {   /* the same for every thread: nothing has started */
         if (tid == 0) atomicOr(err, 2u);
         return;
     }
-    const int v = blockIdx.x, G = gridDim.y;
+    const int G = gridDim.y;   /* vector: blockIdx.x */
     const int ti0 = blockIdx.y, ti1 = blockIdx.y + G;
     const int ntl = ti1 < n_tiles ? 2 : 1;
     const Tile tA = tiles[ti0];
@@ -450,26 +631,18 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
         const bool n0 = t.k_out0 != VK_NONE, n1 = t.k_out1 != VK_NONE;
         if (tid < kTileCols) {
             float h = 0.f, l = 0.f;
-            if (n0 && tid < t.nc) split(vec_ptr(tva(t), t.k_in0, t.in0, v)[tid], h, l);
+            if (n0 && tid < t.nc) split(vp(t, t.k_in0, t.in0)[tid], h, l);
             X.x0h[tid] = h; X.x0l[tid] = l;
         }
         if (n1)
             for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
                 float h = 0.f, l = 0.f;
-                if (r < t.nr) split(vec_ptr(tva(t), t.k_in1, t.in1, v)[r], h, l);
+                if (r < t.nr) split(vp(t, t.k_in1, t.in1)[r], h, l);
                 X.x1h[r] = h; X.x1l[r] = l;
             }
     }
     __syncthreads();   /* inputs, barriers and counters ready; the only CTA-wide barrier */
 
-    const int ng = warp % NG, cg = warp / NG;
-    const int tb = (FMT == FMT_F32) ? warp >> 1 : warp;                 /* T side: box      */
-    /* T side: chunk and row lane. A 16-byte load is served per quarter warp
-     * (8 lanes), which must hit 8 different chunk positions: with 4 chunks
-     * per row lane (single floats) a quarter warp takes rows r and r + 4,
-     * whose swizzles map the 4 chunks to the two halves of the line. */
-    const int tq = ((FMT == FMT_F32) ? (warp & 1) * 4 : 0) + lane % TC;
-    const int trl = (FMT == FMT_F32) ? (lane >> 3) + 4 * ((lane >> 2) & 1) : lane / TC;
     float2 ch[2], cl[2];
     int lost = -1;
     for (int g = 0; g < S; g++) {
@@ -485,158 +658,10 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
             lost = g;
         }
         if (k == 0) ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
-        const unsigned char *buf = sm.ring[slot];
-        const int nr = t.nr;
-
-        if (opN && k * SR + ng * 32 < nr) {
-            /* the lane's row over one box: two anchored chains (even and odd
-             * columns), bounded by their own sums |a| |xh| */
-            const int rr = ng * 32 + lane;
-            const unsigned char *rowp = buf + cg * BOXB + rr * kTmaBoxBytes;
-            float4 q[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) q[j] = *reinterpret_cast<const float4 *>(rowp + 16 * (j ^ (rr & 7)));
-            float2 b0 = make_float2(0.f, 0.f), b1 = b0;
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int cc = cg * 8 + j;
-                if (FMT == FMT_F32) {
-                    const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
-                    b0 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(make_float2(xh.x, xh.y)), b0);
-                    b1 = pk_fma(pk_abs(make_float2(q[j].z, q[j].w)), pk_abs(make_float2(xh.z, xh.w)), b1);
-                } else {
-                    const float2 xh = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
-                    if (j & 1) b1 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(xh), b1);
-                    else b0 = pk_fma(pk_abs(make_float2(q[j].x, q[j].y)), pk_abs(xh), b0);
-                }
-            }
-            /* two chains per half on one anchor (bounded by both): their high
-             * parts are multiples of one ulp below 2^(k-2) and add exactly */
-            const float2 s0 = anchor2(pk_add(b0, b1)), z = make_float2(0.f, 0.f);
-            float2 sa = s0, sb = s0, la1 = z, la2 = z, lb1 = z, lb2 = z;
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int cc = cg * 8 + j;
-                if (FMT == FMT_F32) {
-                    const float4 xh = *reinterpret_cast<const float4 *>(X.x0h + 4 * cc);
-                    const float4 xl = *reinterpret_cast<const float4 *>(X.x0l + 4 * cc);
-                    pk_aacc1(sa, la1, la2, make_float2(q[j].x, q[j].y), make_float2(xh.x, xh.y), make_float2(xl.x, xl.y));
-                    pk_aacc1(sb, lb1, lb2, make_float2(q[j].z, q[j].w), make_float2(xh.z, xh.w), make_float2(xl.z, xl.w));
-                } else {
-                    const float2 xh = *reinterpret_cast<const float2 *>(X.x0h + 2 * cc);
-                    const float2 xl = *reinterpret_cast<const float2 *>(X.x0l + 2 * cc);
-                    if (j & 1) pk_aacc2(sb, lb1, lb2, make_float2(q[j].x, q[j].y), make_float2(q[j].z, q[j].w), xh, xl);
-                    else pk_aacc2(sa, la1, la2, make_float2(q[j].x, q[j].y), make_float2(q[j].z, q[j].w), xh, xl);
-                }
-            }
-            const float2 hi = pk_add(pk_sub(sa, s0), pk_sub(sb, s0));   /* exact */
-            const float2 lo = pk_add(pk_add(la1, la2), pk_add(lb1, lb2));
-            float h = hi.x, l = lo.x;
-            dfadd(h, l, hi.y, lo.y);
-            sm.npart[slot][cg * SR + rr] = make_float2(h, l);
-        }
-
-        if (opT) {
-            /* the lane's chunk over rows trl + TL i of the stage: anchored
-             * chains per column, folded into the tile's float-pair column
-             * sums once per stage. Rows past the tile have zero inputs. */
-            float4 q[TR];
-#pragma unroll
-            for (int i = 0; i < TR; i++) {
-                const int rr = trl + TL * i;
-                q[i] = *reinterpret_cast<const float4 *>(buf + tb * BOXB + rr * kTmaBoxBytes + 16 * (tq ^ (rr & 7)));
-            }
-            const float *x1h = X.x1h + k * SR + trl, *x1l = X.x1l + k * SR + trl;
-            float2 b0 = make_float2(0.f, 0.f), b1 = b0;
-#pragma unroll
-            for (int i = 0; i < TR; i++) {
-                const float2 xa = bcast(fabsf(x1h[TL * i]));
-                if (FMT == FMT_F32) {
-                    b0 = pk_fma(pk_abs(make_float2(q[i].x, q[i].y)), xa, b0);
-                    b1 = pk_fma(pk_abs(make_float2(q[i].z, q[i].w)), xa, b1);
-                } else {
-                    b0 = pk_fma(pk_abs(make_float2(q[i].x, q[i].y)), xa, b0);
-                }
-            }
-            if (FMT == FMT_F32) {
-                const float2 s0 = anchor2(b0), s1 = anchor2(b1), z = make_float2(0.f, 0.f);
-                float2 sa = s0, sb = s1, la1 = z, la2 = z, lb1 = z, lb2 = z;
-#pragma unroll
-                for (int i = 0; i < TR; i++) {
-                    const float2 xh = bcast(x1h[TL * i]), xl = bcast(x1l[TL * i]);
-                    pk_aacc1(sa, la1, la2, make_float2(q[i].x, q[i].y), xh, xl);
-                    pk_aacc1(sb, lb1, lb2, make_float2(q[i].z, q[i].w), xh, xl);
-                }
-                pk_dfadd(ch[0], cl[0], pk_sub(sa, s0), pk_add(la1, la2));
-                pk_dfadd(ch[1], cl[1], pk_sub(sb, s1), pk_add(lb1, lb2));
-            } else {
-                /* two chains over alternate rows on one anchor: their high
-                 * parts are multiples of one ulp below 2^(k-2), so they add
-                 * exactly */
-                const float2 s0 = anchor2(b0), z = make_float2(0.f, 0.f);
-                float2 sa = s0, sb = s0, la1 = z, la2 = z, lb1 = z, lb2 = z;
-#pragma unroll
-                for (int i = 0; i < TR; i += 2) {
-                    const float2 xh0 = bcast(x1h[TL * i]), xl0 = bcast(x1l[TL * i]);
-                    const float2 xh1 = bcast(x1h[TL * (i + 1)]), xl1 = bcast(x1l[TL * (i + 1)]);
-                    pk_aacc2(sa, la1, la2, make_float2(q[i].x, q[i].y), make_float2(q[i].z, q[i].w), xh0, xl0);
-                    pk_aacc2(sb, lb1, lb2, make_float2(q[i + 1].x, q[i + 1].y), make_float2(q[i + 1].z, q[i + 1].w), xh1,
-                             xl1);
-                }
-                pk_dfadd(ch[0], cl[0], pk_add(pk_sub(sa, s0), pk_sub(sb, s0)),
-                         pk_add(pk_add(la1, la2), pk_add(lb1, lb2)));
-            }
-            if (k == (b ? nsB : nsA) - 1) {
-                /* tile done: reduce the column sums over the row lanes */
-#pragma unroll
-                for (int off = TC; off < 32; off <<= 1)
-#pragma unroll
-                    for (int j = 0; j < (FMT == FMT_F32 ? 2 : 1); j++) {
-                        const float2 oh = make_float2(__shfl_xor_sync(0xffffffffu, ch[j].x, off),
-                                                      __shfl_xor_sync(0xffffffffu, ch[j].y, off));
-                        const float2 ol = make_float2(__shfl_xor_sync(0xffffffffu, cl[j].x, off),
-                                                      __shfl_xor_sync(0xffffffffu, cl[j].y, off));
-                        pk_dfadd(ch[j], cl[j], oh, ol);
-                    }
-                if (trl == 0) {
-                    double *out1 = vec_ptr(tva(t), t.k_out1, t.out1, v);
-                    if (FMT == FMT_F32) {
-                        const int c = tb * 32 + tq * 4;
-                        if (c < t.nc) atomic_add_pair(out1 + c, ch[0].x, cl[0].x);
-                        if (c + 1 < t.nc) atomic_add_pair(out1 + c + 1, ch[0].y, cl[0].y);
-                        if (c + 2 < t.nc) atomic_add_pair(out1 + c + 2, ch[1].x, cl[1].x);
-                        if (c + 3 < t.nc) atomic_add_pair(out1 + c + 3, ch[1].y, cl[1].y);
-                    } else {
-                        const int c = tb * 16 + tq * 2;
-                        if (c < t.nc) atomic_add_pair(out1 + c, ch[0].x, cl[0].x);
-                        if (c + 1 < t.nc) atomic_add_pair(out1 + c + 1, ch[0].y, cl[0].y);
-                    }
-                }
-            }
-        }
-
-        __syncwarp();
-        if (opN) {
-            /* the last warp of the row group merges the group's box partials */
-            int last = 0;
-            if (lane == 0) {
-                __threadfence_block();
-                last = atomicAdd(&sm.grp_cnt[slot][ng], 1) == NCG - 1;
-            }
-            if (__shfl_sync(0xffffffffu, last, 0)) {
-                __threadfence_block();
-                const int rr = ng * 32 + lane, grow = k * SR + rr;
-                if (grow < nr) {
-                    const float2 *P = sm.npart[slot];
-                    float h = P[rr].x, l = P[rr].y;
-#pragma unroll
-                    for (int q = 1; q < NCG; q++) dfadd(h, l, P[q * SR + rr].x, P[q * SR + rr].y);
-                    atomic_add_pair(vec_ptr(tva(t), t.k_out0, t.out0, v) + grow, h, l);
-                }
-                if (lane == 0) sm.grp_cnt[slot][ng] = 0;
-            }
-            __syncwarp();
-        }
+        const bool last = k == (b ? nsB : nsA) - 1;
+        double *out0 = opN ? vp(t, t.k_out0, t.out0) : nullptr;
+        double *out1 = opT ? vp(t, t.k_out1, t.out1) : nullptr;
+        mx_stage<FMT>(sm, slot, t, X, k, last, out0, out1, ch, cl);
         /* release the slot; the last warp out reloads it kStages stages ahead */
         if (lane == 0) {
             __threadfence_block();
@@ -648,6 +673,220 @@ k_tile_mx(const Tile *__restrict__ tiles, int n_tiles, const __grid_constant__ V
             }
         }
     }
+    if (lost >= 0) (void)mbar_wait(smem_addr(&sm.full[lost % kStages]), (unsigned)((lost / kStages) & 1));
+}
+
+/* ---- persistent mixed-mode kernel ---- */
+
+/* Shared memory of k_tile_px: the ring, partials and inputs of k_tile_mx
+ * first (so the ring keeps its 1024-byte alignment), then the CTA's item
+ * window: up to four claimed items (ring indexed by claim order) with their
+ * tiles and stage ranges, and the issue state of the stage sequence that
+ * runs across items. */
+struct PxSmem {
+    MxSmem m;
+    Tile tl[4];
+    PItem it[4];
+    int gs[4], ns[4];   /* first stage (CTA sequence) and stage count of each item */
+    int n_known;        /* items claimed so far                                    */
+    int exhausted;      /* the queue is empty                                      */
+    int stage_end;      /* end of the stage sequence of the claimed items          */
+    int ip, ip_item;    /* next stage to issue and its item                        */
+};
+constexpr size_t kPxSmem = (sizeof(PxSmem) + 127) & ~size_t(127);
+static_assert(2 * (kPxSmem + 1024) <= 233472, "two persistent CTAs per SM (228 KB, 1 KB reserved per CTA)");
+constexpr int kPxDone = 32;                        /* ctl[kPxDone + g]: items of range g done */
+
+__device__ __forceinline__ int ld_acquire_gpu(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+/* Persistent mixed-mode tile kernel (FP32 formats): the whole H2 matvec in
+ * one launch. CTAs take items (one tile for one vector) from a queue in a
+ * fixed order (ctl[0] is the next ticket) until it is empty; the order is
+ * topological for the dependencies between ranges (upward levels, coupling
+ * stages, downward levels on the tree chain; the near-field stages on their
+ * lanes), so an item waits only for items with smaller tickets. Before an
+ * item's input vectors are read, the range it depends on must be complete
+ * (ctl[kPxDone + dep] == gneed[dep]); after its last stage, every thread
+ * fences its output atomics and thread 0 counts the item in its range.
+ *
+ * Deadlock freedom: a CTA claims its next item only after the dependency
+ * of its current item is met, so each CTA holds at most one item that is
+ * still waiting, and that item waits only for smaller tickets; by induction
+ * on the smallest unfinished ticket, every item completes. CTAs need not be
+ * co-resident (a CTA that has not started holds no ticket). Every wait is
+ * bounded: a dependency wait longer than dep_limit cycles sets error bit 4
+ * and ctl[1], which makes every other CTA stop waiting, and the results are
+ * invalid.
+ *
+ * The stage ring runs across items: stages of the claimed next item are
+ * copied while the current one is multiplied. Input vectors are read
+ * through L2 (ld.global.cg): other CTAs of this launch wrote them. */
+__global__ void __launch_bounds__(kTileThreads, 2)
+k_tile_px(const Tile *__restrict__ tiles, const PItem *__restrict__ items, int n_items,
+          const int *__restrict__ gneed, int *ctl, const __grid_constant__ VecArgs va,
+          const CUtensorMap *__restrict__ maps, unsigned *err, long long dep_limit)
+{
+    constexpr int NW = kTileThreads / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PxSmem &ps = *reinterpret_cast<PxSmem *>(smem_raw);
+    MxSmem &sm = ps.m;
+    volatile int *dead = &sm.dead;
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (smem_addr(sm.ring) & 1023u) {   /* the same for every thread: nothing has started */
+        if (tid == 0) atomicOr(err, 2u);
+        return;
+    }
+
+    /* thread 0: the next ticket into the item window */
+    auto claim = [&]() {
+        if (ps.exhausted || *dead) { ps.exhausted = 1; return; }
+        const int tk = atomicAdd(&ctl[0], 1);
+        if (tk >= n_items) { ps.exhausted = 1; return; }
+        const int s = ps.n_known, e = s & 3;
+        const PItem it = items[tk];
+        ps.it[e] = it;
+        ps.tl[e] = tiles[it.tile];
+        const int sr = it.fmt == FMT_F32 ? 64 : 32;
+        ps.gs[e] = ps.stage_end;
+        ps.ns[e] = (ps.tl[e].nr + sr - 1) / sr;
+        ps.stage_end += ps.ns[e];
+        ps.n_known = s + 1;
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(maps + ps.tl[e].ld2) : "memory");
+    };
+    /* thread 0: wait until the range item s depends on is complete */
+    auto dep_wait = [&](int s) {
+        const PItem &it = ps.it[s & 3];
+        if (it.dep < 0 || *dead) return;
+        const int need = gneed[it.dep];
+        const int *ctr = ctl + kPxDone + it.dep;
+        if (ld_acquire_gpu(ctr) >= need) return;
+        const long long t0 = clock64();
+        while (ld_acquire_gpu(ctr) < need) {
+            if (ld_acquire_gpu(ctl + 1) != 0) { *dead = 1; return; }
+            if (clock64() - t0 > dep_limit) {
+                atomicOr(err, 4u);
+                atomicExch(ctl + 1, 1);
+                *dead = 1;
+                return;
+            }
+            __nanosleep(64);
+        }
+    };
+    /* one thread (no other issuer is active): copies of stages [ip, lim) of
+     * the claimed items; the slots of every stage below lim - kStages are free */
+    auto issue_upto = [&](int lim) {
+        while (ps.ip < ps.stage_end && ps.ip < lim && !*dead) {
+            int si = ps.ip_item;
+            while (ps.ip >= ps.gs[si & 3] + ps.ns[si & 3]) si++;
+            ps.ip_item = si;
+            const int e = si & 3, g = ps.ip, k = g - ps.gs[e];
+            const Tile &t = ps.tl[e];
+            const unsigned bar = smem_addr(&sm.full[g % kStages]);
+            const unsigned dst = smem_addr(sm.ring[g % kStages]);
+            const CUtensorMap *map = maps + t.ld2;
+            const int tc0 = (int)(t.a2 >> 32), tr0 = (int)(t.a2 & 0xffffffffu);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kStageBytes)
+                         : "memory");
+            if (ps.it[e].fmt == FMT_F32) {
+#pragma unroll
+                for (int bx = 0; bx < 4; bx++) tma_load_2d(dst + bx * 8192, map, tc0 + bx * 32, tr0 + k * 64, bar);
+            } else {
+#pragma unroll
+                for (int bx = 0; bx < 8; bx++) tma_load_2d(dst + bx * 4096, map, tc0 + bx * 16, tr0 + k * 32, bar);
+            }
+            ps.ip = g + 1;
+        }
+    };
+
+    if (tid == 0) {
+        for (int i = 0; i < kStages; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&sm.full[i])) : "memory");
+            sm.slot_cnt[i] = 0;
+            sm.grp_cnt[i][0] = sm.grp_cnt[i][1] = 0;
+        }
+        sm.dead = 0;
+        ps.n_known = ps.exhausted = ps.stage_end = ps.ip = ps.ip_item = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        claim();
+        if (ps.n_known > 0) {
+            dep_wait(0);
+            claim();
+            issue_upto(kStages);
+        }
+    }
+    __syncthreads();
+
+    int lost = -1;
+    for (int s = 0; s < ps.n_known; s++) {
+        const int e = s & 3;
+        const Tile &t = ps.tl[e];
+        const int fmt = ps.it[e].fmt, v = ps.it[e].v, group = ps.it[e].group;
+        MxInputs &X = sm.sx[s & 1];
+        const bool opN = t.k_out0 != VK_NONE, opT = t.k_out1 != VK_NONE;
+        /* split the input slices (the dependency was met before the barrier) */
+        if (tid < kTileCols) {
+            float h = 0.f, l = 0.f;
+            if (opN && tid < t.nc) split(__ldcg(vec_ptr(va, t.k_in0, t.in0, v) + tid), h, l);
+            X.x0h[tid] = h; X.x0l[tid] = l;
+        }
+        if (opT) {
+            const double *in1 = vec_ptr(va, t.k_in1, t.in1, v);
+            for (int r = tid; r < kChunkRows; r += kTileThreads) {   /* rows >= nr read as zero */
+                float h = 0.f, l = 0.f;
+                if (r < t.nr) split(__ldcg(in1 + r), h, l);
+                X.x1h[r] = h; X.x1l[r] = l;
+            }
+        }
+        double *out0 = opN ? vec_ptr(va, t.k_out0, t.out0, v) : nullptr;
+        double *out1 = opT ? vec_ptr(va, t.k_out1, t.out1, v) : nullptr;
+        __syncthreads();
+
+        const int g0 = ps.gs[e], ns = ps.ns[e];
+        float2 ch[2], cl[2];
+        ch[0] = ch[1] = cl[0] = cl[1] = make_float2(0.f, 0.f);
+        for (int k = 0; k < ns; k++) {
+            const int g = g0 + k, slot = g % kStages;
+            if (!*dead && !mbar_wait(smem_addr(&sm.full[slot]), (unsigned)((g / kStages) & 1))) {
+                atomicOr(err, 1u);
+                *dead = 1;
+                lost = g;
+            }
+            if (fmt == FMT_F32) mx_stage<FMT_F32>(sm, slot, t, X, k, k == ns - 1, out0, out1, ch, cl);
+            else mx_stage<FMT_F32X2>(sm, slot, t, X, k, k == ns - 1, out0, out1, ch, cl);
+            /* release the slot; the last warp out issues the stages it frees */
+            if (lane == 0) {
+                __threadfence_block();
+                if (atomicAdd(&sm.slot_cnt[slot], 1) == NW - 1) {
+                    sm.slot_cnt[slot] = 0;
+                    __threadfence_block();
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue_upto(g + kStages + 1);
+                }
+            }
+        }
+        /* the item is done once every thread's output atomics are visible */
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            atomicAdd(&ctl[kPxDone + group], 1);
+            if (s + 1 < ps.n_known) {
+                dep_wait(s + 1);
+                claim();
+            }
+            issue_upto(g0 + ns + kStages);
+        }
+        __syncthreads();
+    }
+    /* copies still in flight after an expired wait: wait for them (bounded) */
+    if (tid == 0 && *dead)
+        for (int g = max(0, ps.ip - kStages); g < ps.ip; g++)
+            (void)mbar_wait(smem_addr(&sm.full[g % kStages]), (unsigned)((g / kStages) & 1));
     if (lost >= 0) (void)mbar_wait(smem_addr(&sm.full[lost % kStages]), (unsigned)((lost / kStages) & 1));
 }
 
@@ -723,6 +962,7 @@ static std::mutex g_mu;
 static std::unordered_map<const void *, DevRep *> g_reps;
 
 static int noalloc_scratch(int dev, double **out);   /* below, with H2ERI_matvec_device_noalloc */
+static void px_free(DevRep *d);                        /* below, with the persistent kernel's work list */
 
 namespace {
 
@@ -937,6 +1177,7 @@ static void free_rep(DevRep *d)
     if (d->ev_bjoin) cudaEventDestroy(d->ev_bjoin);
     for (auto &e : d->ev_t)
         if (e) cudaEventDestroy(e);
+    px_free(d);
     free_exchange_state(d);
     batch_forget(d);
     if (cur >= 0) cudaSetDevice(cur);
@@ -1245,6 +1486,7 @@ static int build_rep(H2ERI_p h, DevRep *d)
     CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
     CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
     CUDA_TRY(cudaFuncSetAttribute(k_tile_mx<FMT_F32X2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMxSmem));
+    CUDA_TRY(cudaFuncSetAttribute(k_tile_px, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPxSmem));
     {
         int rc = mma_init(d);
         if (rc) return rc;
@@ -1324,7 +1566,27 @@ int replan_tiles(DevRep *d, int rows)
     d->tiles = nt;
     d->n_tiles = (int)all.size();
     d->tiles_host = std::move(all);
+    px_free(d);   /* the persistent kernel's work list names tiles of the old plan */
     d->cfg.chunk_rows = rows;
+    return 0;
+}
+
+/* Launch choices fixed through the environment; they take precedence over
+ * the defaults and over choices tuned earlier (applied after those):
+ *   H2G_MMA_LEVELS=4|5      slice levels of the multi-density kernel
+ *   H2G_MMA_MIN_VEC=n       densities per launch from which it runs
+ *   H2G_TILE_ROWS=128|256|512, H2G_TILES_PER_CTA=1|2
+ *   H2G_PERSIST=0|1         mixed single-density matvec as one persistent launch */
+static int apply_env_choices(DevRep *d)
+{
+    if (const char *lv = std::getenv("H2G_MMA_LEVELS")) d->mma_levels = std::atoi(lv) == 4 ? 4 : 5;
+    if (const char *mv = std::getenv("H2G_MMA_MIN_VEC")) d->cfg.mma_min_vec = std::max(2, std::atoi(mv));
+    if (const char *tr = std::getenv("H2G_TILE_ROWS")) {
+        const int rc = replan_tiles(d, std::atoi(tr));
+        if (rc) return rc;
+    }
+    if (const char *tp = std::getenv("H2G_TILES_PER_CTA")) d->cfg.tiles_per_cta = std::atoi(tp) == 1 ? 1 : 2;
+    if (const char *pp = std::getenv("H2G_PERSIST")) d->cfg.persist = std::atoi(pp) == 0 ? 0 : 1;
     return 0;
 }
 
@@ -1355,17 +1617,8 @@ int get_rep(H2ERI_p h, DevRep **out)
     int rc = build_rep(h, d);
     if (rc != 0) { free_rep(d); return rc; }
     tune_apply_cached(d);   /* launch choices tuned earlier for this shape (H2G_TUNE_FILE) */
-    /* H2G_MMA_LEVELS=4|5: slice levels of the multi-density kernel;
-     * H2G_MMA_MIN_VEC=n: densities per launch from which it runs (default 2) */
-    if (const char *lv = std::getenv("H2G_MMA_LEVELS")) d->mma_levels = std::atoi(lv) == 4 ? 4 : 5;
-    if (const char *mv = std::getenv("H2G_MMA_MIN_VEC")) d->cfg.mma_min_vec = std::max(2, std::atoi(mv));
-    /* H2G_TILE_ROWS=128|256|512, H2G_TILES_PER_CTA=1|2: fixed launch choices
-     * instead of the defaults or the tuned ones */
-    if (const char *tr = std::getenv("H2G_TILE_ROWS")) {
-        rc = replan_tiles(d, std::atoi(tr));
-        if (rc) { free_rep(d); return rc; }
-    }
-    if (const char *tp = std::getenv("H2G_TILES_PER_CTA")) d->cfg.tiles_per_cta = std::atoi(tp) == 1 ? 1 : 2;
+    rc = apply_env_choices(d);
+    if (rc) { free_rep(d); return rc; }
     /* H2G_PRECISION=mixed starts the structure in the mixed mode, for callers
      * of the reference's entry points that do not call the extensions */
     if (const char *pe = std::getenv("H2G_PRECISION")) {
@@ -1593,7 +1846,173 @@ int set_precision_mode(DevRep *d, H2ERI_p h, int mode)
     }
     const bool changed = d->precision != mode;
     d->precision = mode;
-    if (changed) tune_apply_cached(d);   /* choices tuned earlier for this shape and precision */
+    if (changed) {
+        tune_apply_cached(d);   /* choices tuned earlier for this shape and precision */
+        return apply_env_choices(d);
+    }
+    return 0;
+}
+
+/* ---- work list of the persistent kernel ---- */
+
+static void px_free(DevRep *d)
+{
+    cudaFree(d->px.items);
+    cudaFree(d->px.gneed);
+    cudaFree(d->px.ctl);
+    d->px = PxPlan();
+}
+
+/* Work list for nvec vectors: one item per (tile, vector), in the order a
+ * list-scheduling simulation of the launch claims them. The simulation runs
+ * `grid` workers, each streaming a tile at an equal share of the HBM rate
+ * plus a fixed per-item cost; when a worker is free it takes the next tile
+ * of the tree chain if that tile's preceding range is complete, else the
+ * next ready near-field tile (the lane with more work left), else whichever
+ * becomes ready first. Every queue is taken in its own order and a range's
+ * items are only placed after all items of the range it depends on, so
+ * the order is topological. */
+static int build_px(DevRep *d, int nvec)
+{
+    if (d->px.items != nullptr && d->px.nvec == nvec) return 0;
+    px_free(d);
+    int occ = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tile_px, kTileThreads, kPxSmem));
+    if (occ < 1) {
+        set_error("persistent tile kernel: no CTA fits on an SM");
+        return 10;
+    }
+    /* ranges: the tree chain, then the near-field lanes */
+    struct Grp { const Range *r; int dep; int queue; };
+    std::vector<Grp> grp;
+    int prev = -1;
+    for (const std::vector<Range> *v : {&d->fwd, &d->mid, &d->bwd})
+        for (const Range &r : *v) {
+            if (r.count == 0) continue;
+            grp.push_back({&r, prev, 0});
+            prev = (int)grp.size() - 1;
+        }
+    int lane_prev[kNfLanes];
+    for (int &x : lane_prev) x = -1;
+    for (const Range &r : d->den) {
+        if (r.count == 0) continue;
+        const int ln = std::min(std::max(r.lane, 0), kNfLanes - 1);
+        grp.push_back({&r, lane_prev[ln], 1 + ln});
+        lane_prev[ln] = (int)grp.size() - 1;
+    }
+    const int ng = (int)grp.size();
+    if (ng > 32000) { set_error("persistent tile kernel: too many ranges"); return 3; }
+    const int nq = 1 + kNfLanes;
+    std::vector<std::vector<PItem>> q(nq);
+    std::vector<int> need(ng, 0);
+    for (int g = 0; g < ng; g++) {
+        const Range &r = *grp[g].r;
+        for (int i = 0; i < r.count; i++)
+            for (int v = 0; v < nvec; v++) {
+                PItem it;
+                it.tile = r.first + i;
+                it.group = (int16_t)g;
+                it.dep = (int16_t)grp[g].dep;
+                it.v = (int16_t)v;
+                it.fmt = (int16_t)(r.pair ? FMT_F32X2 : FMT_F32);
+                it.pad_ = 0;
+                q[grp[g].queue].push_back(it);
+            }
+        need[g] = r.count * nvec;
+    }
+    const int grid_max = occ * d->n_sm;
+    /* simulation: seconds per byte of one worker, fixed cost per item */
+    const double hbm = 6.0e12, per_item = 1.5e-6;
+    const double spb = (double)grid_max / hbm;
+    auto cost = [&](const PItem &it) {
+        const Tile &t = d->tiles_host[it.tile];
+        const double eb = it.fmt == FMT_F32 ? 4.0 : 8.0;
+        return per_item + spb * (double)t.nr * (double)t.nc * eb;
+    };
+    const double INF = 1e300;
+    std::vector<int> left(need);
+    std::vector<double> fin(ng, 0.0);
+    auto ready_at = [&](const PItem &it) { return it.dep < 0 ? 0.0 : (left[it.dep] ? INF : fin[it.dep]); };
+    std::vector<size_t> head(nq, 0);
+    std::vector<double> qleft(nq, 0.0);
+    for (int k = 0; k < nq; k++)
+        for (const PItem &it : q[k]) qleft[k] += cost(it);
+    std::priority_queue<double, std::vector<double>, std::greater<double>> free_at;
+    size_t total = 0;
+    for (int k = 0; k < nq; k++) total += q[k].size();
+    for (int w = 0; w < std::min<size_t>(grid_max, std::max<size_t>(total, 1)); w++) free_at.push(0.0);
+    std::vector<PItem> order;
+    order.reserve(total);
+    double makespan = 0.0;
+    while (order.size() < total) {
+        const double T = free_at.top();
+        free_at.pop();
+        int pick = -1;
+        if (head[0] < q[0].size() && ready_at(q[0][head[0]]) <= T) pick = 0;
+        if (pick < 0)
+            for (int j = 1; j < nq; j++)
+                if (head[j] < q[j].size() && ready_at(q[j][head[j]]) <= T && (pick < 0 || qleft[j] > qleft[pick]))
+                    pick = j;
+        if (pick < 0) {
+            double tb = INF;
+            for (int k = 0; k < nq; k++)
+                if (head[k] < q[k].size() && ready_at(q[k][head[k]]) < tb) { tb = ready_at(q[k][head[k]]); pick = k; }
+        }
+        if (pick < 0) { set_error("persistent tile kernel: schedule stalled"); return 3; }
+        const PItem it = q[pick][head[pick]++];
+        const double c = cost(it);
+        const double t1 = std::max(T, ready_at(it)) + c;
+        qleft[pick] -= c;
+        fin[it.group] = std::max(fin[it.group], t1);
+        left[it.group]--;
+        makespan = std::max(makespan, t1);
+        free_at.push(t1);
+        order.push_back(it);
+    }
+    /* every item depends only on ranges whose items all come before it */
+    {
+        std::vector<int> seen(ng, 0);
+        for (const PItem &it : order) {
+            if (it.dep >= 0 && seen[it.dep] != need[it.dep]) {
+                set_error("persistent tile kernel: work list is not in dependency order");
+                return 3;
+            }
+            seen[it.group]++;
+        }
+    }
+    PxPlan p;
+    p.n_items = (int)order.size();
+    p.n_groups = ng;
+    p.ctl_ints = kPxDone + ng;
+    p.nvec = nvec;
+    p.grid = std::max(1, std::min(grid_max, p.n_items));
+    p.sim_ms = makespan * 1e3;
+    CUDA_TRY(cudaMalloc(&p.items, std::max<size_t>(order.size(), 1) * sizeof(PItem)));
+    CUDA_TRY(cudaMalloc(&p.gneed, std::max(ng, 1) * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&p.ctl, p.ctl_ints * sizeof(int)));
+    if (!order.empty())
+        CUDA_TRY(cudaMemcpy(p.items, order.data(), order.size() * sizeof(PItem), cudaMemcpyHostToDevice));
+    if (ng > 0) CUDA_TRY(cudaMemcpy(p.gneed, need.data(), ng * sizeof(int), cudaMemcpyHostToDevice));
+    d->px = p;
+    return 0;
+}
+
+/* The whole mixed single-density matvec as one persistent launch on s
+ * (work and output already zeroed on s). A dependency wait gives up after
+ * dep_limit cycles; 0 picks the default: about 1 s, or 20 times the
+ * simulated duration of the launch if that is longer. */
+static int launch_px(DevRep *d, const VecArgs &va, int nvec, cudaStream_t s, long long dep_limit = 0)
+{
+    int rc = build_px(d, nvec);
+    if (rc) return rc;
+    if (d->px.n_items == 0) return 0;
+    if (dep_limit <= 0) dep_limit = std::max(2000000000LL, (long long)(d->px.sim_ms * 2.0e6 * 20.0));
+    CUDA_TRY(cudaMemsetAsync(d->px.ctl, 0, d->px.ctl_ints * sizeof(int), s));
+    k_tile_px<<<d->px.grid, kTileThreads, kPxSmem, s>>>(d->tiles, d->px.items, d->px.n_items, d->px.gneed,
+                                                         d->px.ctl, va,
+                                                         reinterpret_cast<const CUtensorMap *>(d->tmaps),
+                                                         d->err_flag_dev, dep_limit);
+    CUDA_TRY(cudaGetLastError());
     return 0;
 }
 
@@ -1653,6 +2072,17 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     /* several densities in the mixed mode: the tensor-core kernel, all
      * densities (up to 16 per pass) sharing each tile's slices */
     const bool mma = d->precision == H2ERI_GPU_MIXED && nvec >= d->cfg.mma_min_vec && d->mslices != nullptr;
+    if (d->precision == H2ERI_GPU_MIXED && !mma && d->cfg.persist) {
+        /* one persistent launch: tree chain and near field from one work list */
+        if (timed) for (int k : {0, 6}) CUDA_TRY(cudaEventRecord(d->ev_t[k], sm));
+        rc = launch_px(d, va, nvec, sm);
+        if (rc) return rc;
+        if (timed) for (int k : {1, 2, 3, 7, 4}) CUDA_TRY(cudaEventRecord(d->ev_t[k], sm));
+        CUDA_TRY(cudaEventRecord(d->ev_done, sm));
+        CUDA_TRY(cudaStreamWaitEvent(s, d->ev_done, 0));
+        CUDA_TRY(cudaGetLastError());
+        return 0;
+    }
     auto launch = [&](const Range &r) {
         if (mma) launch_range_mma(d, r, va, nvec, sm);
         else launch_range(d, r, va, nvec, sm);
@@ -1684,6 +2114,9 @@ static int check_kernel_flag(DevRep *d)
     if (f & 2u)
         set_error("a tile kernel found its shared memory off the 1024-byte alignment that swizzled TMA copies "
                   "need and did nothing; results are invalid");
+    else if (f & 4u)
+        set_error("the persistent tile kernel gave up waiting for a preceding range to complete (bounded wait "
+                  "expired); results are invalid");
     else
         set_error("a tile kernel gave up waiting for a TMA load (bounded wait expired); results are invalid");
     return 11;
@@ -1815,6 +2248,55 @@ extern "C" int H2ERI_gpu_selftest_wait_timeout_async(H2ERI_p h2eri, long long cy
     k_wait_probe<<<1, 32, 0, s>>>(d->err_flag_dev, cycles);
     CUDA_TRY(cudaGetLastError());
     return 0;
+}
+
+/* Failure-detection check of the persistent kernel's dependency waits: one
+ * mixed single-density matvec of h2eri (zero input) with the item count of
+ * its first range raised by one, so that the range after it waits for an
+ * item that never completes. The wait gives up after `cycles`, the kernel
+ * returns, and the expiry must be reported. The count is restored before
+ * returning. Returns 1 when the expiry was reported, 0 when it was not, an
+ * error code (> 1) otherwise. */
+extern "C" int H2ERI_gpu_selftest_persist_timeout(H2ERI_p h2eri, long long cycles)
+{
+    if (cycles <= 0) { set_error("cycles must be > 0"); return 3; }
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return rc;
+    if (d->precision != H2ERI_GPU_MIXED) { set_error("the persistent kernel runs in the mixed mode only"); return 3; }
+    rc = ensure_work(d, 1);
+    if (rc) return rc;
+    rc = build_px(d, 1);
+    if (rc) return rc;
+    if (d->px.n_groups < 2) { set_error("the structure has a single range: nothing waits"); return 3; }
+    CUDA_TRY(cudaDeviceSynchronize());
+    (void)check_kernel_flag(d);   /* start from a clear record */
+    int need0 = 0;
+    CUDA_TRY(cudaMemcpy(&need0, d->px.gneed, sizeof(int), cudaMemcpyDeviceToHost));
+    const int raised = need0 + 1;
+    CUDA_TRY(cudaMemcpy(d->px.gneed, &raised, sizeof(int), cudaMemcpyHostToDevice));
+    VecArgs va;
+    std::memset(&va, 0, sizeof(va));
+    const size_t per_r = (size_t)d->rank_total;
+    va.base[VK_X] = d->xbuf; va.stride[VK_X] = d->krnl;
+    va.base[VK_Y] = d->ybuf; va.stride[VK_Y] = d->krnl;
+    va.base[VK_Y0] = d->work; va.stride[VK_Y0] = d->rank_total;
+    va.base[VK_Y1] = d->work + per_r; va.stride[VK_Y1] = d->rank_total;
+    va.base[VK_T] = d->work + 2 * per_r; va.stride[VK_T] = d->lr_total;
+    cudaStream_t sm = d->s_main;
+    int lrc = 0;
+    if (cudaMemsetAsync(d->xbuf, 0, (size_t)d->krnl * sizeof(double), sm) != cudaSuccess ||
+        cudaMemsetAsync(d->work, 0, (2 * per_r + d->lr_total) * sizeof(double), sm) != cudaSuccess ||
+        cudaMemsetAsync(d->ybuf, 0, (size_t)d->krnl * sizeof(double), sm) != cudaSuccess)
+        lrc = 10;
+    if (lrc == 0) lrc = launch_px(d, va, 1, sm, cycles);
+    const cudaError_t e = cudaStreamSynchronize(sm);
+    CUDA_TRY(cudaMemcpy(d->px.gneed, &need0, sizeof(int), cudaMemcpyHostToDevice));
+    if (lrc) return lrc;
+    if (e != cudaSuccess) { set_error(std::string("persistent self-test: ") + cudaGetErrorString(e)); return 10; }
+    const unsigned f = *d->err_flag;
+    const int frc = check_kernel_flag(d);
+    return (frc == 11 && (f & 4u)) ? 1 : 0;
 }
 
 /* Waits for the structure's own streams and reports what its kernels
@@ -2028,14 +2510,17 @@ extern "C" int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n)
     for (const Range &r : d->bwd) launches += r.count > 0;
     for (const Range &r : d->den) launches += r.count > 0;
     for (const Range &r : d->mid) launches += r.count > 0;
+    /* the mixed single-density path with the persistent kernel: one launch */
+    if (d->precision == H2ERI_GPU_MIXED && d->cfg.persist) launches = 1;
     double mbytes = d->precision == H2ERI_GPU_MIXED ? d->alg_bytes_matrix_mixed : d->alg_bytes_matrix;
-    double vals[19] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
+    double vals[23] = {(double)launches, mbytes, d->alg_bytes_vec, d->alg_flops,
                        (double)d->bytes_U, (double)d->bytes_B, (double)d->bytes_D,
                        d->last_ms[0], d->last_ms[1], d->last_ms[2], d->last_ms[3], d->last_ms[4],
                        (double)d->precision, (double)(2.0 * d->rank_total + d->lr_total),
                        (double)d->cfg.chunk_rows, (double)d->cfg.tiles_per_cta, (double)d->cfg.nf_concurrent,
-                       (double)d->cfg.mma_min_vec, (double)d->cfg.mma_grid_div};
-    int m = std::min(n, 19);
+                       (double)d->cfg.mma_min_vec, (double)d->cfg.mma_grid_div, (double)d->cfg.persist,
+                       (double)d->px.n_items, (double)d->px.grid, d->px.sim_ms};
+    int m = std::min(n, 23);
     for (int i = 0; i < m; i++) out[i] = vals[i];
     return m;
 }

@@ -5,10 +5,11 @@
  * launch configuration is run on the device and timed with CUDA events
  * (H2 matvecs on a fixed non-zero input, after warm-up), and the fastest is
  * kept in the structure's TuneCfg:
- *   single-density path (k_tile / k_tile_mx): rows per tile (512, 256,
- *     128: the tile plan is rebuilt from the recorded products), tiles per
- *     CTA of the mixed kernel (2 or 1), near-field lanes on their own
- *     streams or on one;
+ *   single-density path (k_tile / k_tile_mx / k_tile_px): rows per tile
+ *     (512, 256, 128: the tile plan is rebuilt from the recorded products);
+ *     in the mixed mode one persistent launch, or a launch per range with
+ *     tiles per CTA 2 or 1 and near-field lanes on their own streams or on
+ *     one;
  *   several densities in the mixed mode: the tensor-core kernel (CTAs per
  *     launch n_SM or n_SM / 2, near-field lanes concurrent or not) against
  *     the single-density kernels, which decides the density count from
@@ -64,10 +65,18 @@ void load_file_locked()
     const char *path = std::getenv("H2G_TUNE_FILE");
     if (path == nullptr || path[0] == '\0') return;
     std::ifstream f(path);
-    std::string key;
-    TuneCfg c;
-    while (f >> key >> c.chunk_rows >> c.tiles_per_cta >> c.nf_concurrent >> c.mma_min_vec >> c.mma_grid_div)
+    std::string line;
+    while (std::getline(f, line)) {
+        /* key and five or six choices (files written before the persistent
+         * kernel have five: it is then off) */
+        std::istringstream ls(line);
+        std::string key;
+        TuneCfg c;
+        if (!(ls >> key >> c.chunk_rows >> c.tiles_per_cta >> c.nf_concurrent >> c.mma_min_vec >> c.mma_grid_div))
+            continue;
+        if (!(ls >> c.persist)) c.persist = 0;
         g_tcache[key] = c;
+    }
 }
 
 void save_locked(const std::string &key, const TuneCfg &c)
@@ -77,7 +86,7 @@ void save_locked(const std::string &key, const TuneCfg &c)
     if (path == nullptr || path[0] == '\0') return;
     std::ofstream f(path, std::ios::app);
     f << key << ' ' << c.chunk_rows << ' ' << c.tiles_per_cta << ' ' << c.nf_concurrent << ' ' << c.mma_min_vec << ' '
-      << c.mma_grid_div << '\n';
+      << c.mma_grid_div << ' ' << c.persist << '\n';
 }
 
 int apply_cfg(DevRep *d, const TuneCfg &c)
@@ -138,6 +147,7 @@ void tune_apply_cached(DevRep *d)
         c.chunk_rows = it->second.chunk_rows;
         c.tiles_per_cta = it->second.tiles_per_cta;
         c.nf_concurrent = it->second.nf_concurrent;
+        c.persist = it->second.persist;
         any = true;
     }
     for (int cls : {2, 4, 8, 16}) {
@@ -157,10 +167,10 @@ using namespace h2g;
 /* Runs the autotuner for h2eri at n_den densities per launch in its current
  * precision and keeps the fastest launch choices for it. out (n values at
  * most): [0] ms per matvec with the choice kept, [1] ms with the choices
- * before tuning, [2] number of candidates timed, [3..7] the choice (tile
+ * before tuning, [2] number of candidates timed, [3..8] the choice (tile
  * rows, tiles per CTA, near-field lanes concurrent, density count from which
- * the tensor-core kernel runs, CTA divisor of its launches), [8..] ms of
- * every candidate in the order tried. Returns the number of values written,
+ * the tensor-core kernel runs, CTA divisor of its launches, persistent
+ * launch), [9..] ms of every candidate in the order tried. Returns the number of values written,
  * or < 0 on error. */
 extern "C" int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n)
 {
@@ -191,16 +201,26 @@ extern "C" int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n)
                 cand.push_back(c);
             }
     }
-    for (int rows : {512, 256, 128})
+    for (int rows : {512, 256, 128}) {
+        if (mixed) {
+            /* one persistent launch (tiles per CTA and lanes do not apply) */
+            TuneCfg c = start;
+            c.chunk_rows = rows;
+            c.persist = 1;
+            if (multi) c.mma_min_vec = n_den + 1;
+            cand.push_back(c);
+        }
         for (int tpc : (mixed ? std::vector<int>{2, 1} : std::vector<int>{2}))
             for (int nf : {1, 0}) {
                 TuneCfg c = start;
                 c.chunk_rows = rows;
                 c.tiles_per_cta = tpc;
                 c.nf_concurrent = nf;
+                c.persist = 0;
                 if (multi) c.mma_min_vec = n_den + 1;   /* the single-density kernels for this count */
                 cand.push_back(c);
             }
+    }
     std::vector<double> ms(cand.size(), 1e300);
     size_t best = 0;
     for (size_t i = 0; i < cand.size(); i++) {
@@ -222,7 +242,7 @@ extern "C" int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n)
     }
     std::vector<double> v = {ms[best], ms[0], (double)cand.size(), (double)keep.chunk_rows,
                              (double)keep.tiles_per_cta, (double)keep.nf_concurrent, (double)keep.mma_min_vec,
-                             (double)keep.mma_grid_div};
+                             (double)keep.mma_grid_div, (double)keep.persist};
     v.insert(v.end(), ms.begin(), ms.end());
     const int m = std::min(n, (int)v.size());
     for (int i = 0; i < m; i++) out[i] = v[i];

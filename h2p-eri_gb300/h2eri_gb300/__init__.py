@@ -100,6 +100,7 @@ SIGNATURES = {
     "H2ERI_gpu_check": (ctypes.c_int, [_vp]),
     "H2ERI_gpu_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int]),
     "H2ERI_gpu_selftest_wait_timeout_async": (ctypes.c_int, [_vp, ctypes.c_longlong, _vp]),
+    "H2ERI_gpu_selftest_persist_timeout": (ctypes.c_int, [_vp, ctypes.c_longlong]),
     "H2ERI_save_representation": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "H2ERI_load_representation": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
 }
@@ -251,13 +252,14 @@ class H2ERI:
 
     def report(self):
         """Device-copy figures (see H2ERI_gpu_report in include/h2eri_gb300.h)."""
-        out = np.zeros(19)
-        n = lib().H2ERI_gpu_report(self.handle, out.ctypes.data, 19)
+        out = np.zeros(23)
+        n = lib().H2ERI_gpu_report(self.handle, out.ctypes.data, 23)
         if n < 0:
             _check(-n, "gpu_report")
         keys = ["launches_per_matvec", "alg_matrix_bytes", "alg_vector_bytes", "alg_flops", "arena_U", "arena_B",
                 "arena_D", "ms_fwd", "ms_mid", "ms_bwd", "ms_den", "ms_total", "precision", "noalloc_scratch_doubles",
-                "tile_rows", "tiles_per_cta", "nf_concurrent", "mma_min_vec", "mma_grid_div"]
+                "tile_rows", "tiles_per_cta", "nf_concurrent", "mma_min_vec", "mma_grid_div", "persist",
+                "px_items", "px_grid", "px_sim_ms"]
         return dict(zip(keys, out[:n].tolist()))
 
     def autotune(self, n_den=1):
@@ -269,8 +271,8 @@ class H2ERI:
             _check(-m, "gpu_autotune")
         return {"ms_best": out[0], "ms_before": out[1], "candidates": int(out[2]),
                 "choice": {"tile_rows": int(out[3]), "tiles_per_cta": int(out[4]), "nf_concurrent": int(out[5]),
-                           "mma_min_vec": int(out[6]), "mma_grid_div": int(out[7])},
-                "ms_candidates": out[8:m].tolist()}
+                           "mma_min_vec": int(out[6]), "mma_grid_div": int(out[7]), "persist": int(out[8])},
+                "ms_candidates": out[9:m].tolist()}
 
     def print_statistic(self):
         lib().H2ERI_print_statistic(self.handle)

@@ -93,6 +93,13 @@ int H2ERI_gpu_selftest_wait_timeout(long long cycles);
  * way the kernels of the asynchronous entry points do; returns after
  * enqueueing (0) and leaves the report to H2ERI_gpu_check. */
 int H2ERI_gpu_selftest_wait_timeout_async(H2ERI_p h2eri, long long cycles, void *stream);
+/* Failure-detection check of the persistent mixed-mode kernel (mixed
+ * precision only): one matvec of a zero vector with the item count of the
+ * first range raised by one, so the range after it waits for an item that
+ * never completes; that wait gives up after `cycles` SM cycles, the kernel
+ * returns, and the expiry must be reported. The count is restored. Returns
+ * 1 when the expiry was reported, 0 when not, > 1 on error. */
+int H2ERI_gpu_selftest_persist_timeout(H2ERI_p h2eri, long long cycles);
 /* After asynchronous calls (the _device variants and
  * H2ERI_matvec_device_noalloc return before their kernels run): waits for
  * the structure's own streams and returns 11, with a message in
@@ -164,18 +171,20 @@ int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, v
  * configuration of this structure at n_den densities per launch in its
  * current precision on the device, times each with CUDA events, and keeps
  * the fastest. Candidates: rows per tile of the single-density kernels
- * (512, 256, 128), tiles per CTA (2, 1; mixed mode), near-field lanes on
- * their own streams or one; for several densities in the mixed mode also
- * the tensor-core kernel (n_SM or n_SM / 2 CTAs per launch) against the
- * single-density kernels. The choice is cached per structure shape,
+ * (512, 256, 128); in the mixed mode the persistent launch (the whole
+ * matvec in one launch) or one launch per range with tiles per CTA (2, 1)
+ * and near-field lanes on their own streams or one; for several densities
+ * in the mixed mode also the tensor-core kernel (n_SM or n_SM / 2 CTAs per
+ * launch) against the single-density kernels. The choice is cached per structure shape,
  * precision and density-count class in the process and, with
  * H2G_TUNE_FILE=<path> in the environment, in that file, which later
  * processes read when a structure of the same shape is uploaded or changes
  * precision. Synchronises the device; takes about 0.1-1 s. out: [0] ms per
  * matvec with the choice, [1] ms before tuning, [2] candidates timed,
- * [3..7] the choice (tile rows, tiles per CTA, near-field lanes concurrent,
- * density count from which the tensor-core kernel runs, its CTA divisor),
- * [8..] ms of each candidate. Returns the number of values written, or < 0. */
+ * [3..8] the choice (tile rows, tiles per CTA, near-field lanes concurrent,
+ * density count from which the tensor-core kernel runs, its CTA divisor,
+ * persistent launch), [9..] ms of each candidate. Returns the number of
+ * values written, or < 0. */
 int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n);
 
 /* Figures of the device copy, for reports. out[0] kernel launches per matvec
@@ -184,10 +193,14 @@ int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n);
  * out[4..6] arena bytes of U, B, D, out[7..11] last timed phase durations
  * in ms (upward, coupling, downward, near field, total), out[12] far-field
  * precision mode, out[13] scratch doubles one matvec of one vector needs,
- * out[14..18] the launch choices in use (tile rows, tiles per CTA,
+ * out[14..19] the launch choices in use (tile rows, tiles per CTA,
  * near-field lanes concurrent, density count from which the tensor-core
- * kernel runs, its CTA divisor; see H2ERI_gpu_autotune). Returns the number
- * of values written (<= n), or < 0. */
+ * kernel runs, its CTA divisor, persistent launch; see H2ERI_gpu_autotune),
+ * out[20..22] the persistent kernel's work list (items, CTAs, makespan in ms
+ * of its host schedule simulation; 0 before its first use). In the mixed
+ * single-density path with the persistent launch, the phase durations
+ * out[7..9] all hold the whole launch. Returns the number of values written
+ * (<= n), or < 0. */
 int H2ERI_gpu_report(H2ERI_p h2eri, double *out, int n);
 
 /* Save / load the H2 representation (tree, pair lists, U, B, D and the

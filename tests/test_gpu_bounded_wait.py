@@ -79,3 +79,23 @@ def test_async_expiry_reported_by_gpu_check(library, alk26, oracle_lib):
     oracle_lib.oracle_build_Coulomb(alk26.handle, D.ctypes.data, Jo.ctypes.data)
     assert relerr(dJ.cpu().numpy(), Jo) < 1e-12
     assert library.H2ERI_gpu_selftest_wait_timeout_async(alk26.handle, -1, sp) == 3
+
+
+def test_persistent_dependency_wait_expiry_reported(library, alk26, oracle_lib):
+    """The persistent kernel's waits for a preceding range are bounded too:
+    with the first range's item count raised by one, the range after it waits
+    for an item that never completes; the wait gives up (~1 ms of SM clock),
+    every CTA stops, the expiry is reported, and the next mixed J build on
+    the same structure is correct."""
+    alk26.set_precision(hg.MIXED)
+    try:
+        assert alk26.report()["persist"] == 1
+        assert library.H2ERI_gpu_selftest_persist_timeout(alk26.handle, 2_000_000) == 1
+        D = hg.molecules.seeded_density(alk26.num_bf, 20, 4323)
+        J = alk26.build_coulomb(D)
+    finally:
+        alk26.set_precision(hg.FP64)
+    Jo = np.zeros_like(D)
+    oracle_lib.oracle_build_Coulomb(alk26.handle, D.ctypes.data, Jo.ctypes.data)
+    assert relerr(J, Jo) < 1e-8
+    assert library.H2ERI_gpu_selftest_persist_timeout(alk26.handle, 0) == 3

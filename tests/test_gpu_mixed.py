@@ -262,3 +262,48 @@ def test_batch_in_shared_launches_single_density_kernels(oracle_lib, library, mo
     finally:
         for h in hs:
             h.destroy()
+
+
+@pytest.mark.parametrize("rows", ["512", "128"])
+def test_persistent_launch_against_range_launches(oracle_lib, library, monkeypatch, rows):
+    """The whole mixed single-density matvec in one persistent launch (items
+    taken from one work list, ranges waiting for the ranges they depend on)
+    gives the J of the launch-per-range path up to the order of the FP64
+    output sums, and both meet the 1e-8 target against the oracle; also with
+    three densities per call on the single-density kernels, and with
+    128-row tiles."""
+    torch = pytest.importorskip("torch")
+    mol = os.path.join(GOLDEN, "alk32_ccpvdz.mol")
+    monkeypatch.setenv("H2G_MMA_MIN_VEC", "17")   # several densities on the single-density kernels
+    monkeypatch.setenv("H2G_TILE_ROWS", rows)
+    out = {}
+    for persist in ("1", "0"):
+        monkeypatch.setenv("H2G_PERSIST", persist)
+        h = hg.H2ERI.from_mol(mol, qr_tol=1e-6)
+        try:
+            h.set_precision(hg.MIXED)
+            n = h.num_bf
+            Ds = np.stack([hg.molecules.seeded_density(n, 41, 800 + i) for i in range(3)])
+            dD = torch.tensor(Ds, device="cuda")
+            dJ = torch.empty_like(dD)
+            s = torch.cuda.Stream()
+            torch.cuda.synchronize()
+            for nd in (1, 3):
+                assert library.H2ERI_build_Coulomb_device(h.handle, nd, dD.data_ptr(), dJ.data_ptr(),
+                                                          ctypes.c_void_p(s.cuda_stream)) == 0
+                s.synchronize()
+                assert library.H2ERI_gpu_check(h.handle) == 0
+                out[(persist, nd)] = dJ[:nd].cpu().numpy().copy()
+            rep = h.report()
+            assert rep["persist"] == int(persist)
+            assert rep["tile_rows"] == int(rows)
+            if persist == "1":
+                assert rep["launches_per_matvec"] == 1 and rep["px_items"] > 0 and rep["px_grid"] > 0
+            Jo = [oracle_J(oracle_lib, h, Ds[i]) for i in range(3)]
+        finally:
+            h.destroy()
+        for nd in (1, 3):
+            for i in range(nd):
+                assert relerr(out[(persist, nd)][i], Jo[i]) < TOL_MIXED, (persist, nd, i)
+    for nd in (1, 3):
+        assert relerr(out[("1", nd)], out[("0", nd)]) < 1e-13
