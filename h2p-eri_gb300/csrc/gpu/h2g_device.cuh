@@ -82,12 +82,13 @@ struct PlanRec {
 /* Launch choices of one structure, picked by the autotuner
  * (H2ERI_gpu_autotune) or left at their defaults. */
 struct TuneCfg {
-    int chunk_rows = 512;      /* rows per tile of the single-density tile kernels (128, 256, 512) */
+    int chunk_rows = 512;      /* rows per tile of the single-density tile kernels (64..512), or 0: */
+                               /* per range, the tallest that gives two waves of CTAs              */
     int tiles_per_cta = 2;     /* mixed single-density kernel: tiles per CTA (1 or 2)               */
     int nf_concurrent = 1;     /* near-field lanes on their own streams (1) or one stream (0)       */
     int mma_min_vec = 2;       /* densities per launch from which the tensor-core kernel runs       */
     int mma_grid_div = 1;      /* tensor-core launches use n_SM / mma_grid_div CTAs                  */
-    int persist = 1;           /* mixed single-density path: one persistent launch (1) or a launch  */
+    int persist = 0;           /* mixed single-density path: one persistent launch (1) or a launch  */
                                /* per range on the stream lanes (0)                                 */
 };
 

@@ -1534,10 +1534,31 @@ static int build_rep(H2ERI_p h, DevRep *d)
  * multiple of 64, at most kChunkRows), from the recorded products: same
  * ranges, same arenas. Waits for the device first (the old tile list may be
  * in use). */
+/* Rows per tile of one range in the adaptive plan: the tallest of 512, 256,
+ * 128, 64 that still gives the range at least two waves of CTAs (two tiles
+ * per CTA, two CTAs per SM). A range with few, tall tiles (the narrow levels
+ * of the tree) is otherwise bound by a few CTAs streaming long tiles one
+ * stage at a time, while wide ranges keep tall tiles and their lower
+ * per-CTA overhead. */
+static int adaptive_rows(const std::vector<PlanRec> &recs, int n_sm)
+{
+    const long long want = 2LL * 2 * 2 * std::max(n_sm, 1);   /* tiles for two waves */
+    int rows = kChunkRows;
+    for (; rows > 64; rows /= 2) {
+        long long n = 0;
+        for (const PlanRec &q : recs)
+            n += (long long)((q.nrow + rows - 1) / rows) * ((q.ncol + kTileCols - 1) / kTileCols);
+        if (n >= want) break;
+    }
+    return rows;
+}
+
+/* Rebuild the tile plan from the recorded products with `rows` rows per tile
+ * (a multiple of 64 up to 512), or per range with adaptive_rows (rows 0). */
 int replan_tiles(DevRep *d, int rows)
 {
-    if (rows < 64 || rows > kChunkRows || rows % 64 != 0) {
-        set_error("tile rows must be a multiple of 64 in [64, " + std::to_string(kChunkRows) + "]");
+    if (rows != 0 && (rows < 64 || rows > kChunkRows || rows % 64 != 0)) {
+        set_error("tile rows must be 0 (per range) or a multiple of 64 in [64, " + std::to_string(kChunkRows) + "]");
         return 3;
     }
     if (rows == d->cfg.chunk_rows && d->tiles != nullptr) return 0;
@@ -1545,7 +1566,8 @@ int replan_tiles(DevRep *d, int rows)
     auto emit = [&](std::vector<Range> &rr, const std::vector<std::vector<PlanRec>> &recs) {
         for (size_t k = 0; k < rr.size() && k < recs.size(); k++) {
             rr[k].first = (int)all.size();
-            for (const PlanRec &q : recs[k]) gen_tiles(q, rows, all);
+            const int rk = rows ? rows : adaptive_rows(recs[k], d->n_sm);
+            for (const PlanRec &q : recs[k]) gen_tiles(q, rk, all);
             rr[k].count = (int)all.size() - rr[k].first;
         }
     };

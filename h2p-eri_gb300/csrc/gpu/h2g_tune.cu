@@ -6,7 +6,8 @@
  * (H2 matvecs on a fixed non-zero input, after warm-up), and the fastest is
  * kept in the structure's TuneCfg:
  *   single-density path (k_tile / k_tile_mx / k_tile_px): rows per tile
- *     (512, 256, 128: the tile plan is rebuilt from the recorded products);
+ *     (per range, or 512, 256, 128 for all: the tile plan is rebuilt from the
+ *     recorded products);
  *     in the mixed mode one persistent launch, or a launch per range with
  *     tiles per CTA 2 or 1 and near-field lanes on their own streams or on
  *     one;
@@ -201,7 +202,7 @@ extern "C" int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n)
                 cand.push_back(c);
             }
     }
-    for (int rows : {512, 256, 128}) {
+    for (int rows : {0, 512, 256, 128}) {
         if (mixed) {
             /* one persistent launch (tiles per CTA and lanes do not apply) */
             TuneCfg c = start;

@@ -171,7 +171,8 @@ int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, v
  * configuration of this structure at n_den densities per launch in its
  * current precision on the device, times each with CUDA events, and keeps
  * the fastest. Candidates: rows per tile of the single-density kernels
- * (512, 256, 128); in the mixed mode the persistent launch (the whole
+ * (0: chosen per range, the tallest of 512..64 that gives the range two
+ * waves of CTAs; or 512, 256, 128 for all ranges); in the mixed mode the persistent launch (the whole
  * matvec in one launch) or one launch per range with tiles per CTA (2, 1)
  * and near-field lanes on their own streams or one; for several densities
  * in the mixed mode also the tensor-core kernel (n_SM or n_SM / 2 CTAs per

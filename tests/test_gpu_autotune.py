@@ -30,7 +30,7 @@ def test_autotune_single_density(alk26, oracle_lib, mode, tol):
     try:
         r = alk26.autotune(1)
         assert r["candidates"] >= 6 and r["ms_best"] <= r["ms_before"] * 1.0001
-        assert r["choice"]["tile_rows"] in (128, 256, 512)
+        assert r["choice"]["tile_rows"] in (0, 128, 256, 512)   # 0: chosen per range
         rep = alk26.report()
         assert rep["tile_rows"] == r["choice"]["tile_rows"]
         D = hg.molecules.seeded_density(alk26.num_bf, 30, 6100 + mode)
@@ -39,7 +39,7 @@ def test_autotune_single_density(alk26, oracle_lib, mode, tol):
         alk26.set_precision(hg.FP64)
 
 
-@pytest.mark.parametrize("rows,tpc", [(128, 1), (256, 2), (512, 1)])
+@pytest.mark.parametrize("rows,tpc", [(0, 2), (128, 1), (256, 2), (512, 1)])
 def test_tile_shapes_the_tuner_may_pick(oracle_lib, tmp_path, monkeypatch, rows, tpc):
     """Every tile shape among the tuner's candidates, fixed through the
     environment, gives the oracle's J in both precisions."""

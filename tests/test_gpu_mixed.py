@@ -264,14 +264,14 @@ def test_batch_in_shared_launches_single_density_kernels(oracle_lib, library, mo
             h.destroy()
 
 
-@pytest.mark.parametrize("rows", ["512", "128"])
+@pytest.mark.parametrize("rows", ["512", "128", "0"])
 def test_persistent_launch_against_range_launches(oracle_lib, library, monkeypatch, rows):
     """The whole mixed single-density matvec in one persistent launch (items
     taken from one work list, ranges waiting for the ranges they depend on)
     gives the J of the launch-per-range path up to the order of the FP64
     output sums, and both meet the 1e-8 target against the oracle; also with
     three densities per call on the single-density kernels, and with
-    128-row tiles."""
+    128-row tiles and tile heights chosen per range (0)."""
     torch = pytest.importorskip("torch")
     mol = os.path.join(GOLDEN, "alk32_ccpvdz.mol")
     monkeypatch.setenv("H2G_MMA_MIN_VEC", "17")   # several densities on the single-density kernels
