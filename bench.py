@@ -29,6 +29,7 @@ set-up where its sources exist).
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -662,27 +663,37 @@ def run_gpu(args):
         for i in range(0, B, nden):
             L.H2ERI_build_Coulomb_device(h.handle, nden, dD[i].data_ptr(), dJ[i].data_ptr(), sp)
 
-    def device_run(mode, nden):
-        """K timed steps of B builds, nden densities per call; ms per step."""
+    def device_run(mode, nden, min_s=0.0):
+        """Timed steps of B builds, nden densities per call; ms per step.
+        K steps (the headline); with min_s > 0 (the sub-figures), at least
+        K steps and at least min_s seconds, the count set from the warm-up."""
         L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if mode == "mixed" else hg.FP64)
         if L.H2ERI_build_Coulomb_device(h.handle, nden, dD[0].data_ptr(), dJ[0].data_ptr(), sp) != 0:
             raise RuntimeError(L.H2ERI_gpu_last_error().decode())
+        torch.cuda.synchronize()
+        t_w = time.perf_counter()
         for _ in range(args.warmup):
             one_step(nden)
         torch.cuda.synchronize()
+        steps = args.steps
+        if min_s > 0:
+            per_step = (time.perf_counter() - t_w) / max(args.warmup, 1)
+            steps = max(args.steps, int(math.ceil(min_s / max(per_step, 1e-6))))
         barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with ClockSampler(local) as clk:
             e0.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 one_step(nden)
             e1.record(stream)
             torch.cuda.synchronize()
         barrier()
         if L.H2ERI_gpu_check(h.handle) != 0:
             raise RuntimeError(L.H2ERI_gpu_last_error().decode())
-        return e0.elapsed_time(e1) / args.steps, dJ.cpu().numpy(), clk.summary()
+        ms_total = e0.elapsed_time(e1)
+        summ = dict(clk.summary(), timed_steps=steps, timed_s=ms_total / 1e3)
+        return ms_total / steps, dJ.cpu().numpy(), summ
 
     results = {}
     for mode in modes:
@@ -690,7 +701,7 @@ def run_gpu(args):
         results[mode] = {"ms": ms, "J": J, "clocks": clk}
     best = "mixed" if "mixed" in results else "fp64"
     n16 = 16
-    ms16, J16, clk16 = device_run(best, n16)
+    ms16, J16, clk16 = device_run(best, n16, min_s=1.0)
     L.H2ERI_gpu_set_precision(h.handle, hg.MIXED if best == "mixed" else hg.FP64)
     # kernels per single-density J build with the choices in use: the H2
     # matvec's launches plus the uncontract and contract kernels
@@ -808,6 +819,7 @@ def run_gpu(args):
                                        "peak": peak, "unit": "GB/s",
                                        "frac": bytes16 / (ms16 * n16 / B / 1e3) / 1e9 / peak,
                                        "alg_bytes_per_launch": bytes16},
+                          "timed_steps": clk16["timed_steps"], "timed_s": clk16["timed_s"],
                           "clocks": {k: clk16[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")}},
         "autotune": tuned,
         "setup_s": setup_s, "upload_s": upload_s,
