@@ -10,10 +10,12 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 #include <omp.h>
 
+#include "h2g_eri.h"
 #include "h2g_host.h"
 #include "h2eri_gb300.h"
 
@@ -789,6 +791,96 @@ void eri_block(H2ERI_p h, const int *bra, int nbra, const int *ket, int nket,
     }
 }
 
+/* Shell pairs of near-field block i: a leaf's diagonal block (bra = ket =
+ * its shell pairs, symmetric) or an inadmissible pair's block. */
+void d_block_lists(H2ERI_p h, int i, std::vector<int> &bra, std::vector<int> &ket, bool &sym)
+{
+    const int n_leaf = h->n_leaf_node;
+    bra.clear();
+    ket.clear();
+    int n0, n1;
+    if (i < n_leaf) {
+        n0 = n1 = h->height_nodes[i];
+        sym = true;
+    } else {
+        n0 = h->r_inadm_pairs[2 * (i - n_leaf)];
+        n1 = h->r_inadm_pairs[2 * (i - n_leaf) + 1];
+        sym = false;
+    }
+    for (int k = h->pt_cluster[2 * n0]; k <= h->pt_cluster[2 * n0 + 1]; k++) bra.push_back(k);
+    for (int k = h->pt_cluster[2 * n1]; k <= h->pt_cluster[2 * n1 + 1]; k++) ket.push_back(k);
+}
+
+/* Dense near-field block i with the host engine. Diagonal blocks are
+ * symmetric; only their upper shell-pair triangle is evaluated and mirrored. */
+void d_block_host(H2ERI_p h, int i, H2E_dense_mat_p blk)
+{
+    if (i < h->n_leaf_node) {
+        int node = h->height_nodes[i];
+        int ps = h->pt_cluster[2 * node], pe = h->pt_cluster[2 * node + 1];
+        int n = blk->nrow;
+        std::vector<double> buf(15 * 15 * 15 * 15);
+        for (int a = ps; a <= pe; a++) {
+            int ra = h->sp_bfp_sidx[a] - h->sp_bfp_sidx[ps], na = h->sp_nbfp[a];
+            const h2g_pair *pa = sp_pair(h, a);
+            for (int b = a; b <= pe; b++) {
+                int rb = h->sp_bfp_sidx[b] - h->sp_bfp_sidx[ps], nb = h->sp_nbfp[b];
+                h2g_eri_quartet(pa, sp_pair(h, b), buf.data());
+                for (int x = 0; x < na; x++)
+                    for (int y = 0; y < nb; y++) {
+                        double v = buf[(size_t)x * nb + y];
+                        blk->data[(size_t)(ra + x) * n + rb + y] = v;
+                        blk->data[(size_t)(rb + y) * n + ra + x] = v;
+                    }
+            }
+        }
+    } else {
+        std::vector<int> bra, ket;
+        bool sym;
+        d_block_lists(h, i, bra, ket, sym);
+        eri_pairs_to_mat(h, (int)bra.size(), bra.data(), (int)ket.size(), ket.data(), blk->data, blk->ncol);
+    }
+}
+
+/* The set-up's ERI blocks on the GPU (when gpu_eri_usable(): a CUDA device
+ * and H2G_SETUP_GPU not 0): the structure's shell pairs, uploaded on first
+ * use and kept until the set-up ends; nullptr means the host engine. */
+struct SetupEri {
+    H2ERI_p h = nullptr;
+    EriSet *es = nullptr;
+    bool failed = false;
+};
+static SetupEri g_seri;
+
+EriSet *setup_eri(H2ERI_p h)
+{
+    if (g_seri.h == h) return g_seri.failed ? nullptr : g_seri.es;
+    if (g_seri.es) gpu_eri_free(g_seri.es);
+    g_seri = SetupEri();
+    g_seri.h = h;
+    if (!gpu_eri_usable()) { g_seri.failed = true; return nullptr; }
+    std::vector<const h2g_pair *> pairs(h->num_sp);
+    for (int i = 0; i < h->num_sp; i++) pairs[i] = sp_pair(h, i);
+    if (gpu_eri_create(h->num_sp, pairs.data(), &g_seri.es) != 0) {
+        g_seri.failed = true;
+        g_seri.es = nullptr;
+    }
+    return g_seri.es;
+}
+
+void setup_eri_failed(H2ERI_p h)
+{
+    std::fprintf(stderr, "h2eri_gb300: GPU integral blocks failed (%s); the host engine takes over\n",
+                 H2ERI_gpu_last_error());
+    if (g_seri.h == h) g_seri.failed = true;
+}
+
+void setup_eri_end()
+{
+    if (g_seri.es) gpu_eri_free(g_seri.es);
+    g_seri = SetupEri();
+}
+
 /* Coupling blocks (src/H2ERI_build_H2.c:910-1152). */
 void build_B(H2ERI_p h)
 {
@@ -818,12 +910,11 @@ void build_B(H2ERI_p h)
     coo_to_csr(n_node, (int)pi.size(), pi.data(), pj.data(), pv.data(), h->B_p2i_rowptr, h->B_p2i_colidx, h->B_p2i_val);
 
     h->c_B_blks = (H2E_dense_mat_p *)std::calloc(std::max(n_pair, 1), sizeof(H2E_dense_mat_p));
-    #pragma omp parallel for schedule(dynamic, 1)
-    for (int i = 0; i < n_pair; i++) {
+    /* bra / ket shell pairs of block i and the selected rows / columns */
+    auto lists = [&](int i, std::vector<int> &bra, std::vector<int> &ket, const int *&srow, const int *&scol) {
         int n0 = h->r_adm_pairs[2 * i], n1 = h->r_adm_pairs[2 * i + 1];
         int l0 = h->node_level[n0], l1 = h->node_level[n1];
-        std::vector<int> bra, ket;
-        const int *srow = nullptr, *scol = nullptr;
+        srow = scol = nullptr;
         if (l0 >= l1) {
             bra.assign(h->J_pair[n0]->data, h->J_pair[n0]->data + h->J_pair[n0]->length);
             srow = h->J_row[n0]->data;
@@ -836,6 +927,62 @@ void build_B(H2ERI_p h)
         } else {
             for (int k = h->pt_cluster[2 * n1]; k <= h->pt_cluster[2 * n1 + 1]; k++) ket.push_back(h->index_seq[k]);
         }
+    };
+    int done = 0;
+    if (EriSet *es = setup_eri(h)) {
+        /* full blocks on the GPU in groups of at most 2^27 doubles, rows and
+         * columns selected and blocks compressed on the host */
+        while (done < n_pair) {
+            std::vector<int> idx;
+            std::vector<std::vector<double>> full;
+            std::vector<EriReq> reqs;
+            long long tot = 0;
+            for (int i = done; i < n_pair; i++) {
+                EriReq q;
+                const int *sr, *sc;
+                lists(i, q.bra, q.ket, sr, sc);
+                const long long n = (long long)sum_nbfp(h, q.bra.data(), (int)q.bra.size()) *
+                                    sum_nbfp(h, q.ket.data(), (int)q.ket.size());
+                if (!idx.empty() && tot + n > (1LL << 27)) break;
+                tot += n;
+                idx.push_back(i);
+                reqs.push_back(std::move(q));
+            }
+            full.resize(idx.size());
+            for (size_t k = 0; k < idx.size(); k++) {
+                const int fc = sum_nbfp(h, reqs[k].ket.data(), (int)reqs[k].ket.size());
+                full[k].resize((size_t)sum_nbfp(h, reqs[k].bra.data(), (int)reqs[k].bra.size()) * fc);
+                reqs[k].out = full[k].data();
+                reqs[k].ld = fc;
+            }
+            if (gpu_eri_blocks(es, reqs) != 0) {
+                setup_eri_failed(h);
+                break;
+            }
+            #pragma omp parallel for schedule(dynamic, 1)
+            for (size_t k = 0; k < idx.size(); k++) {
+                const int i = idx[k];
+                std::vector<int> bra, ket;
+                const int *srow, *scol;
+                lists(i, bra, ket, srow, scol);
+                H2E_dense_mat_p blk = dmat_new(h->B_nrow[i], h->B_ncol[i]);
+                const int fc = reqs[k].ld;
+                for (int r = 0; r < blk->nrow; r++) {
+                    const double *src = full[k].data() + (size_t)(srow ? srow[r] : r) * fc;
+                    double *dst = blk->data + (size_t)r * blk->ncol;
+                    for (int c = 0; c < blk->ncol; c++) dst[c] = src[scol ? scol[c] : c];
+                }
+                h->c_B_blks[i] = compress_block(blk, h->QR_stop_tol);
+                dmat_free(&blk);
+            }
+            done += (int)idx.size();
+        }
+    }
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int i = done; i < n_pair; i++) {
+        std::vector<int> bra, ket;
+        const int *srow = nullptr, *scol = nullptr;
+        lists(i, bra, ket, srow, scol);
         H2E_dense_mat_p blk = dmat_new(h->B_nrow[i], h->B_ncol[i]);
         eri_block(h, bra.data(), (int)bra.size(), ket.data(), (int)ket.size(), srow, h->B_nrow[i], scol,
                   h->B_ncol[i], blk->data);
@@ -895,36 +1042,46 @@ void build_D(H2ERI_p h)
     std::sort(order.begin(), order.end(), [&](int a, int b) {
         return (size_t)h->D_nrow[a] * h->D_ncol[a] > (size_t)h->D_nrow[b] * h->D_ncol[b];
     });
+    int done = 0;
+    if (EriSet *es = setup_eri(h)) {
+        /* dense blocks on the GPU in groups of at most 2^27 doubles, each group
+         * compressed on the host before the next is evaluated */
+        while (done < n_D) {
+            std::vector<int> grp;
+            long long tot = 0;
+            for (int t = done; t < n_D; t++) {
+                const int i = order[t];
+                const long long n = (long long)h->D_nrow[i] * h->D_ncol[i];
+                if (!grp.empty() && tot + n > (1LL << 27)) break;
+                tot += n;
+                grp.push_back(i);
+            }
+            std::vector<H2E_dense_mat_p> blks(grp.size());
+            std::vector<EriReq> reqs(grp.size());
+            for (size_t k = 0; k < grp.size(); k++) {
+                d_block_lists(h, grp[k], reqs[k].bra, reqs[k].ket, reqs[k].sym);
+                blks[k] = dmat_new(h->D_nrow[grp[k]], h->D_ncol[grp[k]]);
+                reqs[k].out = blks[k]->data;
+                reqs[k].ld = blks[k]->ncol;
+            }
+            if (gpu_eri_blocks(es, reqs) != 0) {
+                for (H2E_dense_mat_p &b : blks) dmat_free(&b);
+                setup_eri_failed(h);
+                break;
+            }
+            #pragma omp parallel for schedule(dynamic, 1)
+            for (size_t k = 0; k < grp.size(); k++) {
+                h->c_D_blks[grp[k]] = compress_block(blks[k], h->QR_stop_tol);
+                dmat_free(&blks[k]);
+            }
+            done += (int)grp.size();
+        }
+    }
     #pragma omp parallel for schedule(dynamic, 1)
-    for (int t = 0; t < n_D; t++) {
+    for (int t = done; t < n_D; t++) {
         int i = order[t];
         H2E_dense_mat_p blk = dmat_new(h->D_nrow[i], h->D_ncol[i]);
-        if (i < n_leaf) {
-            int node = h->height_nodes[i];
-            int ps = h->pt_cluster[2 * node], pe = h->pt_cluster[2 * node + 1];
-            int n = blk->nrow;
-            std::vector<double> buf(15 * 15 * 15 * 15);
-            for (int a = ps; a <= pe; a++) {
-                int ra = h->sp_bfp_sidx[a] - h->sp_bfp_sidx[ps], na = h->sp_nbfp[a];
-                const h2g_pair *pa = sp_pair(h, a);
-                for (int b = a; b <= pe; b++) {
-                    int rb = h->sp_bfp_sidx[b] - h->sp_bfp_sidx[ps], nb = h->sp_nbfp[b];
-                    h2g_eri_quartet(pa, sp_pair(h, b), buf.data());
-                    for (int x = 0; x < na; x++)
-                        for (int y = 0; y < nb; y++) {
-                            double v = buf[(size_t)x * nb + y];
-                            blk->data[(size_t)(ra + x) * n + rb + y] = v;
-                            blk->data[(size_t)(rb + y) * n + ra + x] = v;
-                        }
-                }
-            }
-        } else {
-            int n0 = h->r_inadm_pairs[2 * (i - n_leaf)], n1 = h->r_inadm_pairs[2 * (i - n_leaf) + 1];
-            std::vector<int> bra, ket;
-            for (int k = h->pt_cluster[2 * n0]; k <= h->pt_cluster[2 * n0 + 1]; k++) bra.push_back(k);
-            for (int k = h->pt_cluster[2 * n1]; k <= h->pt_cluster[2 * n1 + 1]; k++) ket.push_back(k);
-            eri_pairs_to_mat(h, (int)bra.size(), bra.data(), (int)ket.size(), ket.data(), blk->data, blk->ncol);
-        }
+        d_block_host(h, i, blk);
         h->c_D_blks[i] = compress_block(blk, h->QR_stop_tol);
         dmat_free(&blk);
     }
@@ -955,6 +1112,7 @@ void build_h2(H2ERI_p h)
     build_B(h);
     double t2 = wtime();
     build_D(h);
+    setup_eri_end();
     double t3 = wtime();
     h->timers[U_BUILD_TIMER_IDX] = t1 - t0;
     h->timers[B_BUILD_TIMER_IDX] = t2 - t1;
@@ -978,6 +1136,75 @@ extern "C" int h2g_id_rows(int nrow, int ncol, const double *A, double rel_tol, 
     dmat_free(&Um);
     ivec_free(&Jv);
     return r;
+}
+
+/* Dense near-field blocks and full coupling blocks (before compression) of
+ * a built structure from the GPU engine and from the host engine: up to
+ * max_blocks of each kind (diagonal near-field, inadmissible near-field,
+ * coupling). out: [0] largest |difference|, [1] largest |value|, [2]
+ * elements compared, [3] blocks compared. Returns 0, or an error code
+ * (no usable device: 9). */
+extern "C" int H2ERI_gpu_setup_eri_check(H2ERI_p h, int max_blocks, double *out)
+{
+    using namespace h2g;
+    if (h == nullptr || out == nullptr || max_blocks < 1) return 3;
+    if (!gpu_eri_usable()) return 9;
+    std::vector<const h2g_pair *> pairs(h->num_sp);
+    for (int i = 0; i < h->num_sp; i++) pairs[i] = sp_pair(h, i);
+    EriSet *es = nullptr;
+    int rc = gpu_eri_create(h->num_sp, pairs.data(), &es);
+    if (rc) return rc;
+    std::vector<EriReq> reqs;
+    std::vector<std::vector<double>> ref;
+    const int n_leaf = h->n_leaf_node, n_D = h->n_D;
+    auto add_d = [&](int i) {
+        EriReq q;
+        d_block_lists(h, i, q.bra, q.ket, q.sym);
+        H2E_dense_mat_p blk = dmat_new(h->D_nrow[i], h->D_ncol[i]);
+        d_block_host(h, i, blk);
+        ref.emplace_back(blk->data, blk->data + (size_t)blk->nrow * blk->ncol);
+        q.ld = blk->ncol;
+        dmat_free(&blk);
+        reqs.push_back(std::move(q));
+    };
+    for (int i = 0; i < std::min(max_blocks, n_leaf); i++) add_d(i);
+    for (int i = n_leaf; i < std::min(n_D, n_leaf + max_blocks); i++) add_d(i);
+    for (int i = 0; i < std::min(max_blocks, h->n_r_adm_pair); i++) {
+        EriReq q;
+        int n0 = h->r_adm_pairs[2 * i], n1 = h->r_adm_pairs[2 * i + 1];
+        int l0 = h->node_level[n0], l1 = h->node_level[n1];
+        if (l0 >= l1) q.bra.assign(h->J_pair[n0]->data, h->J_pair[n0]->data + h->J_pair[n0]->length);
+        else for (int k = h->pt_cluster[2 * n0]; k <= h->pt_cluster[2 * n0 + 1]; k++) q.bra.push_back(h->index_seq[k]);
+        if (l0 <= l1) q.ket.assign(h->J_pair[n1]->data, h->J_pair[n1]->data + h->J_pair[n1]->length);
+        else for (int k = h->pt_cluster[2 * n1]; k <= h->pt_cluster[2 * n1 + 1]; k++) q.ket.push_back(h->index_seq[k]);
+        const int fr = sum_nbfp(h, q.bra.data(), (int)q.bra.size()), fc = sum_nbfp(h, q.ket.data(), (int)q.ket.size());
+        std::vector<double> full((size_t)fr * fc);
+        eri_pairs_to_mat(h, (int)q.bra.size(), q.bra.data(), (int)q.ket.size(), q.ket.data(), full.data(), fc);
+        ref.push_back(std::move(full));
+        q.ld = fc;
+        reqs.push_back(std::move(q));
+    }
+    std::vector<std::vector<double>> got(reqs.size());
+    for (size_t k = 0; k < reqs.size(); k++) {
+        got[k].assign(ref[k].size(), std::nan(""));
+        reqs[k].out = got[k].data();
+    }
+    rc = gpu_eri_blocks(es, reqs);
+    gpu_eri_free(es);
+    if (rc) return rc;
+    double dmax = 0.0, vmax = 0.0, n = 0.0;
+    for (size_t k = 0; k < reqs.size(); k++)
+        for (size_t e = 0; e < ref[k].size(); e++) {
+            const double d = std::fabs(got[k][e] - ref[k][e]);
+            dmax = std::isnan(d) ? INFINITY : std::max(dmax, d);
+            vmax = std::max(vmax, std::fabs(ref[k][e]));
+            n += 1.0;
+        }
+    out[0] = dmax;
+    out[1] = vmax;
+    out[2] = n;
+    out[3] = (double)reqs.size();
+    return 0;
 }
 
 extern "C" void H2ERI_build_H2(H2ERI_p h2eri, const int BD_JIT)

@@ -101,6 +101,25 @@ static void init_tables(void)
 
 void h2g_ints_init(void) { pthread_once(&g_once, init_tables); }
 
+int h2g_ints_tables(int *lxyz, int *cum, int *dir, int *prev, int *prev2, int *minus, int *plus, double *boys,
+                    int *dims)
+{
+    h2g_ints_init();
+    dims[0] = H2G_MAX_L;
+    dims[1] = H2G_MAXCUM;
+    dims[2] = BOYS_NGRID;
+    dims[3] = BOYS_MTAB;
+    if (lxyz) memcpy(lxyz, g_lxyz, sizeof(g_lxyz));
+    if (cum) memcpy(cum, g_cum, sizeof(g_cum));
+    if (dir) memcpy(dir, g_dir, sizeof(g_dir));
+    if (prev) memcpy(prev, g_prev, sizeof(g_prev));
+    if (prev2) memcpy(prev2, g_prev2, sizeof(g_prev2));
+    if (minus) memcpy(minus, g_minus, sizeof(g_minus));
+    if (plus) memcpy(plus, g_plus, sizeof(g_plus));
+    if (boys) memcpy(boys, g_boys_tab, sizeof(g_boys_tab));
+    return 0;
+}
+
 void h2g_boys(int mmax, double T, double *F)
 {
     if (T < BOYS_TMAX) {

@@ -87,6 +87,15 @@ void h2g_normalize_shell(int am, int nprim, const double *alpha, double *coef);
 /* Initialise the Boys-function table (thread-safe, idempotent). */
 void h2g_ints_init(void);
 
+/* Copies of the engine's tables, for a device implementation of the same
+ * recurrences: Cartesian components over total L <= 2 * H2G_MAX_AM
+ * (lxyz[c][3], cum[L + 2] first index of each L, dir / prev / prev2 of the
+ * recurrence, minus[c][3] / plus[c][3] neighbours) and the Boys-function grid
+ * (boys[k][m], k over 0, 0.05, ..., 40). dims gets {max L, components,
+ * grid points, orders per grid point}; a NULL table is skipped. */
+int h2g_ints_tables(int *lxyz, int *cum, int *dir, int *prev, int *prev2, int *minus, int *plus, double *boys,
+                    int *dims);
+
 #ifdef __cplusplus
 }
 #endif

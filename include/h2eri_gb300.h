@@ -188,6 +188,18 @@ int H2ERI_matvec_device_noalloc(H2ERI_p h2eri, const double *d_x, double *d_y, v
  * values written, or < 0. */
 int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n);
 
+/* Set-up on the GPU (no counterpart in the reference): when a CUDA device is
+ * present and H2G_SETUP_GPU is not 0, H2ERI_build_H2 evaluates the dense
+ * near-field (D) and full coupling (B) blocks of electron-repulsion
+ * integrals on the GPU (same recurrences and tables as the host engine;
+ * shells up to d) and compresses them on the host as before. This check
+ * evaluates up to max_blocks blocks of each kind (diagonal near-field,
+ * inadmissible near-field, coupling) of a built structure with both
+ * engines: out[0] largest |difference|, out[1] largest |value|, out[2]
+ * elements compared, out[3] blocks compared. Returns 0, 9 without a usable
+ * device, or another error code. */
+int H2ERI_gpu_setup_eri_check(H2ERI_p h2eri, int max_blocks, double *out);
+
 /* Figures of the device copy, for reports. out[0] kernel launches per matvec
  * call (one vector block), out[1] algorithmic matrix bytes read per matvec,
  * out[2] algorithmic vector bytes per vector, out[3] flops per vector,
