@@ -25,6 +25,7 @@
  * structure with higher angular momentum stays on the host engine.
  */
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -441,6 +442,7 @@ using namespace eri;
 
 /* Device state of one structure's shell pairs for the set-up. */
 struct EriSet {
+    int device = 0;   /* the device the shell pairs live on (set in every calling thread) */
     Ssp *ssp = nullptr;
     double *P = nullptr, *pe = nullptr, *K = nullptr, *ip = nullptr;
     std::vector<Ssp> host;
@@ -470,6 +472,7 @@ int gpu_eri_create(int n_sp, const h2g_pair *const *pairs, EriSet **out)
     if (rc) return rc;
     EriSet *s = new EriSet();
     s->n_sp = n_sp;
+    cudaGetDevice(&s->device);
     std::vector<double> P, pe, K, ip;
     for (int i = 0; i < n_sp; i++) {
         const h2g_pair *pr = pairs[i];
@@ -513,6 +516,10 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
 
 int gpu_eri_blocks(EriSet *s, std::vector<EriReq> &reqs)
 {
+    if (cudaSetDevice(s->device) != cudaSuccess) {
+        set_error("gpu eri: cannot select the device of the shell pairs");
+        return 10;
+    }
     Tables *t;
     int rc = ensure_tables(&t);
     if (rc) return rc;
@@ -580,24 +587,17 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
     }
     const long long total = boff.back();
     if (total == 0) return 0;
-    double *dout = nullptr;
-    Task *dtasks = nullptr;
-    int *dvoff = nullptr;
-    size_t max_tasks = 0;
-    for (auto &v : by_cls) max_tasks = std::max(max_tasks, v.size());
-    auto fail = [&](const char *m) {
-        cudaFree(dout); cudaFree(dtasks); cudaFree(dvoff);
-        set_error(std::string("gpu eri: ") + m);
-        return 10;
-    };
-    if (cudaMalloc(&dout, (size_t)total * sizeof(double)) != cudaSuccess) return fail("output allocation");
-    if (cudaMalloc(&dtasks, std::max<size_t>(max_tasks, 1) * sizeof(Task)) != cudaSuccess) return fail("task allocation");
-    if (cudaMalloc(&dvoff, (size_t)ncum(2 * kMaxAm) * ncum(2 * kMaxAm) * sizeof(int)) != cudaSuccess)
-        return fail("table allocation");
+    /* every class's tasks and table offsets in one upload */
+    std::vector<Task> all_tasks;
+    std::vector<int> all_voff;
+    struct Launch { Cls C; size_t t0, nt; int warps; };
+    std::vector<Launch> launches;
+    size_t smem_need = 0;
     int dev = 0, smem_max = 0, n_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    std::vector<size_t> voff_at;
     for (int la = 0; la < nc; la++)
         for (int lb = 0; lb < nc; lb++)
             for (int lc = 0; lc < nc; lc++)
@@ -605,35 +605,86 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
                     std::vector<Task> &v = by_cls[((la * nc + lb) * nc + lc) * nc + ld];
                     if (v.empty()) continue;
                     std::vector<int> voff;
-                    Cls C = make_class(*t, la, lb, lc, ld, voff);
-                    const size_t ws_bytes = (size_t)C.ws * sizeof(double);
-                    int warps = (int)std::min<size_t>(kWarps, (size_t)smem_max / std::max<size_t>(ws_bytes, 1));
-                    if (warps < 1) return fail("workspace of a quartet class exceeds shared memory");
-                    if (cudaMemcpy(dvoff, voff.data(), voff.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
-                        cudaMemcpy(dtasks, v.data(), v.size() * sizeof(Task), cudaMemcpyHostToDevice) != cudaSuccess)
-                        return fail("class upload");
-                    C.voff = dvoff;
-                    const size_t smem = ws_bytes * warps;
-                    if (cudaFuncSetAttribute(k_eri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-                        cudaSuccess)
-                        return fail("shared-memory attribute");
-                    const long long blocks = std::min<long long>(((long long)v.size() + warps - 1) / warps,
-                                                                 (long long)n_sm * 32);
-                    k_eri<<<(unsigned)blocks, 32 * warps, smem>>>(C, dtasks, (int)v.size(), s->ssp, s->P, s->pe, s->K,
-                                                                  s->ip, t->boys, dout);
-                    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
-                        return fail("kernel");
+                    Launch L;
+                    L.C = make_class(*t, la, lb, lc, ld, voff);
+                    const size_t ws_bytes = (size_t)L.C.ws * sizeof(double);
+                    L.warps = (int)std::min<size_t>(kWarps, (size_t)smem_max / std::max<size_t>(ws_bytes, 1));
+                    if (L.warps < 1) {
+                        set_error("gpu eri: workspace of a quartet class exceeds shared memory");
+                        return 10;
+                    }
+                    smem_need = std::max(smem_need, ws_bytes * L.warps);
+                    L.t0 = all_tasks.size();
+                    L.nt = v.size();
+                    all_tasks.insert(all_tasks.end(), v.begin(), v.end());
+                    voff_at.push_back(all_voff.size());
+                    all_voff.insert(all_voff.end(), voff.begin(), voff.end());
+                    launches.push_back(L);
                 }
+    double *dout = nullptr;
+    Task *dtasks = nullptr;
+    int *dvoff = nullptr;
+    constexpr int kStreams = 8;
+    cudaStream_t st[kStreams] = {};
+    auto fail = [&](const char *m) {
+        for (cudaStream_t x : st)
+            if (x) cudaStreamDestroy(x);
+        cudaFree(dout); cudaFree(dtasks); cudaFree(dvoff);
+        set_error(std::string("gpu eri: ") + m);
+        return 10;
+    };
+    const auto tk0 = std::chrono::steady_clock::now();
+    if (cudaMalloc(&dout, (size_t)total * sizeof(double)) != cudaSuccess) return fail("output allocation");
+    if (cudaMalloc(&dtasks, all_tasks.size() * sizeof(Task)) != cudaSuccess) return fail("task allocation");
+    if (cudaMalloc(&dvoff, all_voff.size() * sizeof(int)) != cudaSuccess) return fail("table allocation");
+    if (cudaMemcpy(dtasks, all_tasks.data(), all_tasks.size() * sizeof(Task), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dvoff, all_voff.data(), all_voff.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail("upload");
+    if (cudaFuncSetAttribute(k_eri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need) != cudaSuccess)
+        return fail("shared-memory attribute");
+    for (cudaStream_t &x : st)
+        if (cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) return fail("stream");
+    /* classes in order of decreasing work on round-robin streams, so that the
+     * small classes run beside the large ones */
+    std::vector<size_t> ord(launches.size());
+    for (size_t k = 0; k < ord.size(); k++) ord[k] = k;
+    std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+        return (double)launches[a].nt * launches[a].C.T > (double)launches[b].nt * launches[b].C.T;
+    });
+    for (size_t k = 0; k < ord.size(); k++) {
+        Launch &L = launches[ord[k]];
+        L.C.voff = dvoff + voff_at[ord[k]];
+        const size_t smem = (size_t)L.C.ws * sizeof(double) * L.warps;
+        const long long blocks = std::min<long long>(((long long)L.nt + L.warps - 1) / L.warps, (long long)n_sm * 32);
+        k_eri<<<(unsigned)blocks, 32 * L.warps, smem, st[k % kStreams]>>>(L.C, dtasks + L.t0, (int)L.nt, s->ssp, s->P,
+                                                                          s->pe, s->K, s->ip, t->boys, dout);
+        if (cudaGetLastError() != cudaSuccess) return fail("kernel launch");
+    }
+    for (cudaStream_t x : st)
+        if (cudaStreamSynchronize(x) != cudaSuccess) return fail("kernel");
+    for (cudaStream_t &x : st) {
+        cudaStreamDestroy(x);
+        x = nullptr;
+    }
+    const double kms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tk0).count();
+    const auto tc0 = std::chrono::steady_clock::now();
     std::vector<double> host((size_t)total);
     if (cudaMemcpy(host.data(), dout, (size_t)total * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
         return fail("copy back");
     cudaFree(dout); cudaFree(dtasks); cudaFree(dvoff);
+    dout = nullptr; dtasks = nullptr; dvoff = nullptr;
+    const auto tc1 = std::chrono::steady_clock::now();
     for (size_t r = 0; r < reqs.size(); r++) {
         EriReq &q = reqs[r];
         for (int i = 0; i < q.nrow; i++)
             std::memcpy(q.out + (size_t)i * q.ld, host.data() + boff[r] + (size_t)i * q.ncol,
                         sizeof(double) * q.ncol);
     }
+    const auto tc2 = std::chrono::steady_clock::now();
+    if (const char *v = std::getenv("H2G_SETUP_VERBOSE"); v && v[0] == '1')
+        std::fprintf(stderr, "gpu eri: %zu blocks, %.1f M integrals, %zu quartets: kernels %.1f ms, copy %.1f ms, "
+                             "scatter %.1f ms\n", reqs.size(), total / 1e6, all_tasks.size(), kms, std::chrono::duration<double, std::milli>(tc1 - tc0).count(),
+                     std::chrono::duration<double, std::milli>(tc2 - tc1).count());
     return 0;
 }
 

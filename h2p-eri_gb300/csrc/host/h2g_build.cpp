@@ -11,7 +11,10 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <string>
+#include <thread>
 #include <vector>
 #include <omp.h>
 
@@ -842,6 +845,13 @@ void d_block_host(H2ERI_p h, int i, H2E_dense_mat_p blk)
     }
 }
 
+/* H2G_SETUP_VERBOSE=1: timings of the set-up's phases on stderr. */
+bool setup_verbose()
+{
+    const char *v = std::getenv("H2G_SETUP_VERBOSE");
+    return v != nullptr && v[0] == '1';
+}
+
 /* The set-up's ERI blocks on the GPU (when gpu_eri_usable(): a CUDA device
  * and H2G_SETUP_GPU not 0): the structure's shell pairs, uploaded on first
  * use and kept until the set-up ends; nullptr means the host engine. */
@@ -879,6 +889,55 @@ void setup_eri_end()
 {
     if (g_seri.es) gpu_eri_free(g_seri.es);
     g_seri = SetupEri();
+}
+
+/* Groups of ERI blocks evaluated on the GPU one group ahead of their use on
+ * the host: while use(g, reqs) runs for group g in the calling thread
+ * (compression), a worker thread evaluates group g + 1. prep(g, reqs) fills
+ * the requests of group g. Returns the number of groups used; a GPU failure
+ * stops the pipeline, and discard(g, reqs) releases a prepared group that
+ * was not used. */
+template <class Prep, class Use, class Discard>
+int gpu_pipeline(H2ERI_p h, EriSet *es, int n_groups, Prep prep, Use use, Discard discard)
+{
+    if (n_groups == 0) return 0;
+    std::vector<EriReq> cur, nxt;
+    prep(0, cur);
+    const double t0 = wtime();
+    int rc = gpu_eri_blocks(es, cur);
+    double t_gpu_first = wtime() - t0, t_use = 0.0, t_wait = 0.0;
+    int g = 0;
+    for (; g < n_groups; g++) {
+        if (rc != 0) {
+            discard(g, cur);
+            setup_eri_failed(h);
+            break;
+        }
+        int rc_next = 0;
+        std::string msg_next;   /* error messages are per thread */
+        std::thread th;
+        if (g + 1 < n_groups) {
+            nxt.clear();
+            prep(g + 1, nxt);
+            th = std::thread([&] {
+                rc_next = gpu_eri_blocks(es, nxt);
+                if (rc_next) msg_next = H2ERI_gpu_last_error();
+            });
+        }
+        const double tu = wtime();
+        use(g, cur);
+        const double tw = wtime();
+        if (th.joinable()) th.join();
+        t_use += tw - tu;
+        t_wait += wtime() - tw;
+        std::swap(cur, nxt);
+        rc = rc_next;
+        if (rc) std::fprintf(stderr, "h2eri_gb300: GPU integral blocks: %s\n", msg_next.c_str());
+    }
+    if (setup_verbose())
+        std::fprintf(stderr, "gpu pipeline: %d groups, first group on the GPU %.3f s, host use %.3f s, waiting for "
+                     "the GPU %.3f s\n", g, t_gpu_first, t_use, t_wait);
+    return g;
 }
 
 /* Coupling blocks (src/H2ERI_build_H2.c:910-1152). */
@@ -931,52 +990,62 @@ void build_B(H2ERI_p h)
     int done = 0;
     if (EriSet *es = setup_eri(h)) {
         /* full blocks on the GPU in groups of at most 2^27 doubles, rows and
-         * columns selected and blocks compressed on the host */
-        while (done < n_pair) {
-            std::vector<int> idx;
-            std::vector<std::vector<double>> full;
-            std::vector<EriReq> reqs;
-            long long tot = 0;
-            for (int i = done; i < n_pair; i++) {
+         * columns selected and blocks compressed on the host, the next group
+         * evaluated meanwhile */
+        std::vector<int> gstart(1, 0);
+        long long tot = 0;
+        for (int i = 0; i < n_pair; i++) {
+            std::vector<int> bra, ket;
+            const int *sr, *sc;
+            lists(i, bra, ket, sr, sc);
+            const long long n = (long long)sum_nbfp(h, bra.data(), (int)bra.size()) *
+                                sum_nbfp(h, ket.data(), (int)ket.size());
+            if (i > gstart.back() && tot + n > (1LL << 27)) {
+                gstart.push_back(i);
+                tot = 0;
+            }
+            tot += n;
+        }
+        gstart.push_back(n_pair);
+        const int n_groups = (int)gstart.size() - 1;
+        std::vector<std::vector<std::vector<double>>> full(2);
+        auto prep = [&](int g, std::vector<EriReq> &reqs) {
+            std::vector<std::vector<double>> &f = full[g & 1];
+            f.clear();
+            for (int i = gstart[g]; i < gstart[g + 1]; i++) {
                 EriReq q;
                 const int *sr, *sc;
                 lists(i, q.bra, q.ket, sr, sc);
-                const long long n = (long long)sum_nbfp(h, q.bra.data(), (int)q.bra.size()) *
-                                    sum_nbfp(h, q.ket.data(), (int)q.ket.size());
-                if (!idx.empty() && tot + n > (1LL << 27)) break;
-                tot += n;
-                idx.push_back(i);
+                const int fc = sum_nbfp(h, q.ket.data(), (int)q.ket.size());
+                f.emplace_back((size_t)sum_nbfp(h, q.bra.data(), (int)q.bra.size()) * fc);
+                q.ld = fc;
                 reqs.push_back(std::move(q));
             }
-            full.resize(idx.size());
-            for (size_t k = 0; k < idx.size(); k++) {
-                const int fc = sum_nbfp(h, reqs[k].ket.data(), (int)reqs[k].ket.size());
-                full[k].resize((size_t)sum_nbfp(h, reqs[k].bra.data(), (int)reqs[k].bra.size()) * fc);
-                reqs[k].out = full[k].data();
-                reqs[k].ld = fc;
-            }
-            if (gpu_eri_blocks(es, reqs) != 0) {
-                setup_eri_failed(h);
-                break;
-            }
+            for (size_t k = 0; k < reqs.size(); k++) reqs[k].out = f[k].data();
+        };
+        auto use = [&](int g, std::vector<EriReq> &reqs) {
+            std::vector<std::vector<double>> &f = full[g & 1];
             #pragma omp parallel for schedule(dynamic, 1)
-            for (size_t k = 0; k < idx.size(); k++) {
-                const int i = idx[k];
+            for (int k = 0; k < (int)reqs.size(); k++) {
+                const int i = gstart[g] + k;
                 std::vector<int> bra, ket;
                 const int *srow, *scol;
                 lists(i, bra, ket, srow, scol);
                 H2E_dense_mat_p blk = dmat_new(h->B_nrow[i], h->B_ncol[i]);
                 const int fc = reqs[k].ld;
                 for (int r = 0; r < blk->nrow; r++) {
-                    const double *src = full[k].data() + (size_t)(srow ? srow[r] : r) * fc;
+                    const double *src = f[k].data() + (size_t)(srow ? srow[r] : r) * fc;
                     double *dst = blk->data + (size_t)r * blk->ncol;
                     for (int c = 0; c < blk->ncol; c++) dst[c] = src[scol ? scol[c] : c];
                 }
                 h->c_B_blks[i] = compress_block(blk, h->QR_stop_tol);
                 dmat_free(&blk);
             }
-            done += (int)idx.size();
-        }
+            f.clear();
+        };
+        auto discard = [&](int g, std::vector<EriReq> &) { full[g & 1].clear(); };
+        const int used = gpu_pipeline(h, es, n_groups, prep, use, discard);
+        done = gstart[used];
     }
     #pragma omp parallel for schedule(dynamic, 1)
     for (int i = done; i < n_pair; i++) {
@@ -1045,38 +1114,50 @@ void build_D(H2ERI_p h)
     int done = 0;
     if (EriSet *es = setup_eri(h)) {
         /* dense blocks on the GPU in groups of at most 2^27 doubles, each group
-         * compressed on the host before the next is evaluated */
-        while (done < n_D) {
-            std::vector<int> grp;
-            long long tot = 0;
-            for (int t = done; t < n_D; t++) {
-                const int i = order[t];
-                const long long n = (long long)h->D_nrow[i] * h->D_ncol[i];
-                if (!grp.empty() && tot + n > (1LL << 27)) break;
-                tot += n;
-                grp.push_back(i);
+         * compressed on the host while the next is evaluated */
+        std::vector<int> gstart(1, 0);
+        long long tot = 0;
+        for (int t = 0; t < n_D; t++) {
+            const long long n = (long long)h->D_nrow[order[t]] * h->D_ncol[order[t]];
+            if (t > gstart.back() && tot + n > (1LL << 27)) {
+                gstart.push_back(t);
+                tot = 0;
             }
-            std::vector<H2E_dense_mat_p> blks(grp.size());
-            std::vector<EriReq> reqs(grp.size());
-            for (size_t k = 0; k < grp.size(); k++) {
-                d_block_lists(h, grp[k], reqs[k].bra, reqs[k].ket, reqs[k].sym);
-                blks[k] = dmat_new(h->D_nrow[grp[k]], h->D_ncol[grp[k]]);
-                reqs[k].out = blks[k]->data;
-                reqs[k].ld = blks[k]->ncol;
-            }
-            if (gpu_eri_blocks(es, reqs) != 0) {
-                for (H2E_dense_mat_p &b : blks) dmat_free(&b);
-                setup_eri_failed(h);
-                break;
-            }
-            #pragma omp parallel for schedule(dynamic, 1)
-            for (size_t k = 0; k < grp.size(); k++) {
-                h->c_D_blks[grp[k]] = compress_block(blks[k], h->QR_stop_tol);
-                dmat_free(&blks[k]);
-            }
-            done += (int)grp.size();
+            tot += n;
         }
+        gstart.push_back(n_D);
+        const int n_groups = (int)gstart.size() - 1;
+        std::vector<std::vector<H2E_dense_mat_p>> blks(2);
+        auto prep = [&](int g, std::vector<EriReq> &reqs) {
+            std::vector<H2E_dense_mat_p> &b = blks[g & 1];
+            b.clear();
+            for (int t = gstart[g]; t < gstart[g + 1]; t++) {
+                const int i = order[t];
+                EriReq q;
+                d_block_lists(h, i, q.bra, q.ket, q.sym);
+                b.push_back(dmat_new(h->D_nrow[i], h->D_ncol[i]));
+                q.out = b.back()->data;
+                q.ld = b.back()->ncol;
+                reqs.push_back(std::move(q));
+            }
+        };
+        auto use = [&](int g, std::vector<EriReq> &) {
+            std::vector<H2E_dense_mat_p> &b = blks[g & 1];
+            #pragma omp parallel for schedule(dynamic, 1)
+            for (int k = 0; k < (int)b.size(); k++) {
+                h->c_D_blks[order[gstart[g] + k]] = compress_block(b[k], h->QR_stop_tol);
+                dmat_free(&b[k]);
+            }
+            b.clear();
+        };
+        auto discard = [&](int g, std::vector<EriReq> &) {
+            for (H2E_dense_mat_p &x : blks[g & 1]) dmat_free(&x);
+            blks[g & 1].clear();
+        };
+        const int used = gpu_pipeline(h, es, n_groups, prep, use, discard);
+        done = gstart[used];
     }
+    const double th = wtime();
     #pragma omp parallel for schedule(dynamic, 1)
     for (int t = done; t < n_D; t++) {
         int i = order[t];
@@ -1085,6 +1166,9 @@ void build_D(H2ERI_p h)
         h->c_D_blks[i] = compress_block(blk, h->QR_stop_tol);
         dmat_free(&blk);
     }
+    if (setup_verbose() && done < n_D)
+        std::fprintf(stderr, "build_D: %d blocks on the host engine (integrals and compression) %.3f s\n", n_D - done,
+                     wtime() - th);
     h->mat_size[MV_DEN_SIZE_IDX] = 0;
     h->D_ptr[0] = 0;
     std::vector<size_t> sizes(std::max(n_D, 1));
@@ -1142,8 +1226,10 @@ extern "C" int h2g_id_rows(int nrow, int ncol, const double *A, double rel_tol, 
  * a built structure from the GPU engine and from the host engine: up to
  * max_blocks of each kind (diagonal near-field, inadmissible near-field,
  * coupling). out: [0] largest |difference|, [1] largest |value|, [2]
- * elements compared, [3] blocks compared. Returns 0, or an error code
- * (no usable device: 9). */
+ * elements compared, [3] blocks compared, [4] seconds of the GPU evaluation
+ * (with the copy back), [5] seconds of the host engine (one thread, with the
+ * host-side bookkeeping of the check). Returns 0, or an error code (no
+ * usable device: 9). */
 extern "C" int H2ERI_gpu_setup_eri_check(H2ERI_p h, int max_blocks, double *out)
 {
     using namespace h2g;
@@ -1167,6 +1253,8 @@ extern "C" int H2ERI_gpu_setup_eri_check(H2ERI_p h, int max_blocks, double *out)
         dmat_free(&blk);
         reqs.push_back(std::move(q));
     };
+    double t_host = 0.0;
+    const double th0 = wtime();
     for (int i = 0; i < std::min(max_blocks, n_leaf); i++) add_d(i);
     for (int i = n_leaf; i < std::min(n_D, n_leaf + max_blocks); i++) add_d(i);
     for (int i = 0; i < std::min(max_blocks, h->n_r_adm_pair); i++) {
@@ -1184,12 +1272,15 @@ extern "C" int H2ERI_gpu_setup_eri_check(H2ERI_p h, int max_blocks, double *out)
         q.ld = fc;
         reqs.push_back(std::move(q));
     }
+    t_host = wtime() - th0;
     std::vector<std::vector<double>> got(reqs.size());
     for (size_t k = 0; k < reqs.size(); k++) {
         got[k].assign(ref[k].size(), std::nan(""));
         reqs[k].out = got[k].data();
     }
+    const double tg0 = wtime();
     rc = gpu_eri_blocks(es, reqs);
+    const double t_gpu = wtime() - tg0;
     gpu_eri_free(es);
     if (rc) return rc;
     double dmax = 0.0, vmax = 0.0, n = 0.0;
@@ -1204,6 +1295,8 @@ extern "C" int H2ERI_gpu_setup_eri_check(H2ERI_p h, int max_blocks, double *out)
     out[1] = vmax;
     out[2] = n;
     out[3] = (double)reqs.size();
+    out[4] = t_gpu;
+    out[5] = t_host;
     return 0;
 }
 

@@ -196,8 +196,9 @@ int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n);
  * evaluates up to max_blocks blocks of each kind (diagonal near-field,
  * inadmissible near-field, coupling) of a built structure with both
  * engines: out[0] largest |difference|, out[1] largest |value|, out[2]
- * elements compared, out[3] blocks compared. Returns 0, 9 without a usable
- * device, or another error code. */
+ * elements compared, out[3] blocks compared, out[4] seconds on the GPU,
+ * out[5] seconds on the host engine (one thread); out needs 6 values.
+ * Returns 0, 9 without a usable device, or another error code. */
 int H2ERI_gpu_setup_eri_check(H2ERI_p h2eri, int max_blocks, double *out);
 
 /* Figures of the device copy, for reports. out[0] kernel launches per matvec
