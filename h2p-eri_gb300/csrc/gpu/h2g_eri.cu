@@ -82,6 +82,7 @@ struct Cls {
     int A;        /* contracted [e|f] entries for the HRR        */
     int lvl;      /* largest HRR level array                     */
     int lane_ok;  /* lanes may take primitive quartets           */
+    int lstride;  /* doubles per lane in lane mode (odd: no bank conflicts between lanes) */
     int ws;       /* workspace doubles per warp                  */
     const int *voff;   /* compact offsets [ne * nf] (device)     */
 };
@@ -113,6 +114,22 @@ __device__ void boys(int mmax, double T, const double *__restrict__ tab, double 
         F[0] = 0.5 * sqrt(M_PI / T);
         for (int m = 0; m < mmax; m++) F[m + 1] = ((2 * m + 1) * F[m] - et) * inv2t;
     }
+}
+
+/* F_m(T) for one order m and T < 40: the same grid and Taylor step as boys(). */
+__device__ double boys_one(int m, double T, const double *__restrict__ tab)
+{
+    const int k = (int)(T / kBoysH + 0.5);
+    const double d = T - k * kBoysH;
+    const double *row = tab + (size_t)k * kBoysTab + m;
+    const double inv_fact[7] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720};
+    double pw = 1.0, s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        s += __ldg(row + j) * (pw * inv_fact[j]);
+        pw *= -d;
+    }
+    return s;
 }
 
 /* Scalars of one primitive quartet (p from the bra pair, q from the ket). */
@@ -291,7 +308,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_eri(Cls C, const Task *__restri
         __syncwarp();
         if (C.lane_ok && nq >= 8) {
             /* lanes over primitive quartets, each with its own table and sums */
-            double *V = scr + (size_t)lane * (C.T + C.A);
+            double *V = scr + (size_t)lane * C.lstride;
             double *la = V + C.T;
             for (int a = 0; a < C.A; a++) la[a] = 0.0;
             for (int qi = lane; qi < nq; qi += 32) {
@@ -307,7 +324,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_eri(Cls C, const Task *__restri
             __syncwarp();
             for (int a = lane; a < C.A; a += 32) {
                 double s = 0.0;
-                for (int l = 0; l < 32; l++) s += scr[(size_t)l * (C.T + C.A) + C.T + a];
+                for (int l = 0; l < 32; l++) s += scr[(size_t)l * C.lstride + C.T + a];
                 acc[a] = s;
             }
             __syncwarp();
@@ -317,7 +334,9 @@ __global__ void __launch_bounds__(32 * kWarps) k_eri(Cls C, const Task *__restri
             for (int qi = 0; qi < nq; qi++) {
                 Prim q;
                 prim_setup(bra, ket, qi / nk, qi % nk, P, pe, K, ip, q);
-                if (lane == 0) {
+                if (q.T < kBoysTmax) {
+                    if (lane <= C.M) V[lane] = q.pref * boys_one(lane, q.T, boys_tab);   /* one order per lane */
+                } else if (lane == 0) {
                     double F[4 * kMaxAm + 1];
                     boys(C.M, q.T, boys_tab, F);
                     for (int m = 0; m <= C.M; m++) V[m] = q.pref * F[m];
@@ -430,8 +449,9 @@ Cls make_class(const Tables &t, int la, int lb, int lc, int ld, std::vector<int>
     for (int j = 1; j <= ld; j++) lvl = std::max(lvl, (t.cum[lc + ld - j + 1] - f0) * ncart(j) * nab);
     lvl = std::max(lvl, nab * ncart(lc) * ncart(ld));   /* R */
     C.lvl = lvl;
-    const int lane_need = 32 * (C.T + C.A);
-    C.lane_ok = lane_need <= 4096;
+    C.lstride = (C.T + C.A) | 1;
+    const int lane_need = 32 * C.lstride;
+    C.lane_ok = lane_need <= 20480;   /* 160 KB per warp at most */
     C.ws = C.A + std::max({C.lane_ok ? lane_need : 0, C.T, 4 * lvl});
     return C;
 }

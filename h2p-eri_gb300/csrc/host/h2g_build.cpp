@@ -556,6 +556,8 @@ int sum_nbfp(H2ERI_p h, const int *idx, int n)
 }
 
 /* Nested bases U and skeleton sets (src/H2ERI_build_H2.c:351-827). */
+bool setup_verbose();
+
 void build_UJ_proxy(H2ERI_p h)
 {
     const int n_node = h->n_node, n_point = h->n_point, n_leaf = h->n_leaf_node;
@@ -572,6 +574,8 @@ void build_UJ_proxy(H2ERI_p h)
         for (int lv = h->node_level[leaf] + 1; lv <= max_level; lv++) lvl_leaf[lv].push_back(leaf);
     }
     calc_ovlp_ff_idx(h);
+    /* thread seconds per phase (reported with H2G_SETUP_VERBOSE=1) */
+    double t_nai = 0.0, t_eri = 0.0, t_id = 0.0;
 
     for (int lv = max_level; lv >= min_adm; lv--) {
         const int nlv = h->level_n_node[lv];
@@ -621,6 +625,7 @@ void build_UJ_proxy(H2ERI_p h)
             std::vector<double> Ablk((size_t)nrow_blk * ncol_blk, 0.0);
             Rng rng(0x5eed0000ULL + (uint64_t)node * 7919ULL);
             /* (4) potential of proxy points, sketched to nrow_blk columns */
+            const double tp0 = wtime();
             {
                 Sketch s;
                 gen_sketch(16, num_pp, nrow_blk, rng, s);
@@ -638,6 +643,7 @@ void build_UJ_proxy(H2ERI_p h)
                 nai_pairs_to_mat(h, (int)pair_idx.size(), pair_idx.data(), cnt, ppx, ppy, ppz, Apot.data(), cnt);
                 sketch_apply(nrow_blk, s, Apot.data(), cnt, Ablk.data(), ncol_blk);
             }
+            const double tp1 = wtime();
             /* (5) ERI with overlapping far-field SSPs, sketched to nrow_blk columns */
             {
                 Sketch s;
@@ -662,6 +668,7 @@ void build_UJ_proxy(H2ERI_p h)
                     rcnt += nb;
                 }
             }
+            const double tp2 = wtime();
             /* (6) normalise columns, keep candidate rows, ID */
             {
                 std::vector<double> inv(ncol_blk, 0.0);
@@ -697,6 +704,13 @@ void build_UJ_proxy(H2ERI_p h)
                 h->J_row[node] = jr;
                 ivec_free(&J);
             }
+            const double tp3 = wtime();
+            #pragma omp atomic
+            t_nai += tp1 - tp0;
+            #pragma omp atomic
+            t_eri += tp2 - tp1;
+            #pragma omp atomic
+            t_id += tp3 - tp2;
         }
         /* skeleton flags for the next level up */
         std::fill(skel.begin(), skel.end(), 0);
@@ -707,6 +721,9 @@ void build_UJ_proxy(H2ERI_p h)
         for (int leaf : lvl_leaf[lv])
             for (int k = h->pt_cluster[2 * leaf]; k <= h->pt_cluster[2 * leaf + 1]; k++) skel[k] = 1;
     }
+    if (setup_verbose())
+        std::fprintf(stderr, "build_U: thread seconds: proxy-point potentials %.2f, far-field ERI %.2f, ID %.2f\n",
+                     t_nai, t_eri, t_id);
     for (int i = 0; i < n_node; i++) {
         if (h->U[i] == nullptr) {
             h->U[i] = dmat_new(1, 1);
@@ -1000,7 +1017,7 @@ void build_B(H2ERI_p h)
             lists(i, bra, ket, sr, sc);
             const long long n = (long long)sum_nbfp(h, bra.data(), (int)bra.size()) *
                                 sum_nbfp(h, ket.data(), (int)ket.size());
-            if (i > gstart.back() && tot + n > (1LL << 27)) {
+            if (i > gstart.back() && tot + n > (gstart.size() == 1 ? (1LL << 25) : (1LL << 27))) {
                 gstart.push_back(i);
                 tot = 0;
             }
@@ -1119,7 +1136,7 @@ void build_D(H2ERI_p h)
         long long tot = 0;
         for (int t = 0; t < n_D; t++) {
             const long long n = (long long)h->D_nrow[order[t]] * h->D_ncol[order[t]];
-            if (t > gstart.back() && tot + n > (1LL << 27)) {
+            if (t > gstart.back() && tot + n > (gstart.size() == 1 ? (1LL << 25) : (1LL << 27))) {
                 gstart.push_back(t);
                 tot = 0;
             }
