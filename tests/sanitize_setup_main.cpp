@@ -1,15 +1,24 @@
 /* Host set-up driver for the sanitizer test (tests/test_sanitize_setup_cpu.py):
  * the reference call sequence up to H2ERI_build_H2 and a save/load round
  * trip, built from the host sources alone with AddressSanitizer and
- * UndefinedBehaviorSanitizer. The two GPU-side hooks the host code calls are
- * stubbed (nothing is uploaded here). */
+ * UndefinedBehaviorSanitizer. The GPU-side hooks the host code calls are
+ * stubbed (nothing is uploaded here, and the set-up's integral blocks stay on
+ * the host engine). */
 #include <cstdio>
 #include <cstdlib>
 
 #include "h2eri_gb300.h"
+#include "h2g_eri.h"
 
 extern "C" void H2ERI_gpu_release(H2ERI_p) {}
 extern "C" void h2g_gpu_print_statistic(H2ERI_p) {}
+extern "C" const char *H2ERI_gpu_last_error(void) { return "no GPU in this build"; }
+namespace h2g {
+int gpu_eri_usable() { return 0; }
+int gpu_eri_create(int, const h2g_pair *const *, EriSet **out) { *out = nullptr; return 1; }
+int gpu_eri_blocks(EriSet *, std::vector<EriReq> &) { return 1; }
+void gpu_eri_free(EriSet *) {}
+}  // namespace h2g
 
 int main(int argc, char **argv)
 {
