@@ -564,38 +564,40 @@ int gpu_eri_blocks(EriSet *s, std::vector<EriReq> &reqs)
     return 0;
 }
 
-static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_req)
+/* One block of quartets in a device buffer: rows = bf pairs of bra[0..nbra),
+ * columns = those of ket[0..nket), element (r, c) at off + r * ld + c; with
+ * sym only quartets with bra position <= ket position, mirrored. */
+struct BlockSpec {
+    const int *bra, *ket;
+    int nbra, nket;
+    bool sym;
+    long long off;
+    int ld;
+};
+
+/* Evaluate the quartets of blocks into dout (device): one launch per quartet
+ * class, classes on round-robin streams in order of decreasing work (so
+ * that the small classes run beside the large ones); returns after the
+ * kernels end. kms gets the milliseconds of the launches. */
+static int launch_eri(EriSet *s, Tables *t, const std::vector<BlockSpec> &blocks, double *dout, double *kms)
 {
-    struct View {
-        EriReq *p; size_t n;
-        size_t size() const { return n; }
-        EriReq &operator[](size_t k) { return p[k]; }
-    } reqs{reqs_begin, n_req};
     const int nc = kMaxAm + 1;
     std::vector<std::vector<Task>> by_cls((size_t)nc * nc * nc * nc);
-    std::vector<long long> boff(reqs.size() + 1, 0);
     auto nbfp = [&](int sp) { return ncart(s->host[sp].am1) * ncart(s->host[sp].am2); };
-    for (size_t r = 0; r < reqs.size(); r++) {
-        EriReq &q = reqs[r];
-        int nr = 0, ncl = 0;
-        for (int b : q.bra) nr += nbfp(b);
-        for (int k : q.ket) ncl += nbfp(k);
-        q.nrow = nr;
-        q.ncol = ncl;
-        boff[r + 1] = boff[r] + (long long)nr * ncl;
+    for (const BlockSpec &q : blocks) {
         int row = 0;
-        for (size_t i = 0; i < q.bra.size(); i++) {
+        for (int i = 0; i < q.nbra; i++) {
             const int b = q.bra[i];
             int col = 0;
-            for (size_t j = 0; j < q.ket.size(); j++) {
+            for (int j = 0; j < q.nket; j++) {
                 const int k = q.ket[j];
                 if (!q.sym || i <= j) {
                     Task tk;
                     tk.bra = b;
                     tk.ket = k;
-                    tk.off = boff[r] + (long long)row * ncl + col;
-                    tk.off_t = (q.sym && i < j) ? boff[r] + (long long)col * ncl + row : -1;
-                    tk.ld = ncl;
+                    tk.off = q.off + (long long)row * q.ld + col;
+                    tk.off_t = (q.sym && i < j) ? q.off + (long long)col * q.ld + row : -1;
+                    tk.ld = q.ld;
                     tk.pad_ = 0;
                     const Ssp &B = s->host[b], &Kt = s->host[k];
                     by_cls[((B.am1 * nc + B.am2) * nc + Kt.am1) * nc + Kt.am2].push_back(tk);
@@ -605,8 +607,7 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
             row += nbfp(b);
         }
     }
-    const long long total = boff.back();
-    if (total == 0) return 0;
+    *kms = 0.0;
     /* every class's tasks and table offsets in one upload */
     std::vector<Task> all_tasks;
     std::vector<int> all_voff;
@@ -641,7 +642,7 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
                     all_voff.insert(all_voff.end(), voff.begin(), voff.end());
                     launches.push_back(L);
                 }
-    double *dout = nullptr;
+    if (launches.empty()) return 0;
     Task *dtasks = nullptr;
     int *dvoff = nullptr;
     constexpr int kStreams = 8;
@@ -649,12 +650,11 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
     auto fail = [&](const char *m) {
         for (cudaStream_t x : st)
             if (x) cudaStreamDestroy(x);
-        cudaFree(dout); cudaFree(dtasks); cudaFree(dvoff);
+        cudaFree(dtasks); cudaFree(dvoff);
         set_error(std::string("gpu eri: ") + m);
         return 10;
     };
     const auto tk0 = std::chrono::steady_clock::now();
-    if (cudaMalloc(&dout, (size_t)total * sizeof(double)) != cudaSuccess) return fail("output allocation");
     if (cudaMalloc(&dtasks, all_tasks.size() * sizeof(Task)) != cudaSuccess) return fail("task allocation");
     if (cudaMalloc(&dvoff, all_voff.size() * sizeof(int)) != cudaSuccess) return fail("table allocation");
     if (cudaMemcpy(dtasks, all_tasks.data(), all_tasks.size() * sizeof(Task), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -664,8 +664,6 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
         return fail("shared-memory attribute");
     for (cudaStream_t &x : st)
         if (cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) return fail("stream");
-    /* classes in order of decreasing work on round-robin streams, so that the
-     * small classes run beside the large ones */
     std::vector<size_t> ord(launches.size());
     for (size_t k = 0; k < ord.size(); k++) ord[k] = k;
     std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
@@ -675,9 +673,9 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
         Launch &L = launches[ord[k]];
         L.C.voff = dvoff + voff_at[ord[k]];
         const size_t smem = (size_t)L.C.ws * sizeof(double) * L.warps;
-        const long long blocks = std::min<long long>(((long long)L.nt + L.warps - 1) / L.warps, (long long)n_sm * 32);
-        k_eri<<<(unsigned)blocks, 32 * L.warps, smem, st[k % kStreams]>>>(L.C, dtasks + L.t0, (int)L.nt, s->ssp, s->P,
-                                                                          s->pe, s->K, s->ip, t->boys, dout);
+        const long long nblk = std::min<long long>(((long long)L.nt + L.warps - 1) / L.warps, (long long)n_sm * 32);
+        k_eri<<<(unsigned)nblk, 32 * L.warps, smem, st[k % kStreams]>>>(L.C, dtasks + L.t0, (int)L.nt, s->ssp, s->P,
+                                                                        s->pe, s->K, s->ip, t->boys, dout);
         if (cudaGetLastError() != cudaSuccess) return fail("kernel launch");
     }
     for (cudaStream_t x : st)
@@ -686,25 +684,370 @@ static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs_begin, size_t n_r
         cudaStreamDestroy(x);
         x = nullptr;
     }
-    const double kms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tk0).count();
+    cudaFree(dtasks);
+    cudaFree(dvoff);
+    *kms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tk0).count();
+    return 0;
+}
+
+static bool setup_verbose_env()
+{
+    const char *v = std::getenv("H2G_SETUP_VERBOSE");
+    return v != nullptr && v[0] == '1';
+}
+
+static int eri_blocks_range(EriSet *s, Tables *t, EriReq *reqs, size_t n_req)
+{
+    auto nbfp = [&](int sp) { return ncart(s->host[sp].am1) * ncart(s->host[sp].am2); };
+    std::vector<long long> boff(n_req + 1, 0);
+    std::vector<BlockSpec> blocks(n_req);
+    for (size_t r = 0; r < n_req; r++) {
+        EriReq &q = reqs[r];
+        int nr = 0, ncl = 0;
+        for (int b : q.bra) nr += nbfp(b);
+        for (int k : q.ket) ncl += nbfp(k);
+        q.nrow = nr;
+        q.ncol = ncl;
+        boff[r + 1] = boff[r] + (long long)nr * ncl;
+        blocks[r] = BlockSpec{q.bra.data(), q.ket.data(), (int)q.bra.size(), (int)q.ket.size(), q.sym, boff[r], ncl};
+    }
+    const long long total = boff.back();
+    if (total == 0) return 0;
+    double *dout = nullptr;
+    if (cudaMalloc(&dout, (size_t)total * sizeof(double)) != cudaSuccess) {
+        set_error("gpu eri: output allocation");
+        return 10;
+    }
+    double kms = 0.0;
+    int rc = launch_eri(s, t, blocks, dout, &kms);
+    if (rc) {
+        cudaFree(dout);
+        return rc;
+    }
     const auto tc0 = std::chrono::steady_clock::now();
     std::vector<double> host((size_t)total);
-    if (cudaMemcpy(host.data(), dout, (size_t)total * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return fail("copy back");
-    cudaFree(dout); cudaFree(dtasks); cudaFree(dvoff);
-    dout = nullptr; dtasks = nullptr; dvoff = nullptr;
+    rc = cudaMemcpy(host.data(), dout, (size_t)total * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess ? 0 : 10;
+    cudaFree(dout);
+    if (rc) {
+        set_error("gpu eri: copy back");
+        return rc;
+    }
     const auto tc1 = std::chrono::steady_clock::now();
-    for (size_t r = 0; r < reqs.size(); r++) {
+    for (size_t r = 0; r < n_req; r++) {
         EriReq &q = reqs[r];
         for (int i = 0; i < q.nrow; i++)
             std::memcpy(q.out + (size_t)i * q.ld, host.data() + boff[r] + (size_t)i * q.ncol,
                         sizeof(double) * q.ncol);
     }
     const auto tc2 = std::chrono::steady_clock::now();
-    if (const char *v = std::getenv("H2G_SETUP_VERBOSE"); v && v[0] == '1')
-        std::fprintf(stderr, "gpu eri: %zu blocks, %.1f M integrals, %zu quartets: kernels %.1f ms, copy %.1f ms, "
-                             "scatter %.1f ms\n", reqs.size(), total / 1e6, all_tasks.size(), kms, std::chrono::duration<double, std::milli>(tc1 - tc0).count(),
+    if (setup_verbose_env())
+        std::fprintf(stderr, "gpu eri: %zu blocks, %.1f M integrals: kernels %.1f ms, copy %.1f ms, scatter %.1f ms\n",
+                     n_req, total / 1e6, kms, std::chrono::duration<double, std::milli>(tc1 - tc0).count(),
                      std::chrono::duration<double, std::milli>(tc2 - tc1).count());
+    return 0;
+}
+
+/* ---- proxy-point potentials and sketches for the nested bases ---- */
+
+namespace eri {
+
+constexpr int kNaiL = 2 * kMaxAm;                                 /* la + lb  */
+constexpr int kNaiV = 70;        /* compact [e]^(m), m <= L - |e|, for L = 4 */
+constexpr int kNaiAcc = 31;      /* [e] for la <= |e| <= L (la = 2, L = 4)   */
+constexpr int kNaiLvl = 48;      /* largest HRR level (la = lb = 2, j = 1)   */
+
+/* One bra shell pair against a run of point charges: rows of the pair at
+ * out_off (leading dimension ld), one column per point. */
+struct NaiTask {
+    int sp, npt;
+    long long pt_off, out_off;
+    int ld, pad_;
+};
+
+/* Potential integrals -<a| 1/|r - C| |b> of unit point charges: one thread
+ * per point, the pair's primitive pairs in order. Obara-Saika recurrence
+ * [e + 1_i]^(m) = PA_i [e]^(m) - PC_i [e]^(m+1) + e_i / (2p) ([e - 1_i]^(m)
+ * - [e - 1_i]^(m+1)) from [0]^(m) = -2 pi / p K F_m(p |PC|^2), contraction,
+ * then the horizontal recurrence to (a, b) - the host engine's
+ * h2g_potential_points, point by point. */
+__global__ void __launch_bounds__(128) k_nai(const NaiTask *__restrict__ tasks, const Ssp *__restrict__ ssp,
+                                             const double *__restrict__ P, const double *__restrict__ pe,
+                                             const double *__restrict__ K, const double *__restrict__ boys_tab,
+                                             const double *__restrict__ px, const double *__restrict__ py,
+                                             const double *__restrict__ pz, double *__restrict__ out)
+{
+    const NaiTask tk = tasks[blockIdx.x];
+    const Ssp pr = ssp[tk.sp];
+    const int la = pr.am1, lb = pr.am2, L = la + lb;
+    const int ne = c_cum[L + 1], e0 = c_cum[la];
+    const int na = ncart(la), nb = ncart(lb);
+    /* compact offsets of [e]^(m): components of total l hold L - l + 1 orders */
+    int loff[kNaiL + 2];
+    loff[0] = 0;
+    for (int l = 0; l <= L; l++) loff[l + 1] = loff[l] + ncart(l) * (L - l + 1);
+    const double AB[3] = {pr.A[0] - pr.B[0], pr.A[1] - pr.B[1], pr.A[2] - pr.B[2]};
+    for (int pt = threadIdx.x; pt < tk.npt; pt += blockDim.x) {
+        const double C[3] = {px[tk.pt_off + pt], py[tk.pt_off + pt], pz[tk.pt_off + pt]};
+        double acc[kNaiAcc];
+        for (int e = 0; e < ne - e0; e++) acc[e] = 0.0;
+        double V[kNaiV];
+        for (int k = 0; k < pr.nprim; k++) {
+            const int pi = pr.poff + k;
+            const double p = pe[pi];
+            double PA[3], PC[3], PC2 = 0.0;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const double Pd = P[3 * pi + d];
+                PA[d] = Pd - pr.A[d];
+                PC[d] = Pd - C[d];
+                PC2 += PC[d] * PC[d];
+            }
+            double F[kNaiL + 1];
+            boys(L, p * PC2, boys_tab, F);
+            const double pref = -1.0 * 2.0 * M_PI / p * K[pi];
+            for (int m = 0; m <= L; m++) V[m] = pref * F[m];
+            const double i2p = 0.5 / p;
+            for (int c = 1; c < ne; c++) {
+                const int lc = lsum(c), d = c_dir[c], e = c_prev[c], e2 = c_prev2[c];
+                const int le = lc - 1;
+                const double ei = (double)(c_lxyz[c][d] - 1);
+                double *vc = V + loff[lc] + (c - c_cum[lc]) * (L - lc + 1);
+                const double *ve = V + loff[le] + (e - c_cum[le]) * (L - le + 1);
+                if (e2 >= 0) {
+                    const int le2 = lc - 2;
+                    const double *ve2 = V + loff[le2] + (e2 - c_cum[le2]) * (L - le2 + 1);
+                    for (int m = 0; m <= L - lc; m++)
+                        vc[m] = PA[d] * ve[m] - PC[d] * ve[m + 1] + ei * i2p * (ve2[m] - ve2[m + 1]);
+                } else {
+                    for (int m = 0; m <= L - lc; m++) vc[m] = PA[d] * ve[m] - PC[d] * ve[m + 1];
+                }
+            }
+            for (int e = e0; e < ne; e++) {
+                const int le = lsum(e);
+                acc[e - e0] += V[loff[le] + (e - c_cum[le]) * (L - le + 1)];
+            }
+        }
+        /* horizontal recurrence (a, b + 1_i) = (a + 1_i, b) + AB_i (a, b) */
+        double b0[kNaiLvl], b1[kNaiLvl];
+        const double *cur = acc;
+        int nbp = 1;
+        for (int j = 1; j <= lb; j++) {
+            const int nbj = ncart(j), emax = c_cum[L - j + 1];
+            double *nxt = (j & 1) ? b0 : b1;
+            for (int e = e0; e < emax; e++)
+                for (int ib = 0; ib < nbj; ib++) {
+                    const int bf = c_cum[j] + ib, d = c_dir[bf], bp = c_prev[bf] - c_cum[j - 1];
+                    const int ep = c_plus[e][d];
+                    nxt[(e - e0) * nbj + ib] = cur[(ep - e0) * nbp + bp] + AB[d] * cur[(e - e0) * nbp + bp];
+                }
+            cur = nxt;
+            nbp = nbj;
+        }
+        for (int ab = 0; ab < na * nb; ab++) out[tk.out_off + (long long)ab * tk.ld + pt] = cur[ab];
+    }
+}
+
+/* Columns of a sparse sign sketch: Y[i][j] = sum_l val[j][l] X[i][col[j][l]]
+ * for i < nrow, j < n (the host sketch_apply, same order of sums). */
+struct SkJob {
+    long long x_off, s_off, y_off;
+    int ldx, nrow, nnz, n, ldy, pad_;
+};
+
+__global__ void __launch_bounds__(256) k_sketch(const SkJob *__restrict__ jobs, const double *__restrict__ X,
+                                                const int *__restrict__ scol, const double *__restrict__ sval,
+                                                double *__restrict__ Y)
+{
+    const SkJob jb = jobs[blockIdx.y];
+    const long long total = (long long)jb.nrow * jb.n;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / jb.n), j = (int)(idx - (long long)i * jb.n);
+        const double *xi = X + jb.x_off + (long long)i * jb.ldx;
+        const int *c = scol + jb.s_off + (long long)j * jb.nnz;
+        const double *v = sval + jb.s_off + (long long)j * jb.nnz;
+        double r = 0.0;
+        for (int l = 0; l < jb.nnz; l++) r += v[l] * xi[c[l]];
+        Y[jb.y_off + (long long)i * jb.ldy + j] = r;
+    }
+}
+
+}  // namespace eri
+
+static int u_blocks_range(EriSet *s, Tables *t, UReq *reqs, size_t n_req);
+
+int gpu_u_blocks(EriSet *s, std::vector<UReq> &reqs)
+{
+    if (cudaSetDevice(s->device) != cudaSuccess) {
+        set_error("gpu eri: cannot select the device of the shell pairs");
+        return 10;
+    }
+    Tables *t;
+    int rc = ensure_tables(&t);
+    if (rc) return rc;
+    auto nbfp = [&](int sp) { return ncart(s->host[sp].am1) * ncart(s->host[sp].am2); };
+    for (UReq &q : reqs) {
+        q.nrow = 0;
+        for (int i = 0; i < q.nbra; i++) {
+            if (q.bra[i] < 0 || q.bra[i] >= s->n_sp) { set_error("gpu eri: shell pair out of range"); return 3; }
+            q.nrow += nbfp(q.bra[i]);
+        }
+        q.ncol_ff = 0;
+        for (int i = 0; i < q.nket; i++) {
+            if (q.ket[i] < 0 || q.ket[i] >= s->n_sp) { set_error("gpu eri: shell pair out of range"); return 3; }
+            q.ncol_ff += nbfp(q.ket[i]);
+        }
+        /* every sketch index must address a column of its block */
+        for (long long k = 0; k < (long long)q.nrow * q.s1_nnz; k++)
+            if (q.s1_col[k] < 0 || q.s1_col[k] >= q.npt) { set_error("gpu eri: sketch column out of range"); return 3; }
+        for (long long k = 0; k < (long long)q.nrow * q.s2_nnz; k++)
+            if (q.s2_col[k] < 0 || q.s2_col[k] >= q.ncol_ff) { set_error("gpu eri: sketch column out of range"); return 3; }
+    }
+    /* requests in groups of at most 2^27 doubles of unsketched blocks */
+    size_t i = 0;
+    while (i < reqs.size()) {
+        size_t j = i;
+        long long tot = 0;
+        while (j < reqs.size()) {
+            const long long n = (long long)reqs[j].nrow * (reqs[j].npt + reqs[j].ncol_ff);
+            if (j > i && tot + n > (1LL << 27)) break;
+            tot += n;
+            j++;
+        }
+        rc = u_blocks_range(s, t, reqs.data() + i, j - i);
+        if (rc) return rc;
+        i = j;
+    }
+    return 0;
+}
+
+static int u_blocks_range(EriSet *s, Tables *t, UReq *reqs, size_t n_req)
+{
+    auto nbfp = [&](int sp) { return ncart(s->host[sp].am1) * ncart(s->host[sp].am2); };
+    /* device layout: X = [potential block | ERI block] per request, A =
+     * nrow x 2 nrow per request, points and sketches concatenated */
+    std::vector<long long> xn(n_req), xe(n_req), ao(n_req + 1, 0), po(n_req), s1o(n_req), s2o(n_req);
+    long long nx = 0, np = 0, ns = 0;
+    std::vector<BlockSpec> blocks;
+    std::vector<NaiTask> nai;
+    std::vector<SkJob> jobs;
+    for (size_t r = 0; r < n_req; r++) {
+        const UReq &q = reqs[r];
+        xn[r] = nx;
+        nx += (long long)q.nrow * q.npt;
+        xe[r] = nx;
+        nx += (long long)q.nrow * q.ncol_ff;
+        ao[r + 1] = ao[r] + 2LL * q.nrow * q.nrow;
+        po[r] = np;
+        np += q.npt;
+        s1o[r] = ns;
+        ns += (long long)q.nrow * q.s1_nnz;
+        s2o[r] = ns;
+        ns += (long long)q.nrow * q.s2_nnz;
+        if (q.nrow == 0) continue;
+        if (q.nket > 0) blocks.push_back(BlockSpec{q.bra, q.ket, q.nbra, q.nket, false, xe[r], q.ncol_ff});
+        int row = 0;
+        for (int b = 0; b < q.nbra; b++) {
+            if (q.npt > 0) nai.push_back(NaiTask{q.bra[b], q.npt, po[r], xn[r] + (long long)row * q.npt, q.npt, 0});
+            row += nbfp(q.bra[b]);
+        }
+        jobs.push_back(SkJob{xn[r], s1o[r], ao[r], q.npt, q.nrow, q.s1_nnz, q.nrow, 2 * q.nrow, 0});
+        jobs.push_back(SkJob{xe[r], s2o[r], ao[r] + q.nrow, q.ncol_ff, q.nrow, q.s2_nnz, q.nrow, 2 * q.nrow, 0});
+    }
+    if (ao[n_req] == 0) return 0;
+    std::vector<double> pts(3 * (size_t)std::max<long long>(np, 1)), sval((size_t)std::max<long long>(ns, 1));
+    std::vector<int> scol((size_t)std::max<long long>(ns, 1));
+    for (size_t r = 0; r < n_req; r++) {
+        const UReq &q = reqs[r];
+        if (q.npt > 0) {
+            std::memcpy(pts.data() + po[r], q.px, sizeof(double) * q.npt);
+            std::memcpy(pts.data() + np + po[r], q.py, sizeof(double) * q.npt);
+            std::memcpy(pts.data() + 2 * np + po[r], q.pz, sizeof(double) * q.npt);
+        }
+        const size_t n1 = (size_t)q.nrow * q.s1_nnz, n2 = (size_t)q.nrow * q.s2_nnz;
+        if (n1 > 0) {
+            std::memcpy(scol.data() + s1o[r], q.s1_col, sizeof(int) * n1);
+            std::memcpy(sval.data() + s1o[r], q.s1_val, sizeof(double) * n1);
+        }
+        if (n2 > 0) {
+            std::memcpy(scol.data() + s2o[r], q.s2_col, sizeof(int) * n2);
+            std::memcpy(sval.data() + s2o[r], q.s2_val, sizeof(double) * n2);
+        }
+    }
+    double *dX = nullptr, *dA = nullptr, *dpts = nullptr, *dsval = nullptr;
+    int *dscol = nullptr;
+    NaiTask *dnai = nullptr;
+    SkJob *djobs = nullptr;
+    auto release = [&]() {
+        cudaFree(dX); cudaFree(dA); cudaFree(dpts); cudaFree(dsval); cudaFree(dscol); cudaFree(dnai); cudaFree(djobs);
+    };
+    auto fail = [&](const char *m) {
+        release();
+        set_error(std::string("gpu eri (nested bases): ") + m);
+        return 10;
+    };
+    const auto t0 = std::chrono::steady_clock::now();
+    if (cudaMalloc(&dX, (size_t)std::max<long long>(nx, 1) * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&dA, (size_t)ao[n_req] * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&dpts, pts.size() * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&dsval, sval.size() * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&dscol, scol.size() * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&dnai, std::max<size_t>(nai.size(), 1) * sizeof(NaiTask)) != cudaSuccess ||
+        cudaMalloc(&djobs, std::max<size_t>(jobs.size(), 1) * sizeof(SkJob)) != cudaSuccess)
+        return fail("allocation");
+    if (cudaMemcpy(dpts, pts.data(), pts.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dsval, sval.data(), sval.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dscol, scol.data(), scol.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+        (!nai.empty() && cudaMemcpy(dnai, nai.data(), nai.size() * sizeof(NaiTask), cudaMemcpyHostToDevice) != cudaSuccess) ||
+        (!jobs.empty() && cudaMemcpy(djobs, jobs.data(), jobs.size() * sizeof(SkJob), cudaMemcpyHostToDevice) != cudaSuccess))
+        return fail("upload");
+    /* potentials on a stream of their own while the ERI classes run on
+     * theirs; the sketches after both */
+    cudaStream_t sn = nullptr;
+    if (cudaStreamCreateWithFlags(&sn, cudaStreamNonBlocking) != cudaSuccess) return fail("stream");
+    auto fail_s = [&](const char *m) {
+        cudaStreamSynchronize(sn);
+        cudaStreamDestroy(sn);
+        return fail(m);
+    };
+    if (!nai.empty()) {
+        k_nai<<<(unsigned)nai.size(), 128, 0, sn>>>(dnai, s->ssp, s->P, s->pe, s->K, t->boys, dpts, dpts + np,
+                                                    dpts + 2 * np, dX);
+        if (cudaGetLastError() != cudaSuccess) return fail_s("potential kernel launch");
+    }
+    double kms = 0.0;
+    if (!blocks.empty()) {
+        const int rc = launch_eri(s, t, blocks, dX, &kms);
+        if (rc) {
+            cudaStreamSynchronize(sn);
+            cudaStreamDestroy(sn);
+            release();
+            return rc;
+        }
+    }
+    if (!jobs.empty()) {
+        dim3 grid(64, (unsigned)jobs.size());
+        k_sketch<<<grid, 256, 0, sn>>>(djobs, dX, dscol, dsval, dA);
+        if (cudaGetLastError() != cudaSuccess) return fail_s("sketch kernel launch");
+    }
+    if (cudaStreamSynchronize(sn) != cudaSuccess) return fail_s("kernels");
+    cudaStreamDestroy(sn);
+    const auto t1 = std::chrono::steady_clock::now();
+    std::vector<double> host((size_t)ao[n_req]);
+    if (cudaMemcpy(host.data(), dA, host.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail("copy back");
+    release();
+    for (size_t r = 0; r < n_req; r++) {
+        UReq &q = reqs[r];
+        const int w = 2 * q.nrow;
+        for (int i = 0; i < q.nrow; i++)
+            std::memcpy(q.out + (size_t)i * q.ld, host.data() + ao[r] + (size_t)i * w, sizeof(double) * w);
+    }
+    if (setup_verbose_env())
+        std::fprintf(stderr, "gpu nested-basis blocks: %zu nodes, %.1f M potentials + ERIs, %zu potential rows: "
+                     "kernels %.1f ms (ERI classes %.1f ms), copy back and scatter %.1f ms\n", n_req, nx / 1e6,
+                     nai.size(), std::chrono::duration<double, std::milli>(t1 - t0).count(), kms,
+                     std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count());
     return 0;
 }
 

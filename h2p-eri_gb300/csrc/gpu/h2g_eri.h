@@ -35,6 +35,32 @@ int gpu_eri_create(int n_sp, const h2g_pair *const *pairs, EriSet **out);
  * matrices. Returns 0 or an error code (message in H2ERI_gpu_last_error). */
 int gpu_eri_blocks(EriSet *s, std::vector<EriReq> &reqs);
 void gpu_eri_free(EriSet *s);
+
+/* The sketched integral matrix of one node of the nested-basis (U) set-up:
+ * rows = the bf pairs of the bra shell pairs in order; columns [0, nrow) =
+ * the potentials of npt unit point charges (px/py/pz) times a sparse sign
+ * sketch (column j = sum over l < s1_nnz of s1_val[j s1_nnz + l] times the
+ * potential column s1_col[j s1_nnz + l]); columns [nrow, 2 nrow) = the ERIs
+ * with the ket shell pairs (columns = their bf pairs in order) times the
+ * second sketch in the same form. All pointers are host memory owned by the
+ * caller; out is nrow x 2 nrow with leading dimension ld. nrow and ncol_ff
+ * (ket bf pairs) are set by the call. */
+struct UReq {
+    const int *bra = nullptr, *ket = nullptr;
+    int nbra = 0, nket = 0;
+    const double *px = nullptr, *py = nullptr, *pz = nullptr;
+    int npt = 0;
+    const int *s1_col = nullptr, *s2_col = nullptr;
+    const double *s1_val = nullptr, *s2_val = nullptr;
+    int s1_nnz = 0, s2_nnz = 0;
+    double *out = nullptr;
+    int ld = 0;
+    int nrow = 0, ncol_ff = 0;
+};
+/* Evaluate the requests on the device (potentials, ERIs and both sketches)
+ * and copy each sketched matrix into its host matrix. Returns 0 or an error
+ * code (message in H2ERI_gpu_last_error). */
+int gpu_u_blocks(EriSet *s, std::vector<UReq> &reqs);
 /* 1 when the set-up may use the GPU: a CUDA device is present and the
  * environment does not set H2G_SETUP_GPU=0. */
 int gpu_eri_usable();

@@ -555,191 +555,7 @@ int sum_nbfp(H2ERI_p h, const int *idx, int n)
     return s;
 }
 
-/* Nested bases U and skeleton sets (src/H2ERI_build_H2.c:351-827). */
 bool setup_verbose();
-
-void build_UJ_proxy(H2ERI_p h)
-{
-    const int n_node = h->n_node, n_point = h->n_point, n_leaf = h->n_leaf_node;
-    const int max_level = h->max_level, min_adm = h->min_adm_level;
-    const double rel_tol = h->QR_stop_tol;
-    h->n_UJ = n_node;
-    h->U = (H2E_dense_mat_p *)std::calloc(n_node, sizeof(H2E_dense_mat_p));
-    h->J_pair = (H2E_int_vec_p *)std::calloc(n_node, sizeof(H2E_int_vec_p));
-    h->J_row = (H2E_int_vec_p *)std::calloc(n_node, sizeof(H2E_int_vec_p));
-    std::vector<int> skel(n_point, 1);
-    std::vector<std::vector<int>> lvl_leaf(max_level + 1);
-    for (int i = 0; i < n_leaf; i++) {
-        int leaf = h->height_nodes[i];
-        for (int lv = h->node_level[leaf] + 1; lv <= max_level; lv++) lvl_leaf[lv].push_back(leaf);
-    }
-    calc_ovlp_ff_idx(h);
-    /* thread seconds per phase (reported with H2G_SETUP_VERBOSE=1) */
-    double t_nai = 0.0, t_eri = 0.0, t_id = 0.0;
-
-    for (int lv = max_level; lv >= min_adm; lv--) {
-        const int nlv = h->level_n_node[lv];
-        const int *lnodes = h->level_nodes + lv * n_leaf;
-        #pragma omp parallel for schedule(dynamic, 1)
-        for (int jn = 0; jn < nlv; jn++) {
-            const int node = lnodes[jn];
-            const int nch = h->n_child[node];
-            std::vector<int> pair_idx, row_idx;
-            /* (1) candidate rows of this node */
-            if (nch == 0) {
-                for (int k = h->pt_cluster[2 * node]; k <= h->pt_cluster[2 * node + 1]; k++)
-                    pair_idx.push_back(h->index_seq[k]);
-                int nb = sum_nbfp(h, pair_idx.data(), (int)pair_idx.size());
-                for (int k = 0; k < nb; k++) row_idx.push_back(k);
-            } else {
-                int roff = 0;
-                for (int k = 0; k < nch; k++) {
-                    int c = h->children[node * h->max_child + k];
-                    for (int t = 0; t < h->J_pair[c]->length; t++) pair_idx.push_back(h->J_pair[c]->data[t]);
-                    for (int t = 0; t < h->J_row[c]->length; t++) row_idx.push_back(h->J_row[c]->data[t] + roff);
-                    roff += sum_nbfp(h, h->J_pair[c]->data, h->J_pair[c]->length);
-                }
-            }
-            /* (2) proxy points around the node box */
-            const double *eb = h->enbox + 6 * node;
-            double width = eb[3], extent = h->box_extent[node];
-            double r1 = width * (0.5 + H2G_ALPHA_SUP), r2 = width * (0.5 + extent);
-            int nlayer = std::max(1, 1 + (int)std::ceil((extent - H2G_ALPHA_SUP) * (h->pp_nlayer_ext - 1)));
-            std::vector<double> pp;
-            int num_pp;
-            proxy_points(r1, r2, nlayer, h->pp_npts_layer, pp, num_pp);
-            double *ppx = pp.data(), *ppy = ppx + num_pp, *ppz = ppy + num_pp;
-            for (int k = 0; k < num_pp; k++) {
-                ppx[k] += eb[0] + 0.5 * eb[3];
-                ppy[k] += eb[1] + 0.5 * eb[4];
-                ppz[k] += eb[2] + 0.5 * eb[5];
-            }
-            /* (3) far-field SSPs that are still skeletons */
-            std::vector<int> ff;
-            H2E_int_vec_p ov = h->ovlp_ff_idx[node];
-            for (int k = 0; k < ov->length; k++)
-                if (skel[ov->data[k]]) ff.push_back(ov->data[k]);
-            const int nrow_blk = sum_nbfp(h, pair_idx.data(), (int)pair_idx.size());
-            const int ff_ncol = sum_nbfp(h, ff.data(), (int)ff.size());
-            const int ncol_blk = 2 * nrow_blk;
-            std::vector<double> Ablk((size_t)nrow_blk * ncol_blk, 0.0);
-            Rng rng(0x5eed0000ULL + (uint64_t)node * 7919ULL);
-            /* (4) potential of proxy points, sketched to nrow_blk columns */
-            const double tp0 = wtime();
-            {
-                Sketch s;
-                gen_sketch(16, num_pp, nrow_blk, rng, s);
-                std::vector<int> map(num_pp, -1);
-                for (int c : s.col) map[c] = 1;
-                int cnt = 0;
-                for (int k = 0; k < num_pp; k++)
-                    if (map[k] >= 0) {
-                        map[k] = cnt;
-                        ppx[cnt] = ppx[k]; ppy[cnt] = ppy[k]; ppz[cnt] = ppz[k];
-                        cnt++;
-                    }
-                for (auto &c : s.col) c = map[c];
-                std::vector<double> Apot((size_t)nrow_blk * std::max(cnt, 1));
-                nai_pairs_to_mat(h, (int)pair_idx.size(), pair_idx.data(), cnt, ppx, ppy, ppz, Apot.data(), cnt);
-                sketch_apply(nrow_blk, s, Apot.data(), cnt, Ablk.data(), ncol_blk);
-            }
-            const double tp1 = wtime();
-            /* (5) ERI with overlapping far-field SSPs, sketched to nrow_blk columns */
-            {
-                Sketch s;
-                gen_sketch(16, ff_ncol, nrow_blk, rng, s);
-                std::vector<int> used(std::max(ff_ncol, 1), -1);
-                for (int c : s.col) used[c] = 1;
-                std::vector<int> cup;
-                for (int k = 0; k < ff_ncol; k++)
-                    if (used[k] >= 0) { used[k] = (int)cup.size(); cup.push_back(k); }
-                std::vector<int> pos, cup_new;
-                extract_sp_idx(h, cup.data(), (int)cup.size(), ff.data(), (int)ff.size(), pos, cup_new);
-                std::vector<int> ff1(pos.size());
-                for (size_t k = 0; k < pos.size(); k++) ff1[k] = ff[pos[k]];
-                for (auto &c : s.col) c = cup_new[used[c]];
-                const int ff_ncol1 = sum_nbfp(h, ff1.data(), (int)ff1.size());
-                std::vector<double> Aff((size_t)15 * 15 * std::max(ff_ncol1, 1));
-                int rcnt = 0;
-                for (size_t k = 0; k < pair_idx.size(); k++) {
-                    int nb = h->sp_nbfp[pair_idx[k]];
-                    eri_pairs_to_mat(h, 1, &pair_idx[k], (int)ff1.size(), ff1.data(), Aff.data(), ff_ncol1);
-                    sketch_apply(nb, s, Aff.data(), ff_ncol1, Ablk.data() + (size_t)rcnt * ncol_blk + nrow_blk, ncol_blk);
-                    rcnt += nb;
-                }
-            }
-            const double tp2 = wtime();
-            /* (6) normalise columns, keep candidate rows, ID */
-            {
-                std::vector<double> inv(ncol_blk, 0.0);
-                for (int c = 0; c < ncol_blk; c++) {
-                    double s = 0.0;
-                    for (int r = 0; r < nrow_blk; r++) s += Ablk[(size_t)r * ncol_blk + c] * Ablk[(size_t)r * ncol_blk + c];
-                    inv[c] = (s > 0.0) ? 1.0 / std::sqrt(s) : 0.0;
-                }
-                const int nsel = (int)row_idx.size();
-                H2E_dense_mat_p A = dmat_new(nsel, ncol_blk);
-                for (int r = 0; r < nsel; r++) {
-                    const double *src = Ablk.data() + (size_t)row_idx[r] * ncol_blk;
-                    double *dst = A->data + (size_t)r * ncol_blk;
-                    for (int c = 0; c < ncol_blk; c++) dst[c] = src[c] * inv[c];
-                }
-                H2E_int_vec_p J = ivec_new(std::max(nsel, 1));
-                H2E_dense_mat_p U = nullptr;
-                id_compress(A, rel_tol, &U, J);
-                dmat_free(&A);
-                h->U[node] = U;
-                /* (7) skeleton SSPs and their rows */
-                std::vector<int> sub_row(J->length);
-                for (int k = 0; k < J->length; k++) sub_row[k] = row_idx[J->data[k]];
-                std::vector<int> pos, rnew;
-                extract_sp_idx(h, sub_row.data(), (int)sub_row.size(), pair_idx.data(), (int)pair_idx.size(), pos, rnew);
-                H2E_int_vec_p jp = ivec_new(std::max((int)pos.size(), 1));
-                H2E_int_vec_p jr = ivec_new(std::max((int)rnew.size(), 1));
-                for (size_t k = 0; k < pos.size(); k++) jp->data[k] = pair_idx[pos[k]];
-                jp->length = (int)pos.size();
-                for (size_t k = 0; k < rnew.size(); k++) jr->data[k] = rnew[k];
-                jr->length = (int)rnew.size();
-                h->J_pair[node] = jp;
-                h->J_row[node] = jr;
-                ivec_free(&J);
-            }
-            const double tp3 = wtime();
-            #pragma omp atomic
-            t_nai += tp1 - tp0;
-            #pragma omp atomic
-            t_eri += tp2 - tp1;
-            #pragma omp atomic
-            t_id += tp3 - tp2;
-        }
-        /* skeleton flags for the next level up */
-        std::fill(skel.begin(), skel.end(), 0);
-        for (int jn = 0; jn < nlv; jn++) {
-            int node = lnodes[jn];
-            for (int k = 0; k < h->J_pair[node]->length; k++) skel[h->J_pair[node]->data[k]] = 1;
-        }
-        for (int leaf : lvl_leaf[lv])
-            for (int k = h->pt_cluster[2 * leaf]; k <= h->pt_cluster[2 * leaf + 1]; k++) skel[k] = 1;
-    }
-    if (setup_verbose())
-        std::fprintf(stderr, "build_U: thread seconds: proxy-point potentials %.2f, far-field ERI %.2f, ID %.2f\n",
-                     t_nai, t_eri, t_id);
-    for (int i = 0; i < n_node; i++) {
-        if (h->U[i] == nullptr) {
-            h->U[i] = dmat_new(1, 1);
-            h->U[i]->nrow = 0;
-            h->U[i]->ncol = 0;
-            h->U[i]->ld = 0;
-        } else {
-            size_t nr = h->U[i]->nrow, nc = h->U[i]->ncol;
-            h->mat_size[U_SIZE_IDX] += nr * nc;
-            h->mat_size[MV_FWD_SIZE_IDX] += nr * nc + nr + nc;
-            h->mat_size[MV_BWD_SIZE_IDX] += nr * nc + nr + nc;
-        }
-        if (h->J_row[i] == nullptr) h->J_row[i] = ivec_new(1);
-        if (h->J_pair[i] == nullptr) h->J_pair[i] = ivec_new(1);
-    }
-}
 
 /* Dense block -> dense or low-rank storage (src/H2ERI_build_H2.c:843-903). */
 H2E_dense_mat_p compress_block(H2E_dense_mat_p blk, double rel_tol)
@@ -914,14 +730,14 @@ void setup_eri_end()
  * the requests of group g. Returns the number of groups used; a GPU failure
  * stops the pipeline, and discard(g, reqs) releases a prepared group that
  * was not used. */
-template <class Prep, class Use, class Discard>
-int gpu_pipeline(H2ERI_p h, EriSet *es, int n_groups, Prep prep, Use use, Discard discard)
+template <class Req, class Eval, class Prep, class Use, class Discard>
+int gpu_pipeline(H2ERI_p h, int n_groups, Eval eval, Prep prep, Use use, Discard discard)
 {
     if (n_groups == 0) return 0;
-    std::vector<EriReq> cur, nxt;
+    std::vector<Req> cur, nxt;
     prep(0, cur);
     const double t0 = wtime();
-    int rc = gpu_eri_blocks(es, cur);
+    int rc = eval(cur);
     double t_gpu_first = wtime() - t0, t_use = 0.0, t_wait = 0.0;
     int g = 0;
     for (; g < n_groups; g++) {
@@ -937,7 +753,7 @@ int gpu_pipeline(H2ERI_p h, EriSet *es, int n_groups, Prep prep, Use use, Discar
             nxt.clear();
             prep(g + 1, nxt);
             th = std::thread([&] {
-                rc_next = gpu_eri_blocks(es, nxt);
+                rc_next = eval(nxt);
                 if (rc_next) msg_next = H2ERI_gpu_last_error();
             });
         }
@@ -955,6 +771,304 @@ int gpu_pipeline(H2ERI_p h, EriSet *es, int n_groups, Prep prep, Use use, Discar
         std::fprintf(stderr, "gpu pipeline: %d groups, first group on the GPU %.3f s, host use %.3f s, waiting for "
                      "the GPU %.3f s\n", g, t_gpu_first, t_use, t_wait);
     return g;
+}
+
+/* ---- nested bases U and skeleton sets (src/H2ERI_build_H2.c:351-827) ----
+ *
+ * Per node, from the leaves up: the candidate rows (all bf pairs of a leaf,
+ * the children's skeleton rows otherwise), a matrix of their integrals with
+ * proxy point charges around the node box and with the overlapping
+ * far-field shell pairs, each side reduced to nrow columns by a sparse sign
+ * sketch, then an interpolative decomposition of the column-normalised
+ * candidate rows. The integrals and sketches run on the GPU when the set-up
+ * may use it (gpu_eri_usable), a level's nodes in groups, the next group on
+ * the GPU while the host decomposes the current one; otherwise on the host
+ * engine. */
+
+/* One node's inputs and its sketched matrix (nrow_blk x 2 nrow_blk). */
+struct UNode {
+    int node = -1;
+    std::vector<int> pair_idx, row_idx;
+    int nrow_blk = 0;
+    std::vector<double> pp;   /* the proxy points a sketch uses: [x | y | z], cnt each */
+    int cnt = 0;
+    Sketch s1, s2;            /* columns into the points / into ff1's bf pairs */
+    std::vector<int> ff1;     /* far-field shell pairs a sketch uses */
+    int ff_ncol1 = 0;
+    std::vector<double> A;
+};
+
+/* Candidate rows, proxy points, far-field pairs and both sketches of node
+ * (the host path's order of random draws: potentials' sketch first). */
+void u_prep(H2ERI_p h, int node, const std::vector<int> &skel, UNode &w)
+{
+    w.node = node;
+    const int nch = h->n_child[node];
+    w.pair_idx.clear();
+    w.row_idx.clear();
+    /* (1) candidate rows of this node */
+    if (nch == 0) {
+        for (int k = h->pt_cluster[2 * node]; k <= h->pt_cluster[2 * node + 1]; k++)
+            w.pair_idx.push_back(h->index_seq[k]);
+        int nb = sum_nbfp(h, w.pair_idx.data(), (int)w.pair_idx.size());
+        for (int k = 0; k < nb; k++) w.row_idx.push_back(k);
+    } else {
+        int roff = 0;
+        for (int k = 0; k < nch; k++) {
+            int c = h->children[node * h->max_child + k];
+            for (int t = 0; t < h->J_pair[c]->length; t++) w.pair_idx.push_back(h->J_pair[c]->data[t]);
+            for (int t = 0; t < h->J_row[c]->length; t++) w.row_idx.push_back(h->J_row[c]->data[t] + roff);
+            roff += sum_nbfp(h, h->J_pair[c]->data, h->J_pair[c]->length);
+        }
+    }
+    /* (2) proxy points around the node box */
+    const double *eb = h->enbox + 6 * node;
+    double width = eb[3], extent = h->box_extent[node];
+    double r1 = width * (0.5 + H2G_ALPHA_SUP), r2 = width * (0.5 + extent);
+    int nlayer = std::max(1, 1 + (int)std::ceil((extent - H2G_ALPHA_SUP) * (h->pp_nlayer_ext - 1)));
+    int num_pp;
+    proxy_points(r1, r2, nlayer, h->pp_npts_layer, w.pp, num_pp);
+    double *ppx = w.pp.data(), *ppy = ppx + num_pp, *ppz = ppy + num_pp;
+    for (int k = 0; k < num_pp; k++) {
+        ppx[k] += eb[0] + 0.5 * eb[3];
+        ppy[k] += eb[1] + 0.5 * eb[4];
+        ppz[k] += eb[2] + 0.5 * eb[5];
+    }
+    /* (3) far-field SSPs that are still skeletons */
+    std::vector<int> ff;
+    H2E_int_vec_p ov = h->ovlp_ff_idx[node];
+    for (int k = 0; k < ov->length; k++)
+        if (skel[ov->data[k]]) ff.push_back(ov->data[k]);
+    w.nrow_blk = sum_nbfp(h, w.pair_idx.data(), (int)w.pair_idx.size());
+    const int ff_ncol = sum_nbfp(h, ff.data(), (int)ff.size());
+    Rng rng(0x5eed0000ULL + (uint64_t)node * 7919ULL);
+    /* (4) sketch of the proxy-point potentials; only the points it uses stay */
+    gen_sketch(16, num_pp, w.nrow_blk, rng, w.s1);
+    {
+        std::vector<int> map(num_pp, -1);
+        for (int c : w.s1.col) map[c] = 1;
+        int cnt = 0;
+        for (int k = 0; k < num_pp; k++)
+            if (map[k] >= 0) {
+                map[k] = cnt;
+                ppx[cnt] = ppx[k]; ppy[cnt] = ppy[k]; ppz[cnt] = ppz[k];
+                cnt++;
+            }
+        for (auto &c : w.s1.col) c = map[c];
+        std::vector<double> q((size_t)3 * cnt);
+        std::memcpy(q.data(), ppx, sizeof(double) * cnt);
+        std::memcpy(q.data() + cnt, ppy, sizeof(double) * cnt);
+        std::memcpy(q.data() + 2 * cnt, ppz, sizeof(double) * cnt);
+        w.pp.swap(q);
+        w.cnt = cnt;
+    }
+    /* (5) sketch of the ERIs with the far-field SSPs; only the SSPs it uses stay */
+    gen_sketch(16, ff_ncol, w.nrow_blk, rng, w.s2);
+    {
+        std::vector<int> used(std::max(ff_ncol, 1), -1);
+        for (int c : w.s2.col) used[c] = 1;
+        std::vector<int> cup;
+        for (int k = 0; k < ff_ncol; k++)
+            if (used[k] >= 0) { used[k] = (int)cup.size(); cup.push_back(k); }
+        std::vector<int> pos, cup_new;
+        extract_sp_idx(h, cup.data(), (int)cup.size(), ff.data(), (int)ff.size(), pos, cup_new);
+        w.ff1.resize(pos.size());
+        for (size_t k = 0; k < pos.size(); k++) w.ff1[k] = ff[pos[k]];
+        for (auto &c : w.s2.col) c = cup_new[used[c]];
+        w.ff_ncol1 = sum_nbfp(h, w.ff1.data(), (int)w.ff1.size());
+    }
+    w.A.assign((size_t)w.nrow_blk * 2 * w.nrow_blk, 0.0);
+}
+
+/* The node's sketched matrix on the host engine. */
+void u_integrals_host(H2ERI_p h, UNode &w, double &t_nai, double &t_eri)
+{
+    const int nrow_blk = w.nrow_blk, ncol_blk = 2 * nrow_blk, cnt = w.cnt;
+    const double tp0 = wtime();
+    {
+        std::vector<double> Apot((size_t)nrow_blk * std::max(cnt, 1));
+        nai_pairs_to_mat(h, (int)w.pair_idx.size(), w.pair_idx.data(), cnt, w.pp.data(), w.pp.data() + cnt,
+                         w.pp.data() + 2 * cnt, Apot.data(), cnt);
+        sketch_apply(nrow_blk, w.s1, Apot.data(), cnt, w.A.data(), ncol_blk);
+    }
+    const double tp1 = wtime();
+    {
+        std::vector<double> Aff((size_t)15 * 15 * std::max(w.ff_ncol1, 1));
+        int rcnt = 0;
+        for (size_t k = 0; k < w.pair_idx.size(); k++) {
+            int nb = h->sp_nbfp[w.pair_idx[k]];
+            eri_pairs_to_mat(h, 1, &w.pair_idx[k], (int)w.ff1.size(), w.ff1.data(), Aff.data(), w.ff_ncol1);
+            sketch_apply(nb, w.s2, Aff.data(), w.ff_ncol1, w.A.data() + (size_t)rcnt * ncol_blk + nrow_blk, ncol_blk);
+            rcnt += nb;
+        }
+    }
+    const double tp2 = wtime();
+    #pragma omp atomic
+    t_nai += tp1 - tp0;
+    #pragma omp atomic
+    t_eri += tp2 - tp1;
+}
+
+/* (6) normalise columns, keep candidate rows, ID; (7) skeleton SSPs and rows. */
+void u_finish(H2ERI_p h, UNode &w)
+{
+    const int nrow_blk = w.nrow_blk, ncol_blk = 2 * nrow_blk, node = w.node;
+    std::vector<double> &Ablk = w.A;
+    std::vector<double> inv(ncol_blk, 0.0);
+    for (int c = 0; c < ncol_blk; c++) {
+        double s = 0.0;
+        for (int r = 0; r < nrow_blk; r++) s += Ablk[(size_t)r * ncol_blk + c] * Ablk[(size_t)r * ncol_blk + c];
+        inv[c] = (s > 0.0) ? 1.0 / std::sqrt(s) : 0.0;
+    }
+    const int nsel = (int)w.row_idx.size();
+    H2E_dense_mat_p A = dmat_new(nsel, ncol_blk);
+    for (int r = 0; r < nsel; r++) {
+        const double *src = Ablk.data() + (size_t)w.row_idx[r] * ncol_blk;
+        double *dst = A->data + (size_t)r * ncol_blk;
+        for (int c = 0; c < ncol_blk; c++) dst[c] = src[c] * inv[c];
+    }
+    H2E_int_vec_p J = ivec_new(std::max(nsel, 1));
+    H2E_dense_mat_p U = nullptr;
+    id_compress(A, h->QR_stop_tol, &U, J);
+    dmat_free(&A);
+    h->U[node] = U;
+    std::vector<int> sub_row(J->length);
+    for (int k = 0; k < J->length; k++) sub_row[k] = w.row_idx[J->data[k]];
+    std::vector<int> pos, rnew;
+    extract_sp_idx(h, sub_row.data(), (int)sub_row.size(), w.pair_idx.data(), (int)w.pair_idx.size(), pos, rnew);
+    H2E_int_vec_p jp = ivec_new(std::max((int)pos.size(), 1));
+    H2E_int_vec_p jr = ivec_new(std::max((int)rnew.size(), 1));
+    for (size_t k = 0; k < pos.size(); k++) jp->data[k] = w.pair_idx[pos[k]];
+    jp->length = (int)pos.size();
+    for (size_t k = 0; k < rnew.size(); k++) jr->data[k] = rnew[k];
+    jr->length = (int)rnew.size();
+    h->J_pair[node] = jp;
+    h->J_row[node] = jr;
+    ivec_free(&J);
+    std::vector<double>().swap(w.A);
+}
+
+/* The GPU request of a prepared node (host pointers into w). */
+UReq u_request(UNode &w)
+{
+    UReq q;
+    q.bra = w.pair_idx.data();
+    q.nbra = (int)w.pair_idx.size();
+    q.ket = w.ff1.data();
+    q.nket = (int)w.ff1.size();
+    q.px = w.pp.data();
+    q.py = w.pp.data() + w.cnt;
+    q.pz = w.pp.data() + 2 * w.cnt;
+    q.npt = w.cnt;
+    q.s1_col = w.s1.col.data();
+    q.s1_val = w.s1.val.data();
+    q.s1_nnz = w.s1.nnz_col;
+    q.s2_col = w.s2.col.data();
+    q.s2_val = w.s2.val.data();
+    q.s2_nnz = w.s2.nnz_col;
+    q.out = w.A.data();
+    q.ld = 2 * w.nrow_blk;
+    return q;
+}
+
+void build_UJ_proxy(H2ERI_p h)
+{
+    const int n_node = h->n_node, n_point = h->n_point, n_leaf = h->n_leaf_node;
+    const int max_level = h->max_level, min_adm = h->min_adm_level;
+    h->n_UJ = n_node;
+    h->U = (H2E_dense_mat_p *)std::calloc(n_node, sizeof(H2E_dense_mat_p));
+    h->J_pair = (H2E_int_vec_p *)std::calloc(n_node, sizeof(H2E_int_vec_p));
+    h->J_row = (H2E_int_vec_p *)std::calloc(n_node, sizeof(H2E_int_vec_p));
+    std::vector<int> skel(n_point, 1);
+    std::vector<std::vector<int>> lvl_leaf(max_level + 1);
+    for (int i = 0; i < n_leaf; i++) {
+        int leaf = h->height_nodes[i];
+        for (int lv = h->node_level[leaf] + 1; lv <= max_level; lv++) lvl_leaf[lv].push_back(leaf);
+    }
+    calc_ovlp_ff_idx(h);
+    /* thread seconds per phase (reported with H2G_SETUP_VERBOSE=1) */
+    double t_prep = 0.0, t_nai = 0.0, t_eri = 0.0, t_id = 0.0, t_gpu_wall = 0.0;
+    int n_gpu = 0;
+
+    for (int lv = max_level; lv >= min_adm; lv--) {
+        const int nlv = h->level_n_node[lv];
+        const int *lnodes = h->level_nodes + lv * n_leaf;
+        std::vector<UNode> W(nlv);
+        const double tp = wtime();
+        #pragma omp parallel for schedule(dynamic, 1)
+        for (int jn = 0; jn < nlv; jn++) u_prep(h, lnodes[jn], skel, W[jn]);
+        t_prep += wtime() - tp;
+        int done = 0;
+        if (EriSet *es = setup_eri(h)) {
+            /* groups of at most 2^27 doubles of unsketched integrals (2^25
+             * for the first, so that the host starts early) */
+            std::vector<int> gstart(1, 0);
+            long long tot = 0;
+            for (int jn = 0; jn < nlv; jn++) {
+                const long long n = (long long)W[jn].nrow_blk * (W[jn].cnt + W[jn].ff_ncol1);
+                if (jn > gstart.back() && tot + n > (gstart.size() == 1 ? (1LL << 25) : (1LL << 27))) {
+                    gstart.push_back(jn);
+                    tot = 0;
+                }
+                tot += n;
+            }
+            gstart.push_back(nlv);
+            const int n_groups = (int)gstart.size() - 1;
+            auto prep = [&](int g, std::vector<UReq> &reqs) {
+                for (int jn = gstart[g]; jn < gstart[g + 1]; jn++)
+                    if (W[jn].nrow_blk > 0) reqs.push_back(u_request(W[jn]));
+            };
+            auto use = [&](int g, std::vector<UReq> &) {
+                const double t0 = wtime();
+                #pragma omp parallel for schedule(dynamic, 1)
+                for (int jn = gstart[g]; jn < gstart[g + 1]; jn++) u_finish(h, W[jn]);
+                t_id += wtime() - t0;
+            };
+            auto discard = [&](int, std::vector<UReq> &) {};
+            const double tg = wtime();
+            const int used = gpu_pipeline<UReq>(
+                h, n_groups, [es](std::vector<UReq> &r) { return gpu_u_blocks(es, r); }, prep, use, discard);
+            t_gpu_wall += wtime() - tg;
+            done = gstart[used];
+            n_gpu += done;
+        }
+        #pragma omp parallel for schedule(dynamic, 1)
+        for (int jn = done; jn < nlv; jn++) {
+            u_integrals_host(h, W[jn], t_nai, t_eri);
+            const double t0 = wtime();
+            u_finish(h, W[jn]);
+            #pragma omp atomic
+            t_id += wtime() - t0;
+        }
+        /* skeleton flags for the next level up */
+        std::fill(skel.begin(), skel.end(), 0);
+        for (int jn = 0; jn < nlv; jn++) {
+            int node = lnodes[jn];
+            for (int k = 0; k < h->J_pair[node]->length; k++) skel[h->J_pair[node]->data[k]] = 1;
+        }
+        for (int leaf : lvl_leaf[lv])
+            for (int k = h->pt_cluster[2 * leaf]; k <= h->pt_cluster[2 * leaf + 1]; k++) skel[k] = 1;
+    }
+    if (setup_verbose())
+        std::fprintf(stderr, "build_U: %d nodes with GPU integrals (wall %.2f s incl. the decompositions between), "
+                     "host: preparation %.2f s wall, proxy-point potentials %.2f, far-field ERI %.2f thread s, ID "
+                     "%.2f s (wall on the GPU path, thread s on the host path)\n", n_gpu, t_gpu_wall, t_prep, t_nai,
+                     t_eri, t_id);
+    for (int i = 0; i < n_node; i++) {
+        if (h->U[i] == nullptr) {
+            h->U[i] = dmat_new(1, 1);
+            h->U[i]->nrow = 0;
+            h->U[i]->ncol = 0;
+            h->U[i]->ld = 0;
+        } else {
+            size_t nr = h->U[i]->nrow, nc = h->U[i]->ncol;
+            h->mat_size[U_SIZE_IDX] += nr * nc;
+            h->mat_size[MV_FWD_SIZE_IDX] += nr * nc + nr + nc;
+            h->mat_size[MV_BWD_SIZE_IDX] += nr * nc + nr + nc;
+        }
+        if (h->J_row[i] == nullptr) h->J_row[i] = ivec_new(1);
+        if (h->J_pair[i] == nullptr) h->J_pair[i] = ivec_new(1);
+    }
 }
 
 /* Coupling blocks (src/H2ERI_build_H2.c:910-1152). */
@@ -1061,7 +1175,8 @@ void build_B(H2ERI_p h)
             f.clear();
         };
         auto discard = [&](int g, std::vector<EriReq> &) { full[g & 1].clear(); };
-        const int used = gpu_pipeline(h, es, n_groups, prep, use, discard);
+        const int used = gpu_pipeline<EriReq>(
+            h, n_groups, [es](std::vector<EriReq> &r) { return gpu_eri_blocks(es, r); }, prep, use, discard);
         done = gstart[used];
     }
     #pragma omp parallel for schedule(dynamic, 1)
@@ -1171,7 +1286,8 @@ void build_D(H2ERI_p h)
             for (H2E_dense_mat_p &x : blks[g & 1]) dmat_free(&x);
             blks[g & 1].clear();
         };
-        const int used = gpu_pipeline(h, es, n_groups, prep, use, discard);
+        const int used = gpu_pipeline<EriReq>(
+            h, n_groups, [es](std::vector<EriReq> &r) { return gpu_eri_blocks(es, r); }, prep, use, discard);
         done = gstart[used];
     }
     const double th = wtime();
@@ -1314,6 +1430,64 @@ extern "C" int H2ERI_gpu_setup_eri_check(H2ERI_p h, int max_blocks, double *out)
     out[3] = (double)reqs.size();
     out[4] = t_gpu;
     out[5] = t_host;
+    return 0;
+}
+
+/* The sketched integral matrices of the nested-basis set-up (proxy-point
+ * potentials and far-field ERIs, each times its sparse sign sketch) of up to
+ * max_nodes nodes of a built structure, from the GPU and from the host
+ * engine, on the same inputs: nodes taken level by level from the leaves,
+ * every far-field shell pair counted as a skeleton. out: [0] largest
+ * |difference|, [1] largest |value|, [2] elements compared, [3] nodes
+ * compared, [4] seconds on the GPU (with the copy back), [5] seconds of the
+ * host engine (one thread). Returns 0, or an error code (no usable device:
+ * 9). */
+extern "C" int H2ERI_gpu_setup_u_check(H2ERI_p h, int max_nodes, double *out)
+{
+    using namespace h2g;
+    if (h == nullptr || out == nullptr || max_nodes < 1) return 3;
+    if (h->ovlp_ff_idx == nullptr || h->J_pair == nullptr) return 3;
+    if (!gpu_eri_usable()) return 9;
+    std::vector<const h2g_pair *> pairs(h->num_sp);
+    for (int i = 0; i < h->num_sp; i++) pairs[i] = sp_pair(h, i);
+    EriSet *es = nullptr;
+    int rc = gpu_eri_create(h->num_sp, pairs.data(), &es);
+    if (rc) return rc;
+    std::vector<int> skel(h->n_point, 1), nodes;
+    for (int lv = h->max_level; lv >= h->min_adm_level && (int)nodes.size() < max_nodes; lv--)
+        for (int j = 0; j < h->level_n_node[lv] && (int)nodes.size() < max_nodes; j++)
+            nodes.push_back(h->level_nodes[lv * h->n_leaf_node + j]);
+    std::vector<UNode> W(nodes.size());
+    std::vector<std::vector<double>> ref(nodes.size());
+    double t_nai = 0.0, t_eri = 0.0;
+    for (size_t k = 0; k < nodes.size(); k++) {
+        u_prep(h, nodes[k], skel, W[k]);
+        u_integrals_host(h, W[k], t_nai, t_eri);
+        ref[k] = W[k].A;
+        std::fill(W[k].A.begin(), W[k].A.end(), std::nan(""));
+    }
+    std::vector<UReq> reqs;
+    for (UNode &w : W)
+        if (w.nrow_blk > 0) reqs.push_back(u_request(w));
+    const double tg0 = wtime();
+    rc = gpu_u_blocks(es, reqs);
+    const double t_gpu = wtime() - tg0;
+    gpu_eri_free(es);
+    if (rc) return rc;
+    double dmax = 0.0, vmax = 0.0, n = 0.0;
+    for (size_t k = 0; k < W.size(); k++)
+        for (size_t e = 0; e < ref[k].size(); e++) {
+            const double d = std::fabs(W[k].A[e] - ref[k][e]);
+            dmax = std::isnan(d) ? INFINITY : std::max(dmax, d);
+            vmax = std::max(vmax, std::fabs(ref[k][e]));
+            n += 1.0;
+        }
+    out[0] = dmax;
+    out[1] = vmax;
+    out[2] = n;
+    out[3] = (double)reqs.size();
+    out[4] = t_gpu;
+    out[5] = t_nai + t_eri;
     return 0;
 }
 

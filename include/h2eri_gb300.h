@@ -201,6 +201,20 @@ int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n);
  * Returns 0, 9 without a usable device, or another error code. */
 int H2ERI_gpu_setup_eri_check(H2ERI_p h2eri, int max_blocks, double *out);
 
+/* Nested bases on the GPU (no counterpart in the reference): with a usable
+ * device, H2ERI_build_H2 also evaluates the integrals of the nested-basis
+ * construction on the GPU - the potentials of the proxy point charges
+ * around each node and the ERIs with the overlapping far-field shell pairs,
+ * each reduced by its sparse sign sketch on the device - and decomposes the
+ * sketched matrices on the host (H2P-ERI src/H2ERI_build_H2.c:351-827
+ * evaluates them on the host). This check evaluates the sketched matrices
+ * of up to max_nodes nodes with both engines on the same inputs: out[0]
+ * largest |difference|, out[1] largest |value|, out[2] elements compared,
+ * out[3] nodes compared, out[4] seconds on the GPU, out[5] seconds on the
+ * host engine (one thread); out needs 6 values. Returns 0, 9 without a
+ * usable device, or another error code. */
+int H2ERI_gpu_setup_u_check(H2ERI_p h2eri, int max_nodes, double *out);
+
 /* Figures of the device copy, for reports. out[0] kernel launches per matvec
  * call (one vector block), out[1] algorithmic matrix bytes read per matvec,
  * out[2] algorithmic vector bytes per vector, out[3] flops per vector,

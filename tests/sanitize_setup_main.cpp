@@ -17,6 +17,7 @@ namespace h2g {
 int gpu_eri_usable() { return 0; }
 int gpu_eri_create(int, const h2g_pair *const *, EriSet **out) { *out = nullptr; return 1; }
 int gpu_eri_blocks(EriSet *, std::vector<EriReq> &) { return 1; }
+int gpu_u_blocks(EriSet *, std::vector<UReq> &) { return 1; }
 void gpu_eri_free(EriSet *) {}
 }  // namespace h2g
 

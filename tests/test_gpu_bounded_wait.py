@@ -86,10 +86,10 @@ def test_persistent_dependency_wait_expiry_reported(library, alk26, oracle_lib):
     with the first range's item count raised by one, the range after it waits
     for an item that never completes; the wait gives up (~1 ms of SM clock),
     every CTA stops, the expiry is reported, and the next mixed J build on
-    the same structure is correct."""
+    the same structure is correct. (The persistent launch is a tuner
+    candidate, off by default; the self-test runs it whatever the choice.)"""
     alk26.set_precision(hg.MIXED)
     try:
-        assert alk26.report()["persist"] == 1
         assert library.H2ERI_gpu_selftest_persist_timeout(alk26.handle, 2_000_000) == 1
         D = hg.molecules.seeded_density(alk26.num_bf, 20, 4323)
         J = alk26.build_coulomb(D)

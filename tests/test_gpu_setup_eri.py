@@ -1,9 +1,11 @@
 """Set-up on the GPU: the dense near-field (D) and full coupling (B) blocks
 of electron-repulsion integrals evaluated by the GPU engine (h2g_eri.cu)
 equal the host engine's to 1e-13 of the largest value (same recurrences and
-tables; only the order of sums differs), and a representation built with the
-GPU blocks gives the oracle's J to 1e-12 on itself and the reference's
-golden J to the H2 tolerance, as the host-built one does."""
+tables; only the order of sums differs); so do the sketched matrices of the
+nested-basis construction (proxy-point potentials and far-field ERIs times
+their sparse sign sketches); and a representation built with the GPU
+integrals gives the oracle's J to 1e-12 on itself and the reference's golden
+J to the H2 tolerance, as the host-built one does."""
 import ctypes
 import os
 import time
@@ -38,6 +40,30 @@ def test_gpu_blocks_equal_host_engine_alk32(alk32, library):
     assert dmax <= 1e-13 * vmax, (dmax, vmax)
     print(f"C10H22 {int(nb)} blocks, {n / 1e6:.1f} M integrals: GPU {t_gpu:.3f} s, host engine (one thread) "
           f"{t_host:.3f} s")
+
+
+def u_check(library, h, max_nodes):
+    out = np.zeros(6)
+    rc = library.H2ERI_gpu_setup_u_check(h.handle, max_nodes, out.ctypes.data)
+    assert rc == 0, library.H2ERI_gpu_last_error()
+    return out
+
+
+@pytest.mark.parametrize("name", ["CH4", "C2H6", "C4H10"])
+def test_gpu_nested_basis_matrices_equal_host_engine_small(small_mols, library, name):
+    dmax, vmax, n, nn = u_check(library, small_mols[name], 1000)[:4]
+    assert nn >= 1 and n > 0
+    assert dmax <= 1e-13 * vmax, (dmax, vmax)
+
+
+def test_gpu_nested_basis_matrices_equal_host_engine_alk32(alk32, library):
+    """Leaf and upper-level nodes of C10H22: s, p and d pairs against
+    proxy points and far-field pairs of every class."""
+    dmax, vmax, n, nn, t_gpu, t_host = u_check(library, alk32, 1000)
+    assert nn >= 8 and n > 1e5
+    assert dmax <= 1e-13 * vmax, (dmax, vmax)
+    print(f"C10H22 nested bases: {int(nn)} nodes, {n / 1e6:.2f} M sketched entries: GPU {t_gpu:.3f} s, host engine "
+          f"(one thread) {t_host:.3f} s")
 
 
 def test_representation_built_with_gpu_blocks(oracle_lib, library, monkeypatch):
