@@ -23,8 +23,10 @@
  *   G_j[q][t][n] = sum_(p,q) below j  Ufull_j[(p,q)][t] D'[p][n]     q in S_j
  *   H_i[n][q][s] = sum_j B_ij G_j[q][.][n] + (from the parent)    n in S_i & C
  *   K[m][q]     += sum_(m,n) in leaf i  U_i[(m,n)] . H_i[n][q]
- * which are the reference's forward transform (y0), coupling (y1) and
- * backward transform for all (N, Q) columns at once, restricted exactly as
+ * (G_j stored as [n][q][t] and H_i as [n][q][s]: the range index n outermost,
+ * so a coupling product that reads G_j at the n of S_i reads whole contiguous
+ * [q][t] slabs) which are the reference's forward transform (y0), coupling
+ * (y1) and backward transform for all (N, Q) columns at once, restricted exactly as
  * the reference's row / column subtrees restrict them. The near-field blocks
  * are contracted directly. All contractions go through one gathered batched
  * FP64 GEMM kernel; K accumulates with FP64 atomics.
@@ -39,10 +41,12 @@
 #include <type_traits>
 #include <vector>
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "h2eri_gb300.h"
 #include "h2g_gpu_api.h"
+#include "h2g_umma.cuh"
 
 namespace h2g {
 
@@ -80,6 +84,7 @@ struct GemmTask {
     Opnd a, b, c;
     int M, N, K, Z;
     int c64;
+    int swap;   /* tensor-core kernel: tile rows are the product's columns (see k_gemm_tc) */
 };
 
 /* Tile shapes: FP64 64 x 64 (256 threads as 16 x 16, 4 x 4 per thread,
@@ -100,13 +105,15 @@ __host__ __device__ constexpr long long gemm_tiles(int M, int N, int Z)
 }
 
 /* One CTA per TM x TN output tile; tile_start[t] is the first tile of task t
- * (prefix sums, tile_start[n_task] = total). The operands are gathered
+ * (prefix sums, tile_start[n_task] = total) and tile_task[tile] the task of a
+ * tile. The operands are gathered
  * through index lists, so every k-step costs two dependent trips to L2
  * (index, then value): the indices are loaded two k-steps ahead and the
  * values one k-step ahead, both while the current step's FMAs run. */
 template <typename T>
 __global__ void __launch_bounds__(GemmCfg<T>::NT) k_gemm(const GemmTask *__restrict__ tasks,
-                                                          const long long *__restrict__ tile_start, int n_task)
+                                                          const long long *__restrict__ tile_start, int n_task,
+                                                          const int *__restrict__ tile_task)
 {
     constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN, NT = GemmCfg<T>::NT;
     constexpr int TY = NT / 16;                      /* thread rows */
@@ -116,11 +123,7 @@ __global__ void __launch_bounds__(GemmCfg<T>::NT) k_gemm(const GemmTask *__restr
     __shared__ T Bs[kGK][TN + 4];
     const long long tile = blockIdx.x;
     if (tile >= tile_start[n_task]) return;
-    int lo = 0, hi = n_task - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (tile_start[mid] <= tile) lo = mid; else hi = mid - 1;
-    }
+    const int lo = tile_task[tile];
     const GemmTask &Tk = tasks[lo];
     const long long loc = tile - tile_start[lo];
     const long long NZ = (long long)Tk.N * Tk.Z;
@@ -234,6 +237,273 @@ __global__ void __launch_bounds__(GemmCfg<T>::NT) k_gemm(const GemmTask *__restr
                 atomicAdd(reinterpret_cast<T *>(const_cast<void *>(Tk.c.p)) + ro + cco[b], acc[a][b]);
         }
     }
+}
+
+/* ======================================================================== */
+/* The FP32 products on the tensor cores                                     */
+/* ======================================================================== */
+
+/* The mixed-mode products of k_gemm<float> as tcgen05 MMAs. Each FP32
+ * operand element x is split exactly into three bf16 parts, x = h + m + l
+ * (h, m, l: 8 + 8 + 8 significant bits, cut by truncation, see
+ * tc_split2), and a tile accumulates the six products h h, and l h, m m, h l,
+ * m h, h m in FP32 in tensor memory, h h in one accumulator and the five
+ * smaller ones in a second (the tensor core's FP32 accumulation rounds
+ * each MMA's sum, so h h gets the shortest chain; the two are added in
+ * the epilogue); the three dropped products (m l, l m, l l) are below
+ * 2^-24 |a b|, the rounding of FP32 accumulation (the bf16x3
+ * scheme of G. Henry, P. T. P. Tang, A. Heinecke, "Leveraging the bfloat16
+ * artificial intelligence datatype for higher-precision computations",
+ * ARITH 2019).
+ *
+ * One CTA of 256 threads per 128 x 128 tile, two CTAs per SM. The tile's
+ * rows are the TMEM lanes: the rows of C, or - for an output whose columns
+ * are contiguous and rows are not (`swap`) - its columns, so that the
+ * epilogue's atomics from consecutive lanes go to consecutive addresses.
+ * Per 64-wide k step every thread gathers one row of each side (32 values
+ * of each, through the task's index lists), splits them and stores the
+ * slices into the 128-byte-swizzled K-major operand layout; one thread then
+ * issues 4 x 6 MMAs of 128 x 128 x 16 and commits them to an mbarrier,
+ * which the threads wait on (bounded, about a second) before they refill
+ * the slices. After the last step the eight warps read the accumulator
+ * (warp w: lanes 32 (w % 4) .., columns 64 (w / 4) ..) and add it to C with
+ * FP32 or FP64 atomics. */
+constexpr int kTcRows = 128;                          /* tile rows (TMEM lanes) = tile columns */
+constexpr int kTcK = 64;                              /* k per step: one 128-byte row of bf16 */
+constexpr int kTcThreads = 256;
+constexpr uint32_t kTcSlice = kTcRows * kTcK * 2;     /* one bf16 slice of one side: 16 KB */
+constexpr uint32_t kTcOffIdx = 6 * kTcSlice;          /* k offsets of both sides: 2 x 64 long long */
+constexpr uint32_t kTcOffBar = kTcOffIdx + 2 * kTcK * 8;
+constexpr uint32_t kTcSmem = kTcOffBar + 64;
+constexpr uint32_t kTcSmemLaunch = kTcSmem + 1024;    /* + slack to align to 1024 bytes */
+constexpr unsigned kTcErrBit = 8u;
+constexpr uint32_t kTcTmemCols = 2 * kTcRows;         /* h h accumulator, then the corrections' */
+
+__host__ __device__ constexpr long long tc_tiles(int M, int N, int Z)
+{
+    return (long long)((M + kTcRows - 1) / kTcRows) * (((long long)N * Z + kTcRows - 1) / kTcRows);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity)
+{
+    const long long t0 = clock64();
+    uint32_t ok = 0;
+    while (true) {
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > 2000000000LL) return false;
+    }
+}
+
+/* two FP32 values -> their h, m, l bf16 parts, packed low / high. The
+ * parts are cut by truncation: h = the top 16 bits of x (sign, exponent, 7
+ * fraction bits), m = the top 16 bits of x - h, l = x - h - m, which has at
+ * most 8 significant bits left and so is a bf16 value too: x = h + m + l
+ * exactly. */
+__device__ __forceinline__ void tc_split2(float x0, float x1, uint32_t &h, uint32_t &m, uint32_t &l)
+{
+    const uint32_t b0 = __float_as_uint(x0), b1 = __float_as_uint(x1);
+    h = __byte_perm(b0, b1, 0x7632);
+    const float r0 = x0 - __uint_as_float(b0 & 0xFFFF0000u), r1 = x1 - __uint_as_float(b1 & 0xFFFF0000u);
+    const uint32_t c0 = __float_as_uint(r0), c1 = __float_as_uint(r1);
+    m = __byte_perm(c0, c1, 0x7632);
+    const float t0 = r0 - __uint_as_float(c0 & 0xFFFF0000u), t1 = r1 - __uint_as_float(c1 & 0xFFFF0000u);
+    l = __byte_perm(__float_as_uint(t0), __float_as_uint(t1), 0x7632);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(const GemmTask *__restrict__ tasks,
+                                                           const long long *__restrict__ tile_start, int n_task,
+                                                           const int *__restrict__ tile_task, unsigned *err)
+{
+    extern __shared__ __align__(16) unsigned char tc_raw[];
+    unsigned char *sm = tc_raw + ((1024u - (umma::smem_u32(tc_raw) & 1023u)) & 1023u);
+    long long *kofs = reinterpret_cast<long long *>(sm + kTcOffIdx);   /* [side][k] */
+    const uint32_t sbase = umma::smem_u32(sm), bar = sbase + kTcOffBar;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kTcOffBar + 8);
+    volatile int *dead = reinterpret_cast<volatile int *>(sm + kTcOffBar + 12);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    const long long tile = blockIdx.x;
+    if (tile >= tile_start[n_task]) return;
+    const int lo = tile_task[tile];
+    const GemmTask &Tk = tasks[lo];
+    const long long loc = tile - tile_start[lo];
+    const bool swap = Tk.swap != 0;
+    const long long NZ = (long long)Tk.N * Tk.Z;
+    const long long Ne = swap ? (long long)Tk.M : NZ;
+    const long long tn = (Ne + kTcRows - 1) / kTcRows;
+    const long long m0 = (loc / tn) * kTcRows, n0 = (loc % tn) * kTcRows;
+    const int K = Tk.K;
+
+    /* offsets of a row of A, of a column of B and C (-1 past the extent) */
+    auto a_row = [&](long long i) -> long long {
+        return i < Tk.M ? (Tk.a.gr ? (long long)Tk.a.gr[i] : i) * Tk.a.sr : -1;
+    };
+    auto b_col = [&](long long jz) -> long long {
+        if (jz >= NZ) return -1;
+        const int z = (int)(jz / Tk.N), c = (int)(jz - (long long)z * Tk.N);
+        return (Tk.b.gz ? (long long)Tk.b.gz[z] : (long long)z) * Tk.b.sz +
+               (Tk.b.gc ? (long long)Tk.b.gc[c] : (long long)c) * Tk.b.sc;
+    };
+    auto c_row = [&](long long i) -> long long {
+        return i < Tk.M ? (Tk.c.gr ? (long long)Tk.c.gr[i] : i) * Tk.c.sr : -1;
+    };
+    auto c_col = [&](long long jz) -> long long {
+        if (jz >= NZ) return -1;
+        const int z = (int)(jz / Tk.N), c = (int)(jz - (long long)z * Tk.N);
+        return (Tk.c.gz ? (long long)Tk.c.gz[z] : (long long)z) * Tk.c.sz +
+               (Tk.c.gc ? (long long)Tk.c.gc[c] : (long long)c) * Tk.c.sc;
+    };
+    /* side 0 fills the A operand of the MMA (tile rows), side 1 the B operand */
+    const int r = tid & (kTcRows - 1), kh = tid >> 7;
+    const float *Ap = reinterpret_cast<const float *>(Tk.a.p), *Bp = reinterpret_cast<const float *>(Tk.b.p);
+    const float *sp[2] = {swap ? Bp : Ap, swap ? Ap : Bp};
+    const long long sf[2] = {swap ? b_col(m0 + r) : a_row(m0 + r), swap ? a_row(n0 + r) : b_col(n0 + r)};
+
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *dead = 0;
+    }
+    if (warp == 0) umma::tmem_alloc(tmem_slot, kTcTmemCols);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    const int nstep = (K + kTcK - 1) / kTcK;
+    int issued = 0;
+    for (int st = 0; st < nstep; st++) {
+        const int k0 = st * kTcK;
+        if (tid < 2 * kTcK) {
+            /* A's k is its column (gc, sc), B's k is its row (gr, sr) */
+            const int side = tid / kTcK, k = k0 + (tid % kTcK);
+            const bool from_a = (side == 0) != swap;
+            const int *kg = from_a ? Tk.a.gc : Tk.b.gr;
+            const long long ks = from_a ? Tk.a.sc : Tk.b.sr;
+            kofs[tid] = k < K ? (kg ? (long long)kg[k] : (long long)k) * ks : -1;
+        }
+        /* the slices of the previous step are free once its MMAs are done */
+        if (issued > 0 && !tc_wait(bar, (uint32_t)((issued - 1) & 1))) {
+            atomicOr(err, kTcErrBit);
+            *dead = 1;
+        }
+        __syncthreads();
+        if (*dead) break;
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+            const float *p = side ? sp[1] : sp[0];
+            const long long f = side ? sf[1] : sf[0];
+            const long long *ko = kofs + side * kTcK + kh * 32;
+            unsigned char *dst = sm + (uint32_t)side * 3u * kTcSlice;
+            if (f < 0 || k0 + kh * 32 >= K) {
+                /* a padding row, or k past the end: zero slices */
+#pragma unroll
+                for (int g = 0; g < 4; g++) {
+                    const uint32_t off = umma::kmajor_off(r, kh * 32 + g * 8, 0);
+                    const uint4 z = make_uint4(0, 0, 0, 0);
+                    *reinterpret_cast<uint4 *>(dst + off) = z;
+                    *reinterpret_cast<uint4 *>(dst + kTcSlice + off) = z;
+                    *reinterpret_cast<uint4 *>(dst + 2 * kTcSlice + off) = z;
+                }
+                continue;
+            }
+            /* the 32 loads of this side first, then the splits */
+            const float *pr = p + f;
+            float v[32];
+#pragma unroll
+            for (int e = 0; e < 32; e++) {
+                const long long o = ko[e];
+                v[e] = o >= 0 ? pr[o] : 0.f;
+            }
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                uint32_t hw[4], mw[4], lw[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) tc_split2(v[g * 8 + 2 * e], v[g * 8 + 2 * e + 1], hw[e], mw[e], lw[e]);
+                const uint32_t off = umma::kmajor_off(r, kh * 32 + g * 8, 0);
+                *reinterpret_cast<uint4 *>(dst + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(dst + kTcSlice + off) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+                *reinterpret_cast<uint4 *>(dst + 2 * kTcSlice + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+        }
+        umma::fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after_sync();
+            const uint32_t idesc = umma::idesc_bf16(kTcRows, kTcRows, 0, 0);
+            const uint32_t a0 = sbase, b0 = sbase + 3u * kTcSlice;
+            const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+            const int nkk = min(kTcK / 16, (K - k0 + 15) / 16);   /* 16-wide k steps that hold data */
+            for (int kk = 0; kk < nkk; kk++)
+#pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    const uint64_t ad = umma::sdesc(a0 + (uint32_t)pa[q] * kTcSlice + (uint32_t)kk * 32u, 16, 1024);
+                    const uint64_t bd = umma::sdesc(b0 + (uint32_t)pb[q] * kTcSlice + (uint32_t)kk * 32u, 16, 1024);
+                    /* q = 5 (h h) into columns [0, 128), the corrections into [128, 256) */
+                    umma::mma_bf16(q == 5 ? tmem : tmem + kTcRows, ad, bd, idesc, st > 0 || kk > 0 || (q > 0 && q < 5));
+                }
+            umma::mma_commit(bar);
+        }
+        issued++;
+    }
+    if (issued > 0 && !*dead && !tc_wait(bar, (uint32_t)((issued - 1) & 1))) {
+        atomicOr(err, kTcErrBit);
+        *dead = 1;
+    }
+    __syncthreads();
+    umma::fence_after_sync();
+    if (issued > 0 && !*dead) {
+        /* epilogue: lanes of the tile rows, 64 columns per warp */
+        const int q = warp & 3, hcol = warp >> 2;
+        const long long mi = m0 + 32 * q + lane;
+        const long long fc = swap ? c_col(mi) : c_row(mi);
+        double *C64 = reinterpret_cast<double *>(const_cast<void *>(Tk.c.p));
+        float *C32 = reinterpret_cast<float *>(const_cast<void *>(Tk.c.p));
+        /* this warp's columns: nj0 .. nj0 + 63, walked with (z, c) carried
+         * along (no divisions per element) */
+        const long long nj0 = n0 + hcol * 64;
+        const int nvalid = (int)max(0LL, min(64LL, Ne - nj0));
+        int z = 0, c = 0;
+        if (!swap && nvalid > 0) {
+            z = (int)(nj0 / Tk.N);
+            c = (int)(nj0 - (long long)z * Tk.N);
+        }
+#pragma unroll 1
+        for (int j0 = 0; j0 < 64; j0 += 16) {
+            uint32_t rr[16], rc[16];
+            umma::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(hcol * 64 + j0), rr);
+            umma::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(kTcRows + hcol * 64 + j0), rc);
+            umma::tmem_wait_ld();
+            if (fc < 0 || j0 >= nvalid) continue;
+            const int ne = min(16, nvalid - j0);
+#pragma unroll
+            for (int e = 0; e < 16; e++) {
+                if (e >= ne) break;
+                long long o2;
+                if (swap) {
+                    const long long i = nj0 + j0 + e;
+                    o2 = (Tk.c.gr ? (long long)Tk.c.gr[i] : i) * Tk.c.sr;
+                } else {
+                    o2 = (Tk.c.gz ? (long long)Tk.c.gz[z] : (long long)z) * Tk.c.sz +
+                         (Tk.c.gc ? (long long)Tk.c.gc[c] : (long long)c) * Tk.c.sc;
+                    if (++c == Tk.N) { c = 0; z++; }
+                }
+                const float v = __uint_as_float(rr[e]) + __uint_as_float(rc[e]);
+                if (Tk.c64) atomicAdd(C64 + fc + o2, (double)v);
+                else atomicAdd(C32 + fc + o2, v);
+            }
+        }
+    } else if (issued > 0) {
+        (void)tc_wait(bar, (uint32_t)((issued - 1) & 1));   /* MMAs still in flight: wait (bounded) before freeing */
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, kTcTmemCols);
 }
 
 /* ======================================================================== */
@@ -360,6 +630,8 @@ struct KChunk {
 struct KVariant {
     GemmTask *tasks = nullptr;
     long long *tile_start = nullptr;   /* per group: nt + 1 prefix sums, concatenated */
+    int *tile_task = nullptr;          /* per group: the task of each tile, concatenated */
+    std::vector<long long> group_tile_off;
     std::vector<long long> group_pre;  /* offset of each group's prefix array, launch order */
     std::vector<long long> group_tiles;
 };
@@ -371,7 +643,9 @@ struct KState {
     size_t arena_elems = 0;
     int *pool = nullptr;          /* every index list of the plan */
     std::vector<HTask> htasks;    /* host copy of the tasks (the FP32 variant is made from it) */
-    KVariant v64, v32;
+    KVariant v64, v32, vtc;        /* FP64, FP32 SIMT, FP32 on the tensor cores */
+    bool use_tc = true;           /* mixed mode: products on the tensor cores (H2G_K_TC=0: FP32 SIMT) */
+    unsigned *err_dev = nullptr;  /* the structure's kernel error word (device address) */
     NearTask *near = nullptr;
     long long *near_start = nullptr;
     int n_near = 0;
@@ -392,7 +666,7 @@ void free_exchange_state(DevRep *d)
     KState *k = (KState *)d->kstate;
     if (k == nullptr) return;
     cudaFree(k->arena); cudaFree(k->arena32); cudaFree(k->pool); cudaFree(k->dp32);
-    for (KVariant *v : {&k->v64, &k->v32}) { cudaFree(v->tasks); cudaFree(v->tile_start); }
+    for (KVariant *v : {&k->v64, &k->v32, &k->vtc}) { cudaFree(v->tasks); cudaFree(v->tile_start); cudaFree(v->tile_task); }
     cudaFree(k->near); cudaFree(k->near_start);
     cudaFree(k->sb); cudaFree(k->bf_shell); cudaFree(k->sig);
     cudaFree(k->dp); cudaFree(k->gh); cudaFree(k->kbuf);
@@ -450,9 +724,9 @@ static bool opnd_in_bounds(const HOpnd &o, int R, int C, int Z, size_t size, con
 /* Device task list and tile prefix sums of one precision: operands point
  * into the FP64 or the FP32 arena, density and work tensors; K stays FP64. */
 template <typename T>
-static int upload_variant(KState *ks)
+static int upload_variant(KState *ks, bool tc = false)
 {
-    KVariant &v = std::is_same<T, double>::value ? ks->v64 : ks->v32;
+    KVariant &v = std::is_same<T, double>::value ? ks->v64 : (tc ? ks->vtc : ks->v32);
     auto base = [&](int buf) -> const void * {
         switch (buf) {
         case KB_ARENA: return std::is_same<T, double>::value ? (const void *)ks->arena : (const void *)ks->arena32;
@@ -477,24 +751,35 @@ static int upload_variant(KState *ks)
         dt[t].a = conv(Tk.a); dt[t].b = conv(Tk.b); dt[t].c = conv(Tk.c);
         dt[t].M = Tk.M; dt[t].N = Tk.N; dt[t].K = Tk.K; dt[t].Z = Tk.Z;
         dt[t].c64 = Tk.c.buf == KB_K;
+        /* tensor-core tiles run along the output's contiguous dimension */
+        const bool rows_contig = Tk.c.gr < 0 && Tk.c.sr == 1, cols_contig = Tk.c.gc < 0 && Tk.c.sc == 1;
+        dt[t].swap = tc && !rows_contig && cols_contig;
     }
     std::vector<long long> pre;
+    std::vector<int> ttask;
     v.group_pre.clear();
     v.group_tiles.clear();
+    v.group_tile_off.clear();
     for (const KChunk &ch : ks->chunks)
         for (const KGroup &g : ch.groups) {
             v.group_pre.push_back((long long)pre.size());
+            v.group_tile_off.push_back((long long)ttask.size());
             long long acc = 0;
             pre.push_back(0);
             for (int t = g.t0; t < g.t0 + g.nt; t++) {
                 const HTask &Tk = ks->htasks[t];
-                acc += gemm_tiles<T>(Tk.M, Tk.N, Tk.Z);
+                const long long nt = tc ? tc_tiles(Tk.M, Tk.N, Tk.Z) : gemm_tiles<T>(Tk.M, Tk.N, Tk.Z);
+                acc += nt;
                 pre.push_back(acc);
+                if (acc <= 0x7fffffffLL) ttask.insert(ttask.end(), (size_t)nt, t - g.t0);
             }
             if (acc > 0x7fffffffLL) { set_error("exchange: launch too large"); return 4; }
             v.group_tiles.push_back(acc);
         }
     pre.push_back(0);
+    ttask.push_back(0);
+    KCUDA_TRY(cudaMalloc(&v.tile_task, ttask.size() * sizeof(int)));
+    KCUDA_TRY(cudaMemcpy(v.tile_task, ttask.data(), ttask.size() * sizeof(int), cudaMemcpyHostToDevice));
     KCUDA_TRY(cudaMalloc(&v.tasks, dt.size() * sizeof(GemmTask)));
     KCUDA_TRY(cudaMemcpy(v.tasks, dt.data(), dt.size() * sizeof(GemmTask), cudaMemcpyHostToDevice));
     KCUDA_TRY(cudaMalloc(&v.tile_start, pre.size() * sizeof(long long)));
@@ -511,7 +796,13 @@ static int ensure_f32(KState *ks)
     KCUDA_TRY(cudaGetLastError());
     KCUDA_TRY(cudaMalloc(&ks->dp32, (size_t)ks->nbf * ks->nbf * sizeof(float)));
     KCUDA_TRY(cudaDeviceSynchronize());
-    return upload_variant<float>(ks);
+    if (const char *e = std::getenv("H2G_K_TC")) ks->use_tc = std::atoi(e) != 0;
+    int rc = upload_variant<float>(ks);
+    if (rc == 0 && ks->use_tc) {
+        KCUDA_TRY(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemLaunch));
+        rc = upload_variant<float>(ks, true);
+    }
+    return rc;
 }
 
 /* free_bytes: device memory the G / H work tensors may be sized against;
@@ -728,8 +1019,8 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
                 t.a.buf = KB_ARENA; t.a.off = (long long)uoff[j]; t.a.sr = 1;
                 t.a.gc = P_row + g_start[g]; t.a.sc = rank[j];
                 t.b.buf = KB_DP; t.b.off = n0; t.b.gr = P_x + g_start[g]; t.b.sr = nbf; t.b.sc = 1;
-                t.c.buf = KB_GH; t.c.off = goff[j] + (long long)pos_in(S[j], g_y[g]) * rank[j] * nc;
-                t.c.sr = nc; t.c.sc = 1;
+                t.c.buf = KB_GH; t.c.off = goff[j] + (long long)pos_in(S[j], g_y[g]) * rank[j];
+                t.c.sr = 1; t.c.sc = (long long)S[j].size() * rank[j];
                 pb.add(t);
             }
         }
@@ -746,9 +1037,10 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
                     t.M = rank[p]; t.N = nc; t.K = rank[cc]; t.Z = (int)S[cc].size();
                     t.a.buf = KB_ARENA; t.a.off = (long long)uoff[p] + (long long)coff[cc] * rank[p];
                     t.a.sr = 1; t.a.sc = rank[p];
-                    t.b.buf = KB_GH; t.b.off = goff[cc]; t.b.sr = nc; t.b.sc = 1; t.b.sz = (long long)rank[cc] * nc;
-                    t.c.buf = KB_GH; t.c.off = goff[p]; t.c.sr = nc; t.c.sc = 1;
-                    t.c.gz = P_qmap[cc]; t.c.sz = (long long)rank[p] * nc;
+                    t.b.buf = KB_GH; t.b.off = goff[cc]; t.b.sr = 1; t.b.sc = (long long)S[cc].size() * rank[cc];
+                    t.b.sz = rank[cc];
+                    t.c.buf = KB_GH; t.c.off = goff[p]; t.c.sr = 1; t.c.sc = (long long)S[p].size() * rank[p];
+                    t.c.gz = P_qmap[cc]; t.c.sz = rank[p];
                     pb.add(t);
                 }
             }
@@ -770,8 +1062,8 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
                     HTask t{};
                     t.M = rank[i]; t.N = (int)sic[i].size(); t.K = rank[j]; t.Z = (int)S[j].size();
                     beff(b, tr, t.a);
-                    t.b.buf = KB_GH; t.b.off = goff[j]; t.b.sr = nc; t.b.gc = P_sicl[i]; t.b.sc = 1;
-                    t.b.sz = (long long)rank[j] * nc;
+                    t.b.buf = KB_GH; t.b.off = goff[j]; t.b.sr = 1; t.b.gc = P_sicl[i];
+                    t.b.sc = (long long)S[j].size() * rank[j]; t.b.sz = rank[j];
                     t.c.buf = KB_GH; t.c.off = hoff[i]; t.c.sr = 1; t.c.sc = (long long)nbf * rank[i];
                     t.c.gz = P_S[j]; t.c.sz = rank[i];
                     pb.add(t);
@@ -799,7 +1091,8 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
                         t.M = g_cnt[g]; t.N = (int)S[j].size(); t.K = rank[j]; t.Z = 1;
                         beff(b, tr, t.a);
                         t.a.gr = P_row + g_start[g];
-                        t.b.buf = KB_GH; t.b.off = goff[j] + (n - n0); t.b.sr = nc; t.b.sc = (long long)rank[j] * nc;
+                        t.b.buf = KB_GH; t.b.off = goff[j] + (long long)(n - n0) * S[j].size() * rank[j];
+                        t.b.sr = 1; t.b.sc = rank[j];
                         t.c.buf = KB_K; t.c.off = 0; t.c.gr = P_x + g_start[g]; t.c.sr = nbf;
                         t.c.gc = P_S[j]; t.c.sc = 1;
                         pb.add(t);
@@ -862,6 +1155,22 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
                 g.tiles += gemm_tiles<double>(T.M, T.N, T.Z);
             }
     ks->flops = flops;
+    if (const char *v = std::getenv("H2G_KPLAN_VERBOSE"); v && v[0] == '1') {
+        /* per phase of the first n range: tasks, tiles, flops, output elements, mean M / N*Z / K */
+        const KChunk &ch = ks->chunks.front();
+        for (const KGroup &g : ch.groups) {
+            double fl = 0.0, outs = 0.0, sm = 0.0, snz = 0.0, sk = 0.0;
+            for (int t = g.t0; t < g.t0 + g.nt; t++) {
+                const HTask &T = pb.tasks[t];
+                fl += 2.0 * T.M * (double)T.N * T.K * T.Z;
+                outs += (double)T.M * T.N * T.Z;
+                sm += T.M; snz += (double)T.N * T.Z; sk += T.K;
+            }
+            std::fprintf(stderr, "kplan %-10s tasks %7d tiles %8lld GFLOP %8.2f outputs(M) %8.2f mean M %6.1f NZ %8.1f K %6.1f\n",
+                         g.phase, g.nt, g.tiles, fl / 1e9, outs / 1e6, sm / g.nt, snz / g.nt, sk / g.nt);
+        }
+        std::fprintf(stderr, "kplan ranges %zu, near GFLOP %.2f\n", ks->chunks.size(), 0.0);
+    }
     ks->arena_elems = arena_elems;
     for (const KChunk &ch : ks->chunks) ks->gh_elems = std::max(ks->gh_elems, ch.gh_elems);
 
@@ -959,18 +1268,25 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
             et[t].M = T.M; et[t].N = T.N; et[t].K = T.K; et[t].Z = 1;
             epre.push_back(epre.back() + gemm_tiles<double>(T.M, T.N, 1));
         }
+        if (epre.back() > 0x7fffffffLL) { set_error("exchange: expansion launch too large"); return 4; }
+        std::vector<int> etask;
+        for (size_t t = 0; t < expand.size(); t++) etask.insert(etask.end(), (size_t)(epre[t + 1] - epre[t]), (int)t);
+        etask.push_back(0);
         GemmTask *dtask = nullptr;
         long long *dpre = nullptr;
+        int *dtt = nullptr;
         KCUDA_TRY(cudaMalloc(&dtask, et.size() * sizeof(GemmTask)));
         KCUDA_TRY(cudaMalloc(&dpre, epre.size() * sizeof(long long)));
+        KCUDA_TRY(cudaMalloc(&dtt, etask.size() * sizeof(int)));
         KCUDA_TRY(cudaMemcpy(dtask, et.data(), et.size() * sizeof(GemmTask), cudaMemcpyHostToDevice));
         KCUDA_TRY(cudaMemcpy(dpre, epre.data(), epre.size() * sizeof(long long), cudaMemcpyHostToDevice));
-        if (epre.back() > 0x7fffffffLL) { set_error("exchange: expansion launch too large"); return 4; }
-        k_gemm<double><<<(unsigned)epre.back(), kGThreads>>>(dtask, dpre, (int)et.size());
+        KCUDA_TRY(cudaMemcpy(dtt, etask.data(), etask.size() * sizeof(int), cudaMemcpyHostToDevice));
+        k_gemm<double><<<(unsigned)epre.back(), kGThreads>>>(dtask, dpre, (int)et.size(), dtt);
         KCUDA_TRY(cudaGetLastError());
         KCUDA_TRY(cudaDeviceSynchronize());
         cudaFree(dtask);
         cudaFree(dpre);
+        cudaFree(dtt);
         cudaFree(fact);
     }
     pb.pool.push_back(0);
@@ -1028,8 +1344,16 @@ static int enqueue_typed(KState *ks, const double *den, cudaStream_t s)
         KCUDA_TRY(cudaMemsetAsync(ks->gh, 0, ch.gh_elems * sizeof(T), s));
         for (const KGroup &g : ch.groups) {
             const long long tiles = v.group_tiles[gi];
-            if (tiles > 0)
-                k_gemm<T><<<(unsigned)tiles, GemmCfg<T>::NT, 0, s>>>(v.tasks + g.t0, v.tile_start + v.group_pre[gi], g.nt);
+            if (std::is_same<T, float>::value && ks->use_tc) {
+                const KVariant &w = ks->vtc;
+                if (w.group_tiles[gi] > 0)
+                    k_gemm_tc<<<(unsigned)w.group_tiles[gi], kTcThreads, kTcSmemLaunch, s>>>(
+                        w.tasks + g.t0, w.tile_start + w.group_pre[gi], g.nt, w.tile_task + w.group_tile_off[gi],
+                        ks->err_dev);
+            } else if (tiles > 0) {
+                k_gemm<T><<<(unsigned)tiles, GemmCfg<T>::NT, 0, s>>>(v.tasks + g.t0, v.tile_start + v.group_pre[gi], g.nt,
+                                                                      v.tile_task + v.group_tile_off[gi]);
+            }
             gi++;
         }
     }
@@ -1074,6 +1398,7 @@ static int get_kstate(H2ERI_p h, DevRep **d, KState **out)
         cudaGetDevice(&cur);
         if (cur != (*d)->device) cudaSetDevice((*d)->device);
         KState *k = new KState();
+        k->err_dev = (*d)->err_flag_dev;
         (*d)->kstate = k;
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
@@ -1127,6 +1452,12 @@ extern "C" int H2ERI_build_exchange_multi(H2ERI_p h2eri, int n_den, const double
         if (rc) return rc;
         KCUDA_TRY(cudaMemcpyAsync(K_mats + i * nn, ks->kbuf, bytes, cudaMemcpyDeviceToHost, d->s_main));
         KCUDA_TRY(cudaStreamSynchronize(d->s_main));
+        if (d->err_flag != nullptr && (*d->err_flag & kTcErrBit)) {
+            *d->err_flag &= ~kTcErrBit;
+            set_error("the exchange tensor-core kernel gave up waiting for its MMAs (bounded wait expired); "
+                      "results are invalid");
+            return 11;
+        }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ks->ev0, ks->ev1);
         total += ms;
@@ -1180,9 +1511,10 @@ extern "C" int H2ERI_gpu_exchange_report(H2ERI_p h2eri, double *out, int n)
     KState *ks;
     int rc = get_kstate(h2eri, &d, &ks);
     if (rc) return -rc;
-    double vals[6] = {ks->flops, (double)ks->last_ms, (double)ks->chunks.size(),
-                      (double)ks->gh_elems * sizeof(double), (double)ks->near_items, (double)launches_per_build(ks)};
-    int m = std::min(n, 6);
+    double vals[7] = {ks->flops, (double)ks->last_ms, (double)ks->chunks.size(),
+                      (double)ks->gh_elems * sizeof(double), (double)ks->near_items, (double)launches_per_build(ks),
+                      ks->v32.tasks == nullptr ? -1.0 : (double)ks->use_tc};
+    int m = std::min(n, 7);
     for (int i = 0; i < m; i++) out[i] = vals[i];
     return m;
 }

@@ -2139,6 +2139,9 @@ static int check_kernel_flag(DevRep *d)
     else if (f & 4u)
         set_error("the persistent tile kernel gave up waiting for a preceding range to complete (bounded wait "
                   "expired); results are invalid");
+    else if (f & 8u)
+        set_error("the exchange tensor-core kernel gave up waiting for its MMAs (bounded wait expired); results "
+                  "are invalid");
     else
         set_error("a tile kernel gave up waiting for a TMA load (bounded wait expired); results are invalid");
     return 11;

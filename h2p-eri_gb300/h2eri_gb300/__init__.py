@@ -249,7 +249,7 @@ class H2ERI:
         n = lib().H2ERI_gpu_exchange_report(self.handle, out.ctypes.data, 8)
         if n < 0:
             _check(-n, "gpu_exchange_report")
-        keys = ["flops", "ms_last", "n_ranges", "work_bytes", "near_items", "launches"]
+        keys = ["flops", "ms_last", "n_ranges", "work_bytes", "near_items", "launches", "tensor_cores"]
         return dict(zip(keys, out[:n].tolist()))
 
     def report(self):

@@ -136,8 +136,11 @@ int H2ERI_build_exchange_device(H2ERI_p h2eri, const double *d_den, double *d_K,
 /* Figures of the exchange plan: out[0] flops per K build, out[1] device time
  * of the last host-array K build (ms), out[2] number of n ranges the build is
  * split into, out[3] bytes of the G/H work tensors, out[4] near-field work
- * items, out[5] kernel launches per K build. Returns the number of values
- * written (<= n), or < 0. */
+ * items, out[5] kernel launches per K build, out[6] 1 when the mixed mode's
+ * products run on the tensor cores (bf16x3 splits, the default), 0 on the
+ * FP32 SIMT kernel (H2G_K_TC=0 when the first mixed K build runs), -1 before
+ * the first mixed K build. Returns the number of values written (<= n), or
+ * < 0. */
 int H2ERI_gpu_exchange_report(H2ERI_p h2eri, double *out, int n);
 /* Cap the device memory of the exchange work tensors (bytes; 0 = 40 % of
  * the free memory, at most 16 GB). K is then built in more ranges of the
