@@ -32,6 +32,7 @@
  * FP64 GEMM kernel; K accumulates with FP64 atomics.
  */
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -223,18 +224,24 @@ __global__ void __launch_bounds__(GemmCfg<T>::NT) k_gemm(const GemmTask *__restr
             cco[b] = -1;
         }
     }
+    /* output rows first (no index load waits behind the atomics) */
+    long long cro[RM];
 #pragma unroll
     for (int a = 0; a < RM; a++) {
-        int gi = m0 + ty + TY * a;
-        if (gi >= Tk.M) continue;
-        long long ro = (Tk.c.gr ? (long long)Tk.c.gr[gi] : (long long)gi) * Tk.c.sr;
+        const int gi = m0 + ty + TY * a;
+        cro[a] = gi < Tk.M ? (Tk.c.gr ? (long long)Tk.c.gr[gi] : (long long)gi) * Tk.c.sr : -1;
+    }
+    const bool c64 = Tk.c64 != 0;
+    double *C64 = reinterpret_cast<double *>(const_cast<void *>(Tk.c.p));
+    T *CT = reinterpret_cast<T *>(const_cast<void *>(Tk.c.p));
+#pragma unroll
+    for (int a = 0; a < RM; a++) {
+        if (cro[a] < 0) continue;
 #pragma unroll
         for (int b = 0; b < RN; b++) {
             if (cco[b] < 0) continue;
-            if (Tk.c64)
-                atomicAdd(reinterpret_cast<double *>(const_cast<void *>(Tk.c.p)) + ro + cco[b], (double)acc[a][b]);
-            else
-                atomicAdd(reinterpret_cast<T *>(const_cast<void *>(Tk.c.p)) + ro + cco[b], acc[a][b]);
+            if (c64) atomicAdd(C64 + cro[a] + cco[b], (double)acc[a][b]);
+            else atomicAdd(CT + cro[a] + cco[b], acc[a][b]);
         }
     }
 }
@@ -315,6 +322,71 @@ __device__ __forceinline__ void tc_split2(float x0, float x1, uint32_t &h, uint3
     l = __byte_perm(__float_as_uint(t0), __float_as_uint(t1), 0x7632);
 }
 
+/* Output of a tensor-core tile: the task's C operand held in registers. */
+struct TcOut {
+    void *p;
+    const int *gr, *gc, *gz;
+    long long sr, sc, sz, NZ;
+    int M, N, c64, swap;
+};
+
+__device__ __forceinline__ TcOut tc_out(const GemmTask &Tk)
+{
+    TcOut o;
+    o.p = const_cast<void *>(Tk.c.p);
+    o.gr = Tk.c.gr; o.gc = Tk.c.gc; o.gz = Tk.c.gz;
+    o.sr = Tk.c.sr; o.sc = Tk.c.sc; o.sz = Tk.c.sz;
+    o.NZ = (long long)Tk.N * Tk.Z;
+    o.M = Tk.M; o.N = Tk.N; o.c64 = Tk.c64; o.swap = Tk.swap;
+    return o;
+}
+
+/* One warp's share of a tile epilogue: tile row mi (this lane) against the
+ * 64 tile columns nj0 .. nj0 + 63 (those below Ne), accumulators at taddr
+ * (h h) and taddr + 128 (corrections). The output offsets of the 64 columns
+ * are formed first, two per lane, and handed around with shuffles, so that
+ * no index load waits behind the atomics. With release != 0 the warp's
+ * lane 0 arrives there once the accumulators are read. */
+__device__ __forceinline__ void tc_epilogue(const TcOut &o, long long mi, long long nj0, long long Ne, uint32_t taddr,
+                                            int lane, uint32_t release)
+{
+    auto col_off = [&](long long jz) -> long long {
+        const int z = (int)jz / o.N, c = (int)jz - z * o.N;
+        return (o.gz ? (long long)o.gz[z] : (long long)z) * o.sz + (o.gc ? (long long)o.gc[c] : (long long)c) * o.sc;
+    };
+    auto row_off = [&](long long i) -> long long { return (o.gr ? (long long)o.gr[i] : i) * o.sr; };
+    const long long fc = o.swap ? (mi < o.NZ ? col_off(mi) : -1) : (mi < o.M ? row_off(mi) : -1);
+    const long long j0a = nj0 + lane, j1a = nj0 + 32 + lane;
+    const long long oc0 = j0a < Ne ? (o.swap ? row_off(j0a) : col_off(j0a)) : 0;
+    const long long oc1 = j1a < Ne ? (o.swap ? row_off(j1a) : col_off(j1a)) : 0;
+    const int nvalid = (int)max(0LL, min(64LL, Ne - nj0));
+    double *C64 = reinterpret_cast<double *>(o.p);
+    float *C32 = reinterpret_cast<float *>(o.p);
+#pragma unroll 1
+    for (int j0 = 0; j0 < 64; j0 += 16) {
+        uint32_t rr[16], rc[16];
+        umma::tmem_ld16(taddr + (uint32_t)j0, rr);
+        umma::tmem_ld16(taddr + (uint32_t)(kTcRows + j0), rc);
+        umma::tmem_wait_ld();
+        if (release != 0 && j0 == 48) {
+            umma::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(release) : "memory");
+        }
+        if (j0 >= nvalid) continue;
+        const long long ocs = j0 < 32 ? oc0 : oc1;
+#pragma unroll
+        for (int e = 0; e < 16; e++) {
+            if (j0 + e >= nvalid) break;
+            const long long o2 = __shfl_sync(0xffffffffu, ocs, (j0 + e) & 31);
+            if (fc < 0) continue;
+            const float v = __uint_as_float(rr[e]) + __uint_as_float(rc[e]);
+            if (o.c64) atomicAdd(C64 + fc + o2, (double)v);
+            else atomicAdd(C32 + fc + o2, v);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(const GemmTask *__restrict__ tasks,
                                                            const long long *__restrict__ tile_start, int n_task,
                                                            const int *__restrict__ tile_task, unsigned *err)
@@ -348,15 +420,6 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(const GemmTask *__res
         const int z = (int)(jz / Tk.N), c = (int)(jz - (long long)z * Tk.N);
         return (Tk.b.gz ? (long long)Tk.b.gz[z] : (long long)z) * Tk.b.sz +
                (Tk.b.gc ? (long long)Tk.b.gc[c] : (long long)c) * Tk.b.sc;
-    };
-    auto c_row = [&](long long i) -> long long {
-        return i < Tk.M ? (Tk.c.gr ? (long long)Tk.c.gr[i] : i) * Tk.c.sr : -1;
-    };
-    auto c_col = [&](long long jz) -> long long {
-        if (jz >= NZ) return -1;
-        const int z = (int)(jz / Tk.N), c = (int)(jz - (long long)z * Tk.N);
-        return (Tk.c.gz ? (long long)Tk.c.gz[z] : (long long)z) * Tk.c.sz +
-               (Tk.c.gc ? (long long)Tk.c.gc[c] : (long long)c) * Tk.c.sc;
     };
     /* side 0 fills the A operand of the MMA (tile rows), side 1 the B operand */
     const int r = tid & (kTcRows - 1), kh = tid >> 7;
@@ -460,50 +523,256 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(const GemmTask *__res
     if (issued > 0 && !*dead) {
         /* epilogue: lanes of the tile rows, 64 columns per warp */
         const int q = warp & 3, hcol = warp >> 2;
-        const long long mi = m0 + 32 * q + lane;
-        const long long fc = swap ? c_col(mi) : c_row(mi);
-        double *C64 = reinterpret_cast<double *>(const_cast<void *>(Tk.c.p));
-        float *C32 = reinterpret_cast<float *>(const_cast<void *>(Tk.c.p));
-        /* this warp's columns: nj0 .. nj0 + 63, walked with (z, c) carried
-         * along (no divisions per element) */
-        const long long nj0 = n0 + hcol * 64;
-        const int nvalid = (int)max(0LL, min(64LL, Ne - nj0));
-        int z = 0, c = 0;
-        if (!swap && nvalid > 0) {
-            z = (int)(nj0 / Tk.N);
-            c = (int)(nj0 - (long long)z * Tk.N);
-        }
-#pragma unroll 1
-        for (int j0 = 0; j0 < 64; j0 += 16) {
-            uint32_t rr[16], rc[16];
-            umma::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(hcol * 64 + j0), rr);
-            umma::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(kTcRows + hcol * 64 + j0), rc);
-            umma::tmem_wait_ld();
-            if (fc < 0 || j0 >= nvalid) continue;
-            const int ne = min(16, nvalid - j0);
-#pragma unroll
-            for (int e = 0; e < 16; e++) {
-                if (e >= ne) break;
-                long long o2;
-                if (swap) {
-                    const long long i = nj0 + j0 + e;
-                    o2 = (Tk.c.gr ? (long long)Tk.c.gr[i] : i) * Tk.c.sr;
-                } else {
-                    o2 = (Tk.c.gz ? (long long)Tk.c.gz[z] : (long long)z) * Tk.c.sz +
-                         (Tk.c.gc ? (long long)Tk.c.gc[c] : (long long)c) * Tk.c.sc;
-                    if (++c == Tk.N) { c = 0; z++; }
-                }
-                const float v = __uint_as_float(rr[e]) + __uint_as_float(rc[e]);
-                if (Tk.c64) atomicAdd(C64 + fc + o2, (double)v);
-                else atomicAdd(C32 + fc + o2, v);
-            }
-        }
+        const TcOut o = tc_out(Tk);
+        tc_epilogue(o, m0 + 32 * q + lane, n0 + hcol * 64, Ne,
+                    tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(hcol * 64), lane, 0u);
     } else if (issued > 0) {
         (void)tc_wait(bar, (uint32_t)((issued - 1) & 1));   /* MMAs still in flight: wait (bounded) before freeing */
     }
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, kTcTmemCols);
+}
+
+/* Persistent, warp-specialised form of k_gemm_tc (the default): one CTA
+ * per SM walks the launch's tiles (tile = blockIdx.x + i * gridDim.x), and
+ * the three jobs of a tile run in different warps on different tiles at
+ * once: eight producer warps gather, split and store one 64-wide k step
+ * into a two-stage ring of slices (96 KB a stage), one thread issues its 24
+ * MMAs into one of two accumulator buffers (256 TMEM columns each: h h,
+ * then the corrections), and eight epilogue warps read the other buffer
+ * and add it to C. Hand-overs go through mbarriers: full (producer warps
+ * -> MMA), empty (MMA commit -> producers), acc_full (last commit of a tile
+ * -> epilogue), acc_empty (epilogue warps -> MMA). Every wait is bounded
+ * (about a second); on expiry the kernel sets the error bit, every role
+ * stops at its next wait, the MMA thread waits (bounded) for its last
+ * commit, and the tensor memory is freed. */
+constexpr int kPpWarps = 8, kPeWarps = 8;
+constexpr int kPThreads = 32 * (kPpWarps + 1 + kPeWarps);
+constexpr uint32_t kPStage = 6 * kTcSlice;
+constexpr uint32_t kPOffIdx = 2 * kPStage;                        /* k offsets: [stage][side][64] */
+constexpr uint32_t kPOffBar = kPOffIdx + 2 * 2 * kTcK * 8;
+constexpr uint32_t kPSmem = kPOffBar + 128;
+constexpr uint32_t kPSmemLaunch = kPSmem + 1024;
+constexpr uint32_t kPTmemCols = 512;                              /* two buffers of 256 */
+
+/* the tile's task and corner; false past the launch's tiles */
+struct TcTile {
+    int task;
+    bool swap;
+    long long m0, n0, NZ, Ne;
+};
+__device__ __forceinline__ void tc_tile(long long tile, const GemmTask *__restrict__ tasks,
+                                        const long long *__restrict__ tile_start, const int *__restrict__ tile_task,
+                                        TcTile &t)
+{
+    t.task = tile_task[tile];
+    const GemmTask &Tk = tasks[t.task];
+    const long long loc = tile - tile_start[t.task];
+    t.swap = Tk.swap != 0;
+    t.NZ = (long long)Tk.N * Tk.Z;
+    t.Ne = t.swap ? (long long)Tk.M : t.NZ;
+    const long long tn = (t.Ne + kTcRows - 1) / kTcRows;
+    t.m0 = (loc / tn) * kTcRows;
+    t.n0 = (loc % tn) * kTcRows;
+}
+
+__global__ void __launch_bounds__(kPThreads, 1) k_gemm_tcp(const GemmTask *__restrict__ tasks,
+                                                           const long long *__restrict__ tile_start, int n_task,
+                                                           const int *__restrict__ tile_task, unsigned *err)
+{
+    extern __shared__ __align__(16) unsigned char tcp_raw[];
+    unsigned char *sm = tcp_raw + ((1024u - (umma::smem_u32(tcp_raw) & 1023u)) & 1023u);
+    long long *kofs = reinterpret_cast<long long *>(sm + kPOffIdx);   /* [stage][side][k] */
+    const uint32_t sbase = umma::smem_u32(sm), bar0 = sbase + kPOffBar;
+    auto full = [&](int st) { return bar0 + 8u * st; };
+    auto empty = [&](int st) { return bar0 + 16u + 8u * st; };
+    auto acc_full = [&](int b) { return bar0 + 32u + 8u * b; };
+    auto acc_empty = [&](int b) { return bar0 + 48u + 8u * b; };
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kPOffBar + 64);
+    volatile int *dead = reinterpret_cast<volatile int *>(sm + kPOffBar + 68);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long ntiles = tile_start[n_task];
+
+    if (tid == 0) {
+        for (int i = 0; i < 2; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(full(i)), "r"(kPpWarps) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty(i)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(acc_full(i)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(acc_empty(i)), "r"(kPeWarps) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *dead = 0;
+    }
+    if (warp == kPpWarps) umma::tmem_alloc(tmem_slot, kPTmemCols);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    auto wait = [&](uint32_t bar, uint32_t parity) -> bool {
+        if (*dead) return false;
+        if (tc_wait(bar, parity)) return true;
+        atomicOr(err, kTcErrBit);
+        *dead = 1;
+        return false;
+    };
+
+    if (warp < kPpWarps) {
+        /* ---- producers: 256 threads, row r of both sides, k half kh ---- */
+        const int r = tid & (kTcRows - 1), kh = tid >> 7;
+        long long c = 0;   /* k steps filled so far */
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            TcTile ti;
+            tc_tile(tile, tasks, tile_start, tile_task, ti);
+            const GemmTask &Tk = tasks[ti.task];
+            const int K = Tk.K;
+            const float *Ap = reinterpret_cast<const float *>(Tk.a.p), *Bp = reinterpret_cast<const float *>(Tk.b.p);
+            auto a_row = [&](long long i) -> long long {
+                return i < Tk.M ? (Tk.a.gr ? (long long)Tk.a.gr[i] : i) * Tk.a.sr : -1;
+            };
+            auto b_col = [&](long long jz) -> long long {
+                if (jz >= ti.NZ) return -1;
+                const int z = (int)(jz / Tk.N), cc = (int)(jz - (long long)z * Tk.N);
+                return (Tk.b.gz ? (long long)Tk.b.gz[z] : (long long)z) * Tk.b.sz +
+                       (Tk.b.gc ? (long long)Tk.b.gc[cc] : (long long)cc) * Tk.b.sc;
+            };
+            const float *sp0 = ti.swap ? Bp : Ap, *sp1 = ti.swap ? Ap : Bp;
+            const long long sf0 = ti.swap ? b_col(ti.m0 + r) : a_row(ti.m0 + r);
+            const long long sf1 = ti.swap ? a_row(ti.n0 + r) : b_col(ti.n0 + r);
+            const int nstep = (K + kTcK - 1) / kTcK;
+            bool stop = false;
+            for (int st = 0; st < nstep; st++, c++) {
+                const int s = (int)(c & 1);
+                const uint32_t ph = (uint32_t)((c >> 1) & 1);
+                (void)wait(empty(s), ph ^ 1u);
+                const int k0 = st * kTcK;
+                if (tid < 2 * kTcK) {
+                    const int side = tid / kTcK, k = k0 + (tid % kTcK);
+                    const bool from_a = (side == 0) != ti.swap;
+                    const int *kg = from_a ? Tk.a.gc : Tk.b.gr;
+                    const long long ks = from_a ? Tk.a.sc : Tk.b.sr;
+                    kofs[(s * 2 + side) * kTcK + (tid % kTcK)] = k < K ? (kg ? (long long)kg[k] : (long long)k) * ks : -1;
+                }
+                asm volatile("bar.sync 1, %0;" ::"r"(32 * kPpWarps) : "memory");
+                if (*dead) { stop = true; break; }
+                unsigned char *stage = sm + (uint32_t)s * kPStage;
+#pragma unroll
+                for (int side = 0; side < 2; side++) {
+                    const float *p = side ? sp1 : sp0;
+                    const long long f = side ? sf1 : sf0;
+                    const long long *ko = kofs + (s * 2 + side) * kTcK + kh * 32;
+                    unsigned char *dst = stage + (uint32_t)side * 3u * kTcSlice;
+                    if (f < 0 || k0 + kh * 32 >= K) {
+#pragma unroll
+                        for (int g = 0; g < 4; g++) {
+                            const uint32_t off = umma::kmajor_off(r, kh * 32 + g * 8, 0);
+                            const uint4 z = make_uint4(0, 0, 0, 0);
+                            *reinterpret_cast<uint4 *>(dst + off) = z;
+                            *reinterpret_cast<uint4 *>(dst + kTcSlice + off) = z;
+                            *reinterpret_cast<uint4 *>(dst + 2 * kTcSlice + off) = z;
+                        }
+                        continue;
+                    }
+                    const float *pr = p + f;
+                    float v[32];
+#pragma unroll
+                    for (int e = 0; e < 32; e++) {
+                        const long long o = ko[e];
+                        v[e] = o >= 0 ? pr[o] : 0.f;
+                    }
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        uint32_t hw[4], mw[4], lw[4];
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            tc_split2(v[g * 8 + 2 * e], v[g * 8 + 2 * e + 1], hw[e], mw[e], lw[e]);
+                        const uint32_t off = umma::kmajor_off(r, kh * 32 + g * 8, 0);
+                        *reinterpret_cast<uint4 *>(dst + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                        *reinterpret_cast<uint4 *>(dst + kTcSlice + off) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+                        *reinterpret_cast<uint4 *>(dst + 2 * kTcSlice + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                    }
+                }
+                umma::fence_async_smem();
+                __syncwarp();
+                if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(full(s)) : "memory");
+            }
+            if (stop) break;
+        }
+    } else if (warp == kPpWarps) {
+        /* ---- MMA issue: one thread ---- */
+        long long c = 0;
+        int i = 0;
+        uint32_t last_bar = 0, last_par = 0;
+        bool any = false;
+        const uint32_t idesc = umma::idesc_bf16(kTcRows, kTcRows, 0, 0);
+        const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, i++) {
+            TcTile ti;
+            tc_tile(tile, tasks, tile_start, tile_task, ti);
+            const int K = tasks[ti.task].K;
+            const int b = i & 1;
+            const uint32_t acc = tmem + (uint32_t)(b * 2 * kTcRows);
+            bool ok = true;
+            if (lane == 0) ok = wait(acc_empty(b), (uint32_t)(((i >> 1) & 1) ^ 1));
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            const int nstep = (K + kTcK - 1) / kTcK;
+            for (int st = 0; st < nstep; st++, c++) {
+                const int s = (int)(c & 1);
+                if (lane == 0) ok = wait(full(s), (uint32_t)((c >> 1) & 1));
+                ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+                if (!ok) break;
+                if (lane == 0) {
+                    umma::fence_after_sync();
+                    const uint32_t a0 = sbase + (uint32_t)s * kPStage, b0 = a0 + 3u * kTcSlice;
+                    const int nkk = min(kTcK / 16, (K - st * kTcK + 15) / 16);
+                    for (int kk = 0; kk < nkk; kk++)
+#pragma unroll
+                        for (int q = 0; q < 6; q++) {
+                            const uint64_t ad = umma::sdesc(a0 + (uint32_t)pa[q] * kTcSlice + (uint32_t)kk * 32u, 16, 1024);
+                            const uint64_t bd = umma::sdesc(b0 + (uint32_t)pb[q] * kTcSlice + (uint32_t)kk * 32u, 16, 1024);
+                            umma::mma_bf16(q == 5 ? acc : acc + kTcRows, ad, bd, idesc,
+                                           st > 0 || kk > 0 || (q > 0 && q < 5));
+                        }
+                    umma::mma_commit(empty(s));
+                    last_bar = empty(s);
+                    last_par = (uint32_t)((c >> 1) & 1);
+                    any = true;
+                }
+                __syncwarp();
+            }
+            if (!ok) break;
+            if (lane == 0) {
+                umma::mma_commit(acc_full(b));
+                last_bar = acc_full(b);
+                last_par = (uint32_t)((i >> 1) & 1);
+            }
+            __syncwarp();
+        }
+        /* after an expiry, MMAs may still be in flight: wait (bounded) for the last commit */
+        if (lane == 0 && *dead && any) (void)tc_wait(last_bar, last_par);
+    } else {
+        /* ---- epilogue: 8 warps, lane quarter warp % 4, column half ---- */
+        const int e = warp - kPpWarps - 1, q = warp & 3, hcol = e >> 2;
+        int i = 0;
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, i++) {
+            const int b = i & 1;
+            bool ok = true;
+            if (lane == 0) ok = wait(acc_full(b), (uint32_t)((i >> 1) & 1));
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            umma::fence_after_sync();
+            TcTile ti;
+            tc_tile(tile, tasks, tile_start, tile_task, ti);
+            const TcOut o = tc_out(tasks[ti.task]);
+            tc_epilogue(o, ti.m0 + 32 * q + lane, ti.n0 + hcol * 64, ti.Ne,
+                        tmem + (uint32_t)(b * 2 * kTcRows) + ((uint32_t)(32 * q) << 16) + (uint32_t)(hcol * 64), lane,
+                        acc_empty(b));
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == kPpWarps) umma::tmem_dealloc(tmem, kPTmemCols);
 }
 
 /* ======================================================================== */
@@ -644,7 +913,8 @@ struct KState {
     int *pool = nullptr;          /* every index list of the plan */
     std::vector<HTask> htasks;    /* host copy of the tasks (the FP32 variant is made from it) */
     KVariant v64, v32, vtc;        /* FP64, FP32 SIMT, FP32 on the tensor cores */
-    bool use_tc = true;           /* mixed mode: products on the tensor cores (H2G_K_TC=0: FP32 SIMT) */
+    int use_tc = 1;               /* mixed mode: 1 persistent tensor-core kernel, 2 one tile per CTA, 0 FP32 SIMT (H2G_K_TC) */
+    int n_sm = 1;
     unsigned *err_dev = nullptr;  /* the structure's kernel error word (device address) */
     NearTask *near = nullptr;
     long long *near_start = nullptr;
@@ -796,10 +1066,14 @@ static int ensure_f32(KState *ks)
     KCUDA_TRY(cudaGetLastError());
     KCUDA_TRY(cudaMalloc(&ks->dp32, (size_t)ks->nbf * ks->nbf * sizeof(float)));
     KCUDA_TRY(cudaDeviceSynchronize());
-    if (const char *e = std::getenv("H2G_K_TC")) ks->use_tc = std::atoi(e) != 0;
+    if (const char *e = std::getenv("H2G_K_TC")) ks->use_tc = std::min(2, std::max(0, std::atoi(e)));
+    int dev = 0;
+    KCUDA_TRY(cudaGetDevice(&dev));
+    KCUDA_TRY(cudaDeviceGetAttribute(&ks->n_sm, cudaDevAttrMultiProcessorCount, dev));
     int rc = upload_variant<float>(ks);
     if (rc == 0 && ks->use_tc) {
         KCUDA_TRY(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemLaunch));
+        KCUDA_TRY(cudaFuncSetAttribute(k_gemm_tcp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmemLaunch));
         rc = upload_variant<float>(ks, true);
     }
     return rc;
@@ -809,6 +1083,9 @@ static int ensure_f32(KState *ks)
  * upload = false builds and checks the plan on the host only. */
 static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
 {
+    const auto tp0 = std::chrono::steady_clock::now();
+    auto secs = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - tp0).count(); };
+    const bool verbose = [] { const char *v = std::getenv("H2G_KPLAN_VERBOSE"); return v && v[0] == '1'; }();
     const int nbf = h->num_bf, nsh = h->nshell, n_node = h->n_node, num_sp = h->num_sp;
     const int krnl = h->krnl_mat_size, nl = h->n_leaf_node, maxc = h->max_child;
     const int *sb = h->shell_bf_sidx;
@@ -1218,6 +1495,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
                     return 5;
                 }
     }
+    const double t_plan = secs();
     if (!upload) return 0;
 
     /* ---- upload ---- */
@@ -1240,6 +1518,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
     };
     for (int b = 0; b < h->n_B; b++) if (put_dense(h->c_B_blks[b], boff[b])) return 10;
     for (int b = 0; b < h->n_D; b++) if (put_dense(h->c_D_blks[b], doff[b])) return 10;
+    const double t_arena = secs();
     if (!expand.empty()) {
         double *fact = nullptr;
         KCUDA_TRY(cudaMalloc(&fact, fact_elems * sizeof(double)));
@@ -1317,6 +1596,10 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
     ks->ext.gc = ks->pool + P_gc;
     KCUDA_TRY(cudaEventCreate(&ks->ev0));
     KCUDA_TRY(cudaEventCreate(&ks->ev1));
+    if (verbose)
+        std::fprintf(stderr, "kplan: index sets and tasks %.2f s, arena upload %.2f s, low-rank expansion and "
+                     "task upload %.2f s (%zu tasks, %zu index entries, %.2f GB arena)\n", t_plan, t_arena - t_plan,
+                     secs() - t_arena, ks->htasks.size(), pb.pool.size(), arena_elems * 8e-9);
     return 0;
 }
 
@@ -1346,8 +1629,13 @@ static int enqueue_typed(KState *ks, const double *den, cudaStream_t s)
             const long long tiles = v.group_tiles[gi];
             if (std::is_same<T, float>::value && ks->use_tc) {
                 const KVariant &w = ks->vtc;
-                if (w.group_tiles[gi] > 0)
-                    k_gemm_tc<<<(unsigned)w.group_tiles[gi], kTcThreads, kTcSmemLaunch, s>>>(
+                const long long nt = w.group_tiles[gi];
+                if (nt > 0 && ks->use_tc == 1)
+                    k_gemm_tcp<<<(unsigned)std::min<long long>(nt, ks->n_sm), kPThreads, kPSmemLaunch, s>>>(
+                        w.tasks + g.t0, w.tile_start + w.group_pre[gi], g.nt, w.tile_task + w.group_tile_off[gi],
+                        ks->err_dev);
+                else if (nt > 0)
+                    k_gemm_tc<<<(unsigned)nt, kTcThreads, kTcSmemLaunch, s>>>(
                         w.tasks + g.t0, w.tile_start + w.group_pre[gi], g.nt, w.tile_task + w.group_tile_off[gi],
                         ks->err_dev);
             } else if (tiles > 0) {
@@ -1513,7 +1801,7 @@ extern "C" int H2ERI_gpu_exchange_report(H2ERI_p h2eri, double *out, int n)
     if (rc) return -rc;
     double vals[7] = {ks->flops, (double)ks->last_ms, (double)ks->chunks.size(),
                       (double)ks->gh_elems * sizeof(double), (double)ks->near_items, (double)launches_per_build(ks),
-                      ks->v32.tasks == nullptr ? -1.0 : (double)ks->use_tc};
+                      ks->v32.tasks == nullptr ? -1.0 : (double)(ks->use_tc != 0)};
     int m = std::min(n, 7);
     for (int i = 0; i < m; i++) out[i] = vals[i];
     return m;

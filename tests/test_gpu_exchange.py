@@ -111,30 +111,35 @@ def test_exchange_mixed_precision(alk26, oracle_lib):
 
 def test_exchange_mixed_tensor_cores_and_simt(oracle_lib, library, monkeypatch):
     """The mixed mode's products on the tensor cores (FP32 operands split
-    into three bf16 parts, six products accumulated in FP32 in tensor memory)
-    and on the FP32 SIMT kernel (H2G_K_TC=0) both stay within the exchange
+    into three bf16 parts, six products accumulated in FP32 in tensor memory;
+    the persistent warp-specialised kernel and the one-tile-per-CTA kernel,
+    H2G_K_TC=2) and on the FP32 SIMT kernel (H2G_K_TC=0) all stay within the exchange
     tolerance of the FP64 oracle, also with the n range split into several
     ranges, and agree with each other to FP32-accumulation level."""
     mol = os.path.join(GOLDEN, "alk26_ccpvdz.mol")
     Ks, hs = {}, {}
     try:
-        for flag in ("1", "0"):
+        for flag in ("1", "2", "0"):
             monkeypatch.setenv("H2G_K_TC", flag)
             h = hs[flag] = hg.H2ERI.from_mol(mol, qr_tol=1e-6)
             n = h.num_bf
             D = hg.molecules.seeded_density(n, 33, 2101)
             h.set_precision(hg.MIXED)
             Ks[flag] = h.build_exchange(D)
-            assert h.exchange_report()["tensor_cores"] == float(flag)
+            assert h.exchange_report()["tensor_cores"] == float(flag != "0")
             assert library.H2ERI_gpu_set_exchange_memory(h.handle, 2e7) == 0
             K_split = h.build_exchange(D)
             assert h.exchange_report()["n_ranges"] > 1
             assert relerr(K_split, Ks[flag]) < 1e-8
         K64 = oracle_K(oracle_lib, hs["1"], D)
-        e_tc, e_simt = relerr(Ks["1"], K64), relerr(Ks["0"], K64)
-        print(f"mixed K relerr vs FP64 oracle: tensor cores {e_tc:.3e}, FP32 SIMT {e_simt:.3e}")
-        assert e_tc < TOL_MIXED_K and e_simt < TOL_MIXED_K
+        e_tc, e_tile, e_simt = relerr(Ks["1"], K64), relerr(Ks["2"], K64), relerr(Ks["0"], K64)
+        print(f"mixed K relerr vs FP64 oracle: tensor cores {e_tc:.3e} (one tile per CTA {e_tile:.3e}), "
+              f"FP32 SIMT {e_simt:.3e}")
+        assert e_tc < TOL_MIXED_K and e_tile < TOL_MIXED_K and e_simt < TOL_MIXED_K
         assert relerr(Ks["1"], Ks["0"]) < TOL_MIXED_K
+        # the two tensor-core kernels form the same tile products (their FP32
+        # atomics into the work tensors land in a different order)
+        assert relerr(Ks["1"], Ks["2"]) < TOL_MIXED_K
     finally:
         for h in hs.values():
             h.destroy()
