@@ -537,8 +537,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(const GemmTask *__res
 /* Persistent, warp-specialised form of k_gemm_tc (the default): one CTA
  * per SM walks the launch's tiles (tile = blockIdx.x + i * gridDim.x), and
  * the three jobs of a tile run in different warps on different tiles at
- * once: eight producer warps gather, split and store one 64-wide k step
- * into a two-stage ring of slices (96 KB a stage), one thread issues its 24
+ * once: two groups of four producer warps gather, split and store the
+ * 64-wide k steps of alternate tiles into their own slot of slices (96 KB a
+ * slot; two tiles' loads in flight), one thread issues its 24
  * MMAs into one of two accumulator buffers (256 TMEM columns each: h h,
  * then the corrections), and eight epilogue warps read the other buffer
  * and add it to C. Hand-overs go through mbarriers: full (producer warps
@@ -596,7 +597,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_gemm_tcp(const GemmTask *__res
 
     if (tid == 0) {
         for (int i = 0; i < 2; i++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(full(i)), "r"(kPpWarps) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(full(i)), "r"(kPpWarps / 2) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty(i)) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(acc_full(i)) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(acc_empty(i)), "r"(kPeWarps) : "memory");
@@ -618,10 +619,14 @@ __global__ void __launch_bounds__(kPThreads, 1) k_gemm_tcp(const GemmTask *__res
     };
 
     if (warp < kPpWarps) {
-        /* ---- producers: 256 threads, row r of both sides, k half kh ---- */
-        const int r = tid & (kTcRows - 1), kh = tid >> 7;
-        long long c = 0;   /* k steps filled so far */
-        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        /* ---- producers: two groups of four warps; group g fills slot g
+         * with the k steps of the CTA's tiles of parity g, so that two
+         * tiles' loads are in flight at once. Thread: row r of both sides. ---- */
+        const int grp = warp >> 2, r = tid & (kTcRows - 1), s = grp;
+        long long uses = 0;   /* fills of slot s so far */
+        int j = 0;
+        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, j++) {
+            if ((j & 1) != grp) continue;
             TcTile ti;
             tc_tile(tile, tasks, tile_start, tile_task, ti);
             const GemmTask &Tk = tasks[ti.task];
@@ -632,7 +637,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_gemm_tcp(const GemmTask *__res
             };
             auto b_col = [&](long long jz) -> long long {
                 if (jz >= ti.NZ) return -1;
-                const int z = (int)(jz / Tk.N), cc = (int)(jz - (long long)z * Tk.N);
+                const int z = (int)jz / Tk.N, cc = (int)jz - z * Tk.N;
                 return (Tk.b.gz ? (long long)Tk.b.gz[z] : (long long)z) * Tk.b.sz +
                        (Tk.b.gc ? (long long)Tk.b.gc[cc] : (long long)cc) * Tk.b.sc;
             };
@@ -641,23 +646,22 @@ __global__ void __launch_bounds__(kPThreads, 1) k_gemm_tcp(const GemmTask *__res
             const long long sf1 = ti.swap ? a_row(ti.n0 + r) : b_col(ti.n0 + r);
             const int nstep = (K + kTcK - 1) / kTcK;
             bool stop = false;
-            for (int st = 0; st < nstep; st++, c++) {
-                const int s = (int)(c & 1);
-                const uint32_t ph = (uint32_t)((c >> 1) & 1);
-                (void)wait(empty(s), ph ^ 1u);
+            for (int st = 0; st < nstep; st++, uses++) {
+                (void)wait(empty(s), (uint32_t)((uses & 1) ^ 1));
                 const int k0 = st * kTcK;
-                if (tid < 2 * kTcK) {
-                    const int side = tid / kTcK, k = k0 + (tid % kTcK);
+                {
+                    const int side = r >> 6, kk = r & (kTcK - 1), k = k0 + kk;
                     const bool from_a = (side == 0) != ti.swap;
                     const int *kg = from_a ? Tk.a.gc : Tk.b.gr;
                     const long long ks = from_a ? Tk.a.sc : Tk.b.sr;
-                    kofs[(s * 2 + side) * kTcK + (tid % kTcK)] = k < K ? (kg ? (long long)kg[k] : (long long)k) * ks : -1;
+                    kofs[(s * 2 + side) * kTcK + kk] = k < K ? (kg ? (long long)kg[k] : (long long)k) * ks : -1;
                 }
-                asm volatile("bar.sync 1, %0;" ::"r"(32 * kPpWarps) : "memory");
+                asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(32 * kPpWarps / 2) : "memory");
                 if (*dead) { stop = true; break; }
                 unsigned char *stage = sm + (uint32_t)s * kPStage;
 #pragma unroll
-                for (int side = 0; side < 2; side++) {
+                for (int part = 0; part < 4; part++) {
+                    const int side = part >> 1, kh = part & 1;
                     const float *p = side ? sp1 : sp0;
                     const long long f = side ? sf1 : sf0;
                     const long long *ko = kofs + (s * 2 + side) * kTcK + kh * 32;
@@ -700,7 +704,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_gemm_tcp(const GemmTask *__res
         }
     } else if (warp == kPpWarps) {
         /* ---- MMA issue: one thread ---- */
-        long long c = 0;
+        long long used0 = 0, used1 = 0;   /* k steps consumed from each slot */
         int i = 0;
         uint32_t last_bar = 0, last_par = 0;
         bool any = false;
@@ -717,9 +721,12 @@ __global__ void __launch_bounds__(kPThreads, 1) k_gemm_tcp(const GemmTask *__res
             ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
             if (!ok) break;
             const int nstep = (K + kTcK - 1) / kTcK;
-            for (int st = 0; st < nstep; st++, c++) {
-                const int s = (int)(c & 1);
-                if (lane == 0) ok = wait(full(s), (uint32_t)((c >> 1) & 1));
+            const int s = i & 1;      /* the slot of the producer group of this tile's parity */
+            const long long ub = s ? used1 : used0;
+            if (s) used1 += nstep; else used0 += nstep;
+            for (int st = 0; st < nstep; st++) {
+                const uint32_t par = (uint32_t)((ub + st) & 1);
+                if (lane == 0) ok = wait(full(s), par);
                 ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
                 if (!ok) break;
                 if (lane == 0) {
@@ -736,7 +743,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_gemm_tcp(const GemmTask *__res
                         }
                     umma::mma_commit(empty(s));
                     last_bar = empty(s);
-                    last_par = (uint32_t)((c >> 1) & 1);
+                    last_par = par;
                     any = true;
                 }
                 __syncwarp();
