@@ -1658,6 +1658,7 @@ static int enqueue_typed(KState *ks, const double *den, cudaStream_t s)
 /* K of one density on device arrays; mixed = FP32 contractions (FP64 K). */
 static int enqueue_exchange(KState *ks, const double *den, double *K, cudaStream_t s, bool timed, bool mixed)
 {
+    (void)cudaGetLastError();   /* a stale error of an earlier, handled runtime call is not ours */
     const int nbf = ks->nbf;
     if (mixed) {
         int rc = ensure_f32(ks);

@@ -2067,6 +2067,9 @@ static int launch_near_field(DevRep *d, const VecArgs &va, int nvec, bool timed 
  * the auxiliary stream). */
 int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t s, bool timed)
 {
+    /* an error an earlier runtime call left in this thread's error slot (and
+     * handled where it happened) must not be reported as one of ours */
+    (void)cudaGetLastError();
     int rc = ensure_work(d, nvec);
     if (rc) return rc;
     const size_t per_r = (size_t)d->rank_total * nvec, per_t = (size_t)d->lr_total * nvec;

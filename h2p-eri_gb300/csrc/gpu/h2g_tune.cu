@@ -228,7 +228,15 @@ extern "C" int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n)
         rc = apply_cfg(d, cand[i]);
         if (rc == 0) rc = time_matvec(d, n_den, &ms[i]);
         if (rc) {
+            const TuneCfg &c = cand[i];
+            const std::string why = std::string(H2ERI_gpu_last_error()) + " (autotune candidate " + std::to_string(i) +
+                                    ": tile rows " + std::to_string(c.chunk_rows) + ", tiles per CTA " +
+                                    std::to_string(c.tiles_per_cta) + ", lanes concurrent " +
+                                    std::to_string(c.nf_concurrent) + ", tensor-core kernel from " +
+                                    std::to_string(c.mma_min_vec) + " densities, CTA divisor " +
+                                    std::to_string(c.mma_grid_div) + ", persistent " + std::to_string(c.persist) + ")";
             (void)apply_cfg(d, start);
+            set_error(why);
             return -rc;
         }
         if (ms[i] < ms[best]) best = i;
