@@ -1854,14 +1854,17 @@ static int pack_mixed(DevRep *d)
     CUDA_TRY(cudaMemcpy(d->arena32x2, h32x2.data(), h32x2.size() * sizeof(float2), cudaMemcpyHostToDevice));
     int rc = mma_scales(d, h32, h32x2);
     if (rc) return rc;
-    rc = mma_make_slices(d);
-    if (rc) return rc;
     return build_tensor_maps(d);
 }
 
 int set_precision_mode(DevRep *d, H2ERI_p h, int mode)
 {
     (void)h;
+    if (mode == H2ERI_GPU_FP64 && d->arena == nullptr) {
+        set_error("the FP64 copy of this structure was dropped (H2ERI_gpu_drop_fp64); release it "
+                  "(H2ERI_gpu_release) and upload it again for the FP64 mode");
+        return 3;
+    }
     if (mode == H2ERI_GPU_MIXED) {
         int rc = pack_mixed(d);
         if (rc) return rc;
@@ -2096,7 +2099,12 @@ int enqueue_matvec(DevRep *d, int nvec, const double *x, double *y, cudaStream_t
     if (timed) CUDA_TRY(cudaEventRecord(d->ev_t[6], sm));
     /* several densities in the mixed mode: the tensor-core kernel, all
      * densities (up to 16 per pass) sharing each tile's slices */
-    const bool mma = d->precision == H2ERI_GPU_MIXED && nvec >= d->cfg.mma_min_vec && d->mslices != nullptr;
+    bool mma = d->precision == H2ERI_GPU_MIXED && nvec >= d->cfg.mma_min_vec;
+    if (mma && d->mslices == nullptr) {
+        rc = mma_make_slices(d);   /* first use of the tensor-core kernel */
+        if (rc) return rc;
+    }
+    mma = mma && d->mslices != nullptr;
     if (d->precision == H2ERI_GPU_MIXED && !mma && d->cfg.persist) {
         /* one persistent launch: tree chain and near field from one work list */
         if (timed) for (int k : {0, 6}) CUDA_TRY(cudaEventRecord(d->ev_t[k], sm));
@@ -2356,6 +2364,24 @@ extern "C" int H2ERI_gpu_upload(H2ERI_p h2eri)
     return get_rep(h2eri, &d);
 }
 
+/* Frees the FP64 copy of a structure that runs in the mixed mode (see the
+ * header). Returns 0, 3 outside the mixed mode, or another error code. */
+extern "C" int H2ERI_gpu_drop_fp64(H2ERI_p h2eri)
+{
+    DevRep *d;
+    int rc = get_rep(h2eri, &d);
+    if (rc) return rc;
+    if (d->precision != H2ERI_GPU_MIXED) {
+        set_error("H2ERI_gpu_drop_fp64: the structure is not in the mixed mode");
+        return 3;
+    }
+    if (d->arena == nullptr) return 0;
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaFree(d->arena));
+    d->arena = nullptr;
+    return 0;
+}
+
 extern "C" void H2ERI_gpu_release(H2ERI_p h2eri)
 {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -2457,6 +2483,11 @@ extern "C" int H2ERI_build_Coulomb_batch(int n, H2ERI_p *h2eris, const int *n_de
     cudaStream_t s = (cudaStream_t)stream;
     /* mixed mode with at most 16 densities per structure: every structure's
      * tiles in shared tensor-core launches, phase by phase */
+    for (int i = 0; i < n; i++)   /* slices of the structures that will run the tensor-core kernel */
+        if (reps[i]->precision == H2ERI_GPU_MIXED && n_den[i] >= reps[i]->cfg.mma_min_vec && n_den[i] <= 16) {
+            const int rc = mma_make_slices(reps[i]);
+            if (rc) return rc;
+        }
     if (const int kind = batch_merged_kind(n, reps.data(), n_den))
         return batch_coulomb_merged(kind, n, reps.data(), n_den, d_dens, d_Js, s);
     for (int i = 0; i < n; i++) {

@@ -672,11 +672,14 @@ int mma_init(DevRep *d)
     return 0;
 }
 
-/* Pre-computed slices of every tile (first use of the mixed mode, after the
- * mixed arenas and the tiles' exponents are on the device). */
+/* Pre-computed slices of every tile, made on the first use of the
+ * tensor-core kernel (a launch with at least mma_min_vec densities, or the
+ * autotuner trying it), after the mixed arenas and the tiles' exponents are
+ * on the device: about 8 bytes per stored element, which a structure that
+ * never runs several densities per launch does not hold. */
 int mma_make_slices(DevRep *d)
 {
-    if (d->n_mtiles == 0) return 0;
+    if (d->n_mtiles == 0 || d->mslices != nullptr) return 0;
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) { if (e == cudaSuccess && x != cudaSuccess) e = x; };
     chk(cudaMalloc(&d->mslices, std::max<size_t>(d->mslice_bytes, 16)));

@@ -190,7 +190,14 @@ extern "C" int H2ERI_gpu_autotune(H2ERI_p h2eri, int n_den, double *out, int n)
     const TuneCfg start = d->cfg;
     std::vector<TuneCfg> cand;
     const bool mixed = d->precision == H2ERI_GPU_MIXED;
-    const bool multi = mixed && n_den >= 2 && d->mslices != nullptr;
+    /* the tensor-core kernel is a candidate where the current choices allow
+     * it for this density count (its slices are made for the trial) */
+    bool multi = mixed && n_den >= 2 && start.mma_min_vec <= n_den;
+    if (multi) {
+        rc = mma_make_slices(d);
+        if (rc) return -rc;
+        multi = d->mslices != nullptr;
+    }
     cand.push_back(start);   /* the current choices first */
     if (multi) {
         for (int div : {1, 2})

@@ -103,6 +103,7 @@ SIGNATURES = {
     "H2ERI_gpu_selftest_persist_timeout": (ctypes.c_int, [_vp, ctypes.c_longlong]),
     "H2ERI_gpu_setup_eri_check": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
     "H2ERI_gpu_setup_u_check": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "H2ERI_gpu_drop_fp64": (ctypes.c_int, [_vp]),
     "H2ERI_save_representation": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "H2ERI_load_representation": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
 }

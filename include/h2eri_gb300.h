@@ -78,6 +78,14 @@ void H2ERI_gpu_release(H2ERI_p h2eri);
 /* Select the far-field precision for subsequent calls (default FP64).
  * Re-uploads the far-field blocks if needed. Returns 0 on success. */
 int H2ERI_gpu_set_precision(H2ERI_p h2eri, int mode);
+/* Device memory (no counterpart in the reference): a structure in the mixed
+ * mode reads only its FP32 / float-pair copy and the tensor-core slices, so
+ * its FP64 copy (about 40 % of its device footprint) can be freed, e.g. to
+ * keep a large batch of molecules resident in HBM. Afterwards the structure
+ * refuses H2ERI_gpu_set_precision(.., FP64) with an error; H2ERI_gpu_release
+ * and a new upload bring the FP64 mode back. Returns 0, or 3 when the
+ * structure is not in the mixed mode. */
+int H2ERI_gpu_drop_fp64(H2ERI_p h2eri);
 /* Message of the last failure of any gpu extension call on this thread
  * ("" if none). */
 const char *H2ERI_gpu_last_error(void);

@@ -307,3 +307,37 @@ def test_persistent_launch_against_range_launches(oracle_lib, library, monkeypat
                 assert relerr(out[(persist, nd)][i], Jo[i]) < TOL_MIXED, (persist, nd, i)
     for nd in (1, 3):
         assert relerr(out[("1", nd)], out[("0", nd)]) < 1e-13
+
+
+def test_drop_fp64_copy(oracle_lib, library, tmp_path):
+    """H2ERI_gpu_drop_fp64: a structure in the mixed mode keeps giving the
+    same J after its FP64 copy is freed, the device's free memory grows by
+    about that copy, the FP64 mode is refused until the structure is
+    released and uploaded again, and then FP64 J matches the oracle."""
+    torch = pytest.importorskip("torch")
+    p = str(tmp_path / "c6.mol")
+    hg.molecules.write_alkane(p, 6)
+    h = hg.H2ERI.from_mol(p, qr_tol=1e-6)
+    try:
+        D = hg.molecules.seeded_density(h.num_bf, 20, 77)
+        Jo = np.zeros_like(D)
+        oracle_lib.oracle_build_Coulomb(h.handle, D.ctypes.data, Jo.ctypes.data)
+        assert library.H2ERI_gpu_drop_fp64(h.handle) == 3          # FP64 mode: refused
+        h.set_precision(hg.MIXED)
+        J1 = h.build_coulomb(D)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        assert library.H2ERI_gpu_drop_fp64(h.handle) == 0
+        free1 = torch.cuda.mem_get_info()[0]
+        arena = h.report()["arena_U"] + h.report()["arena_B"] + h.report()["arena_D"]
+        assert free1 - free0 >= 0.9 * arena, (free1 - free0, arena)
+        assert library.H2ERI_gpu_drop_fp64(h.handle) == 0          # idempotent
+        J2 = h.build_coulomb(D)
+        assert relerr(J2, J1) < 1e-14 and relerr(J2, Jo) < 1e-8
+        assert library.H2ERI_gpu_set_precision(h.handle, hg.FP64) == 3
+        assert b"dropped" in library.H2ERI_gpu_last_error()
+        library.H2ERI_gpu_release(h.handle)
+        h.set_precision(hg.FP64)
+        assert relerr(h.build_coulomb(D), Jo) < 1e-12
+    finally:
+        h.destroy()
