@@ -57,9 +57,13 @@ struct BatchPlan {
     void *maps = nullptr;
     BatchMol *mols = nullptr;
     std::vector<Range> phases;          /* launch order (pair: float-pair format, single-density plan) */
+    int nf_phases = 0;                  /* the first nf_phases are the near field (own stream) */
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int n_tiles = 0;
     ~BatchPlan()
     {
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
         cudaFree(tiles);
         cudaFree(scales);
         cudaFree(stiles);
@@ -140,6 +144,7 @@ int build_plan_simt(int n, DevRep *const *reps, const int *n_den, BatchPlan *p)
             return v;
         });
     }
+    p->nf_phases = (int)p->phases.size();
     size_t nf = 0, nb = 0;
     for (int i = 0; i < n; i++) {
         nf = std::max(nf, reps[i]->fwd.size());
@@ -230,6 +235,7 @@ int build_plan(bool simt, int n, DevRep *const *reps, const int *n_den, BatchPla
             for (int ln = 0; ln < kNfLanes; ln++) v.push_back(&d->mden[ln * 3 + s]);
             return v;
         });
+    p->nf_phases = (int)p->phases.size();
     size_t nf = 0, nb = 0;
     for (int i = 0; i < n; i++) {
         nf = std::max(nf, reps[i]->mfwd.size());
@@ -272,14 +278,16 @@ int build_plan(bool simt, int n, DevRep *const *reps, const int *n_den, BatchPla
 }  // namespace
 
 /* 1: every structure runs the tensor-core kernel at its density count (its
- * own choice, default or tuned); 2: every structure runs the mixed
- * single-density kernels and all have the same density count; 0: neither
- * (each structure then runs on its own streams). */
+ * own choice, default or tuned); 2 (only with H2G_BATCH_MERGED=1): every
+ * structure runs the mixed single-density kernels and all have the same
+ * density count; 0: otherwise (each structure then runs on its own
+ * streams). */
 int batch_merged_kind(int n, DevRep *const *reps, const int *n_den)
 {
     if (n < 1) return 0;
-    if (const char *e = std::getenv("H2G_BATCH_MERGED"))
-        if (std::strcmp(e, "0") == 0) return 0;
+    const char *e = std::getenv("H2G_BATCH_MERGED");
+    if (e != nullptr && std::strcmp(e, "0") == 0) return 0;
+    const bool force = e != nullptr && std::strcmp(e, "1") == 0;
     bool mma = true, simt = true;
     for (int i = 0; i < n; i++) {
         const DevRep *d = reps[i];
@@ -288,7 +296,10 @@ int batch_merged_kind(int n, DevRep *const *reps, const int *n_den)
         if (n_den[i] >= d->cfg.mma_min_vec && d->mslices != nullptr) simt = false;
         if (n_den[i] != n_den[0]) simt = false;
     }
-    return mma ? 1 : (simt ? 2 : 0);
+    /* the single-density kernels' shared launches (kind 2) ran 7 % slower
+     * than every structure on its own streams (64 alkanes C9..C59, two
+     * densities each: 70.7 against 65.2 ms), so they run only on request */
+    return mma ? 1 : (simt && force ? 2 : 0);
 }
 
 void batch_forget(const DevRep *d)
@@ -331,15 +342,31 @@ int batch_coulomb_merged(int kind, int n, DevRep *const *reps, const int *n_den,
         int rc = enqueue_uncontract(d, n_den[i], d_dens[i], s);
         if (rc) return rc;
     }
-    for (const Range &r : p->phases) {
+    /* the near-field phases on the first structure's low-priority stream,
+     * beside the tree phases on s (as in the single-structure path: the near
+     * field depends only on x, and its tiles fill the SMs the short tree
+     * levels leave idle) */
+    BatchPlan *pm = g_bplan;
+    if (pm->ev_fork == nullptr) {
+        BCUDA_TRY(cudaEventCreateWithFlags(&pm->ev_fork, cudaEventDisableTiming));
+        BCUDA_TRY(cudaEventCreateWithFlags(&pm->ev_join, cudaEventDisableTiming));
+    }
+    cudaStream_t aux = reps[0]->s_aux;
+    BCUDA_TRY(cudaEventRecord(pm->ev_fork, s));
+    BCUDA_TRY(cudaStreamWaitEvent(aux, pm->ev_fork, 0));
+    for (size_t k = 0; k < p->phases.size(); k++) {
+        const Range &r = p->phases[k];
+        cudaStream_t ls = (int)k < p->nf_phases ? aux : s;
         if (simt)
             launch_batch_mx(p->stiles + r.first, r.count, r.pair, p->maps, p->mols, n_den[0],
-                            reps[0]->cfg.tiles_per_cta, reps[0]->err_flag_dev, s);
+                            reps[0]->cfg.tiles_per_cta, reps[0]->err_flag_dev, ls);
         else
             launch_batch_mma(p->tiles + r.first, p->scales + (size_t)r.first * 256, p->mols, r.count,
-                             reps[0]->mma_levels, reps[0]->n_sm, reps[0]->err_flag_dev, s);
+                             reps[0]->mma_levels, reps[0]->n_sm, reps[0]->err_flag_dev, ls);
     }
     BCUDA_TRY(cudaGetLastError());
+    BCUDA_TRY(cudaEventRecord(pm->ev_join, aux));
+    BCUDA_TRY(cudaStreamWaitEvent(s, pm->ev_join, 0));
     for (int i = 0; i < n; i++) {
         int rc = enqueue_contract(reps[i], n_den[i], d_Js[i], s);
         if (rc) return rc;
