@@ -52,3 +52,24 @@ def test_exchange_plan_in_bounds(small_mols, alk26, library, device_bytes):
         rc = library.H2ERI_exchange_plan_check(h.handle, device_bytes, out.ctypes.data, 5)
         assert rc == 0, library.H2ERI_gpu_last_error()
         assert out[0] > 0 and out[1] >= 1 and out[4] > 0
+
+
+def test_exchange_plan_in_bounds_3d_cluster(library, tmp_path):
+    """The same on a 3-D system (8 CH4 on a jittered lattice: every node has
+    neighbours on all sides), with the work tensors in one range, a few and
+    many ranges of n."""
+    import h2eri_gb300 as hg
+    p = str(tmp_path / "ch4x8.mol")
+    hg.molecules.write_methane_cluster(p, shape=(2, 2, 2))
+    h = hg.H2ERI.from_mol(p, qr_tol=1e-7)
+    try:
+        ranges = []
+        for device_bytes in (100e9, 2e8, 2e6):
+            out = np.zeros(5)
+            rc = library.H2ERI_exchange_plan_check(h.handle, device_bytes, out.ctypes.data, 5)
+            assert rc == 0, library.H2ERI_gpu_last_error()
+            assert out[0] > 0 and out[4] > 0
+            ranges.append(out[1])
+        assert ranges[0] == 1 and ranges[2] > ranges[1] > 1
+    finally:
+        h.destroy()
