@@ -922,6 +922,7 @@ struct KState {
     KVariant v64, v32, vtc;        /* FP64, FP32 SIMT, FP32 on the tensor cores */
     int use_tc = 1;               /* mixed mode: 1 persistent tensor-core kernel, 2 one tile per CTA, 0 FP32 SIMT (H2G_K_TC) */
     int n_sm = 1;
+    bool f32_ready = false;       /* FP32 arena, density buffer and the task list of use_tc uploaded */
     unsigned *err_dev = nullptr;  /* the structure's kernel error word (device address) */
     NearTask *near = nullptr;
     long long *near_start = nullptr;
@@ -1067,22 +1068,29 @@ static int upload_variant(KState *ks, bool tc = false)
 /* FP32 arena, density and task list, made on the first mixed-mode K build. */
 static int ensure_f32(KState *ks)
 {
-    if (ks->v32.tasks != nullptr) return 0;
-    KCUDA_TRY(cudaMalloc(&ks->arena32, ks->arena_elems * sizeof(float)));
-    k_to_f32<<<1216, 256>>>(ks->arena, ks->arena32, (long long)ks->arena_elems);
-    KCUDA_TRY(cudaGetLastError());
-    KCUDA_TRY(cudaMalloc(&ks->dp32, (size_t)ks->nbf * ks->nbf * sizeof(float)));
+    if (ks->f32_ready) return 0;
+    if (ks->arena32 == nullptr) {
+        KCUDA_TRY(cudaMalloc(&ks->arena32, ks->arena_elems * sizeof(float)));
+        k_to_f32<<<1216, 256>>>(ks->arena, ks->arena32, (long long)ks->arena_elems);
+        KCUDA_TRY(cudaGetLastError());
+    }
+    if (ks->dp32 == nullptr) KCUDA_TRY(cudaMalloc(&ks->dp32, (size_t)ks->nbf * ks->nbf * sizeof(float)));
     KCUDA_TRY(cudaDeviceSynchronize());
     if (const char *e = std::getenv("H2G_K_TC")) ks->use_tc = std::min(2, std::max(0, std::atoi(e)));
     int dev = 0;
     KCUDA_TRY(cudaGetDevice(&dev));
     KCUDA_TRY(cudaDeviceGetAttribute(&ks->n_sm, cudaDevAttrMultiProcessorCount, dev));
-    int rc = upload_variant<float>(ks);
-    if (rc == 0 && ks->use_tc) {
+    /* only the task list of the kernel in use (a large 3-D plan holds
+     * millions of tasks) */
+    KVariant &w = ks->use_tc ? ks->vtc : ks->v32;
+    for (void *q : {(void *)w.tasks, (void *)w.tile_start, (void *)w.tile_task}) cudaFree(q);
+    w.tasks = nullptr; w.tile_start = nullptr; w.tile_task = nullptr;
+    if (ks->use_tc) {
         KCUDA_TRY(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemLaunch));
         KCUDA_TRY(cudaFuncSetAttribute(k_gemm_tcp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmemLaunch));
-        rc = upload_variant<float>(ks, true);
     }
+    const int rc = upload_variant<float>(ks, ks->use_tc != 0);
+    if (rc == 0) ks->f32_ready = true;
     return rc;
 }
 
@@ -1633,7 +1641,6 @@ static int enqueue_typed(KState *ks, const double *den, cudaStream_t s)
     for (const KChunk &ch : ks->chunks) {
         KCUDA_TRY(cudaMemsetAsync(ks->gh, 0, ch.gh_elems * sizeof(T), s));
         for (const KGroup &g : ch.groups) {
-            const long long tiles = v.group_tiles[gi];
             if (std::is_same<T, float>::value && ks->use_tc) {
                 const KVariant &w = ks->vtc;
                 const long long nt = w.group_tiles[gi];
@@ -1645,9 +1652,9 @@ static int enqueue_typed(KState *ks, const double *den, cudaStream_t s)
                     k_gemm_tc<<<(unsigned)nt, kTcThreads, kTcSmemLaunch, s>>>(
                         w.tasks + g.t0, w.tile_start + w.group_pre[gi], g.nt, w.tile_task + w.group_tile_off[gi],
                         ks->err_dev);
-            } else if (tiles > 0) {
-                k_gemm<T><<<(unsigned)tiles, GemmCfg<T>::NT, 0, s>>>(v.tasks + g.t0, v.tile_start + v.group_pre[gi], g.nt,
-                                                                      v.tile_task + v.group_tile_off[gi]);
+            } else if (v.group_tiles[gi] > 0) {
+                k_gemm<T><<<(unsigned)v.group_tiles[gi], GemmCfg<T>::NT, 0, s>>>(
+                    v.tasks + g.t0, v.tile_start + v.group_pre[gi], g.nt, v.tile_task + v.group_tile_off[gi]);
             }
             gi++;
         }
@@ -1809,7 +1816,7 @@ extern "C" int H2ERI_gpu_exchange_report(H2ERI_p h2eri, double *out, int n)
     if (rc) return -rc;
     double vals[7] = {ks->flops, (double)ks->last_ms, (double)ks->chunks.size(),
                       (double)ks->gh_elems * sizeof(double), (double)ks->near_items, (double)launches_per_build(ks),
-                      ks->v32.tasks == nullptr ? -1.0 : (double)(ks->use_tc != 0)};
+                      !ks->f32_ready ? -1.0 : (double)(ks->use_tc != 0)};
     int m = std::min(n, 7);
     for (int i = 0; i < m; i++) out[i] = vals[i];
     return m;
