@@ -1206,6 +1206,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
         return (int)(std::lower_bound(v.begin(), v.end(), x) - v.begin());
     };
 
+    const double t_sets = secs();
     PlanBuilder pb;
     const long long P_row = pb.put(e_row), P_x = pb.put(e_x);
     (void)pb.put(e_y);
@@ -1438,6 +1439,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
         ks->chunks.push_back(ch);
     }
 
+    const double t_tasks = secs();
     /* ---- tile counts and flops ---- */
     for (KChunk &ch : ks->chunks)
         for (KGroup &g : ch.groups)
@@ -1468,6 +1470,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
 
     ks->near_items = near_pre.back();
 
+    const double t_count = secs();
     /* ---- bounds of every access, checked before anything is launched ---- */
     const size_t nbf2 = (size_t)nbf * nbf;
     for (const HTask &T : expand)
@@ -1511,6 +1514,9 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
                 }
     }
     const double t_plan = secs();
+    if (verbose)
+        std::fprintf(stderr, "kplan (host): rows and column sets %.2f s, tasks %.2f s, tile counts %.2f s, bounds "
+                     "check %.2f s\n", t_sets, t_tasks - t_sets, t_count - t_tasks, t_plan - t_count);
     if (!upload) return 0;
 
     /* ---- upload ---- */
