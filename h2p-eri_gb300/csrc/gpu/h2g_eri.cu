@@ -1025,9 +1025,9 @@ static int u_blocks_range(EriSet *s, Tables *t, UReq *reqs, size_t n_req)
             return rc;
         }
     }
-    if (!jobs.empty()) {
-        dim3 grid(64, (unsigned)jobs.size());
-        k_sketch<<<grid, 256, 0, sn>>>(djobs, dX, dscol, dsval, dA);
+    for (size_t j0 = 0; j0 < jobs.size(); j0 += 65535) {   /* grid.y is at most 65535 */
+        dim3 grid(64, (unsigned)std::min<size_t>(65535, jobs.size() - j0));
+        k_sketch<<<grid, 256, 0, sn>>>(djobs + j0, dX, dscol, dsval, dA);
         if (cudaGetLastError() != cudaSuccess) return fail_s("sketch kernel launch");
     }
     if (cudaStreamSynchronize(sn) != cudaSuccess) return fail_s("kernels");
