@@ -1094,9 +1094,15 @@ static int ensure_f32(KState *ks)
     return rc;
 }
 
+/* Default cap of the G / H work tensors (bytes, sized for FP64): with 40 %
+ * of the free memory as the other bound. C30H62's mixed K build: 5 n ranges
+ * under a 16 GB cap 238 ms, 3 ranges (25-32 GB) 227 ms, 2 ranges 228 ms, one
+ * range (80 GB) 233 ms. */
+constexpr double kWorkCap = 32e9;
+
 /* free_bytes: device memory the G / H work tensors may be sized against;
  * upload = false builds and checks the plan on the host only. */
-static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
+static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload, double cap_bytes = kWorkCap)
 {
     const auto tp0 = std::chrono::steady_clock::now();
     auto secs = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - tp0).count(); };
@@ -1250,7 +1256,7 @@ static int build_kplan(H2ERI_p h, KState *ks, size_t free_bytes, bool upload)
     double full = 0.0;
     for (int j = 0; j < n_node; j++)
         if (has_far(j)) full += 2.0 * (double)S[j].size() * rank[j] * nbf;
-    const double budget = std::max(1e6, std::min(16e9, 0.4 * (double)free_bytes) / sizeof(double));
+    const double budget = std::max(1e6, std::min(cap_bytes, 0.4 * (double)free_bytes) / sizeof(double));
     int nchunk = (int)std::ceil(full / budget);
     nchunk = std::max(1, std::min(nchunk, nbf));
 
@@ -1711,8 +1717,12 @@ static int get_kstate(H2ERI_p h, DevRep **d, KState **out)
         (*d)->kstate = k;
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
-        if ((*d)->k_work_bytes > 0) free_b = (size_t)((*d)->k_work_bytes / 0.4);
-        rc = build_kplan(h, k, free_b, true);
+        double cap = kWorkCap;   /* an explicit budget replaces the default cap */
+        if ((*d)->k_work_bytes > 0) {
+            free_b = (size_t)((*d)->k_work_bytes / 0.4);
+            cap = (*d)->k_work_bytes;
+        }
+        rc = build_kplan(h, k, free_b, true, cap);
         if (cur != (*d)->device && cur >= 0) cudaSetDevice(cur);
         if (rc) {
             free_exchange_state(*d);
