@@ -693,7 +693,7 @@ struct SetupEri {
     EriSet *es = nullptr;
     bool failed = false;
 };
-static SetupEri g_seri;
+static thread_local SetupEri g_seri;   /* per calling thread: set-ups of different structures may run at once */
 
 EriSet *setup_eri(H2ERI_p h)
 {
