@@ -127,7 +127,7 @@ def representation(hg, molecules, rank, ws, barrier):
         tmp = path + ".tmp"
         h.save(tmp)
         os.replace(tmp, path)
-        log(f"set-up (host, not timed): {setup_s:.1f} s")
+        log(f"set-up (not timed): {setup_s:.1f} s")
     else:
         h = None
     barrier()
@@ -336,7 +336,7 @@ def run_reference_exchange(args):
 
 
 def run_setup(args):
-    """--path setup: seconds per host set-up of the workload's molecule
+    """--path setup: seconds per set-up of the workload's molecule
     (H2ERI_init, CMS_read_mol_file, H2ERI_process_shells, H2ERI_partition,
     H2ERI_build_H2; OpenMP over the host cores). With --impl reference: the
     reference's own set-up, compiled from its sources (the integral engine of
@@ -373,7 +373,8 @@ def run_setup(args):
         one()
         times.append(time.perf_counter() - t0)
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    out = {"metric": f"host set-up seconds {WORKLOAD['molecule']} (H2ERI_build_H2 and the calls before it)",
+    out = {"metric": f"set-up seconds {WORKLOAD['molecule']} (H2ERI_build_H2 and the calls before it; integrals on "
+                     f"the GPU when one is present, decompositions on the host)",
            "value": statistics.median(times), "unit": "s", "higher_is_better": False, "steps": steps,
            "warmup": 1, "samples_s": [round(t, 3) for t in times], "cores": cores, "dtype": "f64",
            "data": f"synthetic (generated {geometry_kind()} geometry)", "config": dict(WORKLOAD)}
