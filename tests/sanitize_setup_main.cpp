@@ -12,7 +12,7 @@
 
 extern "C" void H2ERI_gpu_release(H2ERI_p) {}
 extern "C" void h2g_gpu_print_statistic(H2ERI_p) {}
-extern "C" const char *H2ERI_gpu_last_error(void) { return "no GPU in this build"; }
+extern "C" const char *H2ERI_gpu_last_error(void) { return "the GPU hooks are stubbed in this test program"; }
 namespace h2g {
 int gpu_eri_usable() { return 0; }
 int gpu_eri_create(int, const h2g_pair *const *, EriSet **out) { *out = nullptr; return 1; }
